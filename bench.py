@@ -1,0 +1,432 @@
+#!/usr/bin/env python
+"""Benchmark of the GP hot path on one GB300: large full GP regression.
+
+Workload (the headline configuration): n = 16384 training points, d = 8,
+x ~ U[-1, 1]^8, y = draw from cf_matern52(lscale 0.7, magn 1) + cf_const(1)
+plus N(0, 0.05^2) noise; lik_gaussian, method_full. One step = one
+gp_energy + gradient evaluation (a full fit: covariance, blocked Cholesky,
+solves, evidence, then the gradient: triangular inverse, B^-1, contraction)
+at the next hyperparameters of a fixed 20-point sequence, as gp_optim would
+request them. Data are synthetic (numpy seeded); the matrices (2.1 GB each)
+are far larger than L2, so no flush is needed between steps.
+
+Prints one JSON line (rank 0). ``--impl reference`` times the CPU
+restatement of the reference (R is not available) on the same workload.
+Multi-GPU (``--gpus N`` under torchrun): replicas only -- the factorisation of
+one n = 16384 problem does not shard; every rank runs the same steps on its
+own GPU and the value is the total over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FULL = 16384
+D = 8
+SIGMA = 0.05
+LSCALE, MAGN, CMAGN = 0.7, 1.0, 1.0
+NPRED = 8192
+
+
+def theta_sequence(k):
+    """Log-hyperparameters of step k: [log lscale, log magn, log const magn, log sigma]."""
+    base = np.log([LSCALE, MAGN, CMAGN, SIGMA])
+    return base + 0.05 * np.sin((k % 20 + 1) * np.arange(1, 5))
+
+
+def make_data(n, seed=2):
+    """x ~ U[-1,1]^8; y = GP draw (matern52 + const) + noise. The draw uses a Cholesky
+    of the prior covariance computed with torch on the GPU when available (setup only)."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (n, D))
+    zn = rng.standard_normal(n)
+    eps = rng.standard_normal(n)
+    try:
+        import torch
+        if torch.cuda.is_available():
+            dev = torch.device("cuda")
+            X = torch.from_numpy(x).to(dev)
+            r = torch.cdist(X, X)
+            a = math.sqrt(5.0) * r / LSCALE
+            K = MAGN ** 2 * (1 + a + a * a / 3) * torch.exp(-a) + CMAGN ** 2
+            K.diagonal().add_(1e-6)
+            L = torch.linalg.cholesky(K)
+            f = (L @ torch.from_numpy(zn).to(dev)).cpu().numpy()
+            del X, r, a, K, L
+            torch.cuda.empty_cache()
+            return x, f + SIGMA * eps
+    except Exception:
+        pass
+    from scipy.spatial.distance import cdist
+    r = cdist(x, x)
+    a = math.sqrt(5.0) * r / LSCALE
+    K = MAGN ** 2 * (1 + a + a * a / 3) * np.exp(-a) + CMAGN ** 2
+    K[np.diag_indices(n)] += 1e-6
+    f = np.linalg.cholesky(K) @ zn
+    return x, f + SIGMA * eps
+
+
+# ----------------------------------------------------------------------------
+# CPU leg: the oracle (restatement of gplite's R path) + the same gradient
+# ----------------------------------------------------------------------------
+
+def cpu_energy_grad(x, y, theta):
+    """One energy + gradient on the CPU: the oracle's gp_fit (B factorisation,
+    R/laplace.R:13-39) plus the gradient 1/2 tr((aa^T - C^-1) dC) in numpy."""
+    from oracle import gplite_ref as R
+    from scipy import linalg as sla
+    ls, mg, cm, sg = np.exp(theta)
+    gp = R.gp_init([R.cf("matern52", lscale=ls, magn=mg), R.cf("const", magn=cm)], R.lik("gaussian", sigma=sg))
+    gp = R.gp_fit(gp, x, y)
+    n = len(y)
+    Lc = gp.fit["C_chol"]
+    alpha = gp.fit["alpha"]
+    Ci = sla.cho_solve((Lc, True), np.eye(n))
+    W = np.outer(alpha, alpha) - Ci
+    del Ci
+    from scipy.spatial.distance import cdist
+    a = math.sqrt(5.0) * cdist(x, x) / ls
+    e = np.exp(-a)
+    dls = mg * mg * a * a * (1 + a) / 3 * e
+    dm = 2 * mg * mg * (1 + a + a * a / 3) * e
+    g = np.array([0.5 * (W * dls).sum(), 0.5 * (W * dm).sum(), 0.5 * W.sum() * 2 * cm * cm,
+                  sg * sg * (alpha @ alpha - np.trace(sla.cho_solve((Lc, True), np.eye(n))))])
+    return gp.fit["log_evidence"], g
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """--impl reference: the reference's path on the host cores (R is unavailable,
+    so the oracle restatement, all threads)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n = args.cpu_n
+    x, y = make_data(n, seed=2)
+    for k in range(args.warmup):
+        cpu_energy_grad(x, y, theta_sequence(k))
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        cpu_energy_grad(x, y, theta_sequence(args.warmup + k))
+    t = (time.perf_counter() - t0) / args.steps
+    scale = (N_FULL / n) ** 3
+    val = 1.0 / (t * scale)
+    line = {
+        "impl": "reference", "metric": "GP solves/s (energy+gradient, n=16384 full GP)", "value": val,
+        "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * scale * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (numpy seeded; GP draw matern52+const)",
+        "config": {"workload": "full GP regression energy+gradient, n=16384 d=8 matern52+const", "n": N_FULL,
+                   "d": D, "sample_n": n},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": "oracle fit + numpy gradient at n=%d per step (R unavailable), time "
+                                   "scaled by (16384/%d)^3" % (n, n)},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# clocks sampling during the timed region
+# ----------------------------------------------------------------------------
+
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self._t = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, s[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def fp64_peak_gflops(torch):
+    """Measured FP64 GEMM rate of this GPU (cuBLAS DGEMM, 8192^3, best of 3): the FP64 peak
+    used as the denominator of the plain path's roofline (the measured-peaks file has no FP64)."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2 * 8192 ** 3 / best / 1e9
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from gplite_gb300 import _lib as L
+    from gplite_gb300.gp import kernel_struct
+    import gplite_gb300 as G
+
+    lib = L.load()
+    ctx = L.Context(local)
+    n = args.n
+    x, y = make_data(n, seed=2 + rank * 0)
+    xf = np.asfortranarray(x)
+    # x column-major on the device: the memory of a row-major (d, n) array
+    xd = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    yd = torch.from_numpy(y).cuda()
+    prec = L.PRECISION[args.precision]
+
+    def specs(theta):
+        ls, mg, cm, sg = np.exp(theta)
+        cfs = [G.cf_matern52(lscale=ls, magn=mg), G.cf_const(magn=cm)]
+        k = kernel_struct(cfs, D)
+        lk = L.Lik()
+        lk.kind, lk.link, lk.sigma = 0, 0, sg
+        me = L.Method()
+        ap = L.Approx()
+        ap.kind, ap.maxiter, ap.tol = 0, 30, 1e-4
+        op = L.FitOpts()
+        op.jitter, op.precision, op.refine_iters = 1e-6, prec, 2
+        return k, lk, me, ap, op
+
+    gt = np.zeros(2 * L.TERM_NPARAM)
+    gs = C.c_double()
+
+    def step_dev(k):
+        kk, lk, me, ap, op = specs(theta_sequence(k))
+        h = C.c_void_p()
+        res = L.FitResult()
+        st = lib.gpgp_fit_dev(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
+                              C.c_void_p(xd.data_ptr()), n, D, C.c_void_p(yd.data_ptr()), None, None,
+                              C.byref(h), C.byref(res))
+        L.check(st, ctx.h)
+        st = lib.gpgp_model_grad(h, L.ptr(gt), C.byref(gs))
+        L.check(st, ctx.h)
+        lib.gpgp_model_free(h)
+        return res.log_evidence
+
+    yh = np.ascontiguousarray(y)
+
+    def step_host(k):
+        kk, lk, me, ap, op = specs(theta_sequence(k))
+        h = C.c_void_p()
+        res = L.FitResult()
+        st = lib.gpgp_fit(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
+                          L.ptr(xf), n, D, L.ptr(yh), None, None, C.byref(h), C.byref(res))
+        L.check(st, ctx.h)
+        st = lib.gpgp_model_grad(h, L.ptr(gt), C.byref(gs))
+        L.check(st, ctx.h)
+        lib.gpgp_model_free(h)
+        return res.log_evidence
+
+    def barrier():
+        torch.cuda.synchronize()
+        ctx.sync()
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    stream = torch.cuda.ExternalStream(lib.gpgp_stream(ctx.h))
+    # warm-up
+    for k in range(args.warmup):
+        step_dev(k)
+    barrier()
+    # timed: device-resident inputs
+    lib.gpgp_profile_enable(ctx.h, 1)
+    launches0 = L.launch_count()
+    clk = ClockSampler(local)
+    clk.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    lmls = []
+    for k in range(args.steps):
+        lmls.append(step_dev(args.warmup + k))
+    ev1.record(stream)
+    barrier()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    launches = L.launch_count() - launches0
+    ms = np.zeros(8)
+    calls = np.zeros(8, dtype=np.int64)
+    lib.gpgp_profile_read(ctx.h, L.ptr(ms), calls.ctypes.data_as(C.c_void_p))
+    lib.gpgp_profile_enable(ctx.h, 0)
+    t_step = max_over_ranks(dev_s) / args.steps
+    value = world / t_step
+
+    # e2e through the host-buffer C ABI call (copies inside the timed region)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step_host(args.warmup + k)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0) / args.steps
+    h2d = xf.nbytes + yh.nbytes
+    d2h = 8 * (1 + gt.size + 1)
+
+    out = None
+    if rank == 0:
+        phases = {nm: {"ms_total": float(ms[i]), "calls": int(calls[i])} for i, nm in enumerate(L.PHASES)}
+        peaks = measured_peaks()
+        if args.precision == "fp64":
+            fp64 = fp64_peak_gflops(torch)
+            t_potrf = ms[1] / max(calls[1], 1) / 1e3
+            achieved = (n ** 3 / 3) / t_potrf / 1e12
+            roof = {"bound": "fp64", "kernel": "blocked potrf (gemm64_kernel trailing updates)",
+                    "achieved": achieved, "peak": fp64 / 1e3, "unit": "TFLOP/s",
+                    "frac": achieved / (fp64 / 1e3),
+                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 is not in "
+                                   "MEASURED_PEAKS.json)",
+                    "traffic": None}
+        else:
+            bf = peaks.get("bf16_tflops", 1900.0)
+            t_potrf = ms[1] / max(calls[1], 1) / 1e3
+            achieved = (n ** 3 / 3) / t_potrf / 1e12
+            roof = {"bound": "tensor", "kernel": "blocked potrf, mixed", "achieved": achieved, "peak": bf,
+                    "unit": "TFLOP/s", "frac": achieved / bf, "peak_source": "MEASURED_PEAKS.json bf16_tflops",
+                    "traffic": None}
+        cpu = None
+        if not args.no_cpu and world == 1:
+            xs, ys = make_data(args.cpu_n, seed=2)
+            t0 = time.perf_counter()
+            cpu_energy_grad(xs, ys, theta_sequence(0))
+            tc = time.perf_counter() - t0
+            sc = (N_FULL / args.cpu_n) ** 3
+            cpu = {"value": 1.0 / (tc * sc), "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
+                   "sample": "one oracle fit + numpy gradient at n=%d (R unavailable), time scaled by "
+                             "(16384/%d)^3" % (args.cpu_n, args.cpu_n)}
+        out = {
+            "metric": "GP solves/s (energy+gradient, n=16384 full GP)", "value": value, "unit": "solves/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64 (bf16-split tensor updates)",
+            "data": "synthetic (numpy seeded; GP draw from matern52+const)",
+            "config": {"workload": "full GP regression energy+gradient, n=%d d=8 matern52+const, "
+                                   "lik_gaussian sigma 0.05, fixed 20-step theta sequence" % n,
+                       "n": n, "d": D, "precision": args.precision,
+                       "l2": "inputs larger than L2 (K and its factor are %.1f GB each)" % (n * n * 8 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+            "wall_s_timed": wall,
+            "phases_ms": phases,
+            "log_evidence_last": lmls[-1],
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--n", type=int, default=N_FULL)
+    ap.add_argument("--cpu-n", type=int, default=8192)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1022 @@
+// C ABI of libgpgp: contexts, models, and the host-side orchestration of the
+// GP hot path (fit / energy gradient / prediction / LOO) on one GPU.
+//
+// The iteration logic restates the reference's R loops: laplace.method_full
+// (R/laplace.R:274-297), laplace_iter.method_full (R/laplace.R:13-39),
+// ep.method_full (R/ep.R:286-330), ep_iter.method_full (R/ep.R:16-49),
+// gp_pred_post.method_full (R/gp_pred.R:202-232) and loo_posteriors
+// (R/gp_loo.R:119-133). All O(n^2) and O(n^3) work runs in the kernels of
+// cov.cu / dense.cu / lik.cu; the host only sequences launches and reads back
+// the few scalars the convergence tests need.
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace gpgp;
+
+struct gpgp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  double *h_pinned = nullptr;  // host pinned scalars
+  // live profiling: (phase, start event, stop event) per recorded interval
+  bool prof = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
+  double prof_ms[GPGP_NPHASE] = {0};
+  int64_t prof_calls[GPGP_NPHASE] = {0};
+};
+
+namespace {
+// Scoped phase timer: records a pair of events on the context stream when enabled.
+struct Phase {
+  gpgp_ctx *c;
+  int ph;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Phase(gpgp_ctx *ctx, int phase) : c(ctx), ph(phase) {
+    if (!c->prof) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, c->stream);
+  }
+  ~Phase() {
+    if (!c->prof || !a) return;
+    cudaEventRecord(b, c->stream);
+    c->prof_ev.push_back({ph, {a, b}});
+  }
+};
+
+void prof_collect(gpgp_ctx *c) {
+  for (auto &e : c->prof_ev) {
+    float ms = 0.f;
+    cudaEventSynchronize(e.second.second);
+    cudaEventElapsedTime(&ms, e.second.first, e.second.second);
+    c->prof_ms[e.first] += ms;
+    c->prof_calls[e.first] += 1;
+    cudaEventDestroy(e.second.first);
+    cudaEventDestroy(e.second.second);
+  }
+  c->prof_ev.clear();
+}
+}  // namespace
+
+namespace {
+
+// RAII device buffer on the context's stream-ordered pool.
+struct DBuf {
+  double *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { reset(); }
+  void alloc(cudaStream_t st, size_t count) {
+    reset();
+    s = st;
+    n = count;
+    if (count == 0) return;
+    cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(double), st);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+  }
+  void reset() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct IBuf {
+  int *p = nullptr;
+  cudaStream_t s = nullptr;
+  ~IBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  void alloc(cudaStream_t st, size_t count) {
+    s = st;
+    if (cudaMallocAsync((void **)&p, count * sizeof(int), st) != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+  }
+};
+
+}  // namespace
+
+struct gpgp_model {
+  gpgp_ctx *ctx = nullptr;
+  gpgp_kernel spec;
+  DevKernel dk;
+  std::vector<HostTermPrep> prep;
+  gpgp_lik lik;
+  LikDev lk;
+  gpgp_method method;
+  gpgp_approx approx;
+  gpgp_fit_opts opts;
+  int64_t n = 0;
+  int d = 0;
+  // inputs (owned copies)
+  DBuf x, y, trials, offset, F;
+  // full-method fit
+  DBuf L, Winv, s, alpha, fmean, z, V;
+  DBuf fvar, cav_mean, cav_var;  // EP
+  DBuf binv_diag;                // diag(B^-1), filled on demand
+  bool have_binv_diag = false;
+  bool has_trials = false, has_offset = false;
+  double log_evidence = 0.0;
+  int fitted = 0;
+};
+
+namespace {
+
+thread_local std::string tl_error;
+
+gpgp_status fail(gpgp_ctx *ctx, gpgp_status st, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  tl_error = msg;
+  return st;
+}
+
+template <class F>
+gpgp_status guarded(gpgp_ctx *ctx, F &&fn) {
+  try {
+    return fn();
+  } catch (const CudaError &e) {
+    std::string m = std::string("CUDA error ") + cudaGetErrorString(e.err) + " in " + e.what;
+    return fail(ctx, GPGP_ECUDA, m);
+  } catch (const std::bad_alloc &) {
+    return fail(ctx, GPGP_EOOM, "device or host allocation failed");
+  }
+}
+
+LikDev make_likdev(const gpgp_lik &l) {
+  LikDev d;
+  d.kind = l.kind;
+  d.link = l.link;
+  d.sigma = l.sigma;
+  d.phi = l.phi;
+  return d;
+}
+
+void copy_in(cudaStream_t s, DBuf &dst, const double *src, size_t count, bool src_on_device) {
+  dst.alloc(s, count);
+  if (count == 0) return;
+  GPGP_CUDA(cudaMemcpyAsync(dst.p, src, count * sizeof(double),
+                            src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+}
+
+double read_scalar(gpgp_ctx *ctx, const double *dptr) {
+  GPGP_CUDA(cudaMemcpyAsync(ctx->h_pinned, dptr, sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  GPGP_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ctx->h_pinned[0];
+}
+
+// ---------------------------------------------------------------------------
+// small elementwise kernels used only by the orchestration
+// ---------------------------------------------------------------------------
+__global__ void make_B_kernel(const double *__restrict__ K, int64_t n, const double *__restrict__ s,
+                              double *__restrict__ B) {
+  // B = I + diag(s) K diag(s), lower triangle (R/laplace.R:27: sqrt(1/V) * (K * sqrt(1/V)))
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    for (int64_t i = j + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const double v = s[i] * (K[i + j * n] * s[j]);
+      B[i + j * n] = (i == j) ? 1.0 + v : v;
+    }
+  }
+}
+
+__global__ void add_scalar_kernel(int64_t n, double a, double *__restrict__ v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] += a;
+}
+
+__global__ void gauss_alpha_prep(int64_t n, const double *__restrict__ s, const double *__restrict__ z,
+                                 double *__restrict__ t) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) t[i] = s[i] * z[i];
+}
+
+__global__ void check_positive_kernel(int64_t n, const double *__restrict__ V, int *flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double v = V[i];
+    if (isnan(v)) atomicOr(flag, 2);
+    else if (!(v > 0.0)) atomicOr(flag, 4);
+  }
+}
+
+// fvar_i = V_i (1 - [B^-1]_ii)  (= V * diag(C^-1 K), R/ep.R:41)
+__global__ void ep_fvar_kernel(int64_t n, const double *__restrict__ V,
+                               const double *__restrict__ bdiag, double *__restrict__ fvar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) fvar[i] = V[i] * (1.0 - bdiag[i]);
+}
+
+// per-site terms of the EP evidence (R/ep.R:45-46):
+// out_i = logC_i + 0.5 log(vc_i + V_i) + 0.5 (mc_i - z_i)^2 / (vc_i + V_i)
+__global__ void ep_site_terms_kernel(int64_t n, const double *__restrict__ logC,
+                                     const double *__restrict__ vc, const double *__restrict__ mc,
+                                     const double *__restrict__ z, const double *__restrict__ V,
+                                     double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double sv = vc[i] + V[i];
+    const double dz = mc[i] - z[i];
+    out[i] = logC[i] + 0.5 * log(sv) + 0.5 * (dz * dz / sv);
+  }
+}
+
+__global__ void log_vec_kernel(int64_t n, const double *__restrict__ v, double *__restrict__ o) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) o[i] = log(v[i]);
+}
+
+__global__ void recip_kernel(int64_t n, const double *__restrict__ v, double *__restrict__ o) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) o[i] = 1.0 / v[i];
+}
+
+// LOO posteriors for approx_laplace (R/gp_loo.R:119-129) with the training-point
+// posterior variance post_var_i = D_i - D_i^2 [B^-1]_ii / V_i, D_i = V_i + jitter
+// (identical to diag(K - K C^-1 K) with C = K + jitter I + diag(V)).
+__global__ void loo_laplace_kernel(int64_t n, double jitter, const double *__restrict__ fhat,
+                                   const double *__restrict__ z, const double *__restrict__ V,
+                                   const double *__restrict__ bdiag, double *__restrict__ lmean,
+                                   double *__restrict__ lvar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double Vi = V[i];
+    const double D = Vi + jitter;
+    const double pv = D - D * D * (bdiag[i] / Vi);
+    const double grad = (z[i] - fhat[i]) / Vi;
+    const double lv = 1.0 / (1.0 / pv - 1.0 / Vi);
+    lvar[i] = lv;
+    lmean[i] = fhat[i] - lv * grad;
+  }
+}
+
+// W_ij = alpha_i alpha_j - s_i s_j Binv_ij on the lower triangle (in place)
+__global__ void grad_w_kernel(int64_t n, const double *__restrict__ alpha,
+                              const double *__restrict__ s, double *__restrict__ W) {
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y)
+    for (int64_t i = j + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      W[i + j * n] = alpha[i] * alpha[j] - s[i] * s[j] * W[i + j * n];
+}
+
+__global__ void diag_scaled_kernel(int64_t n, const double *__restrict__ W,
+                                   const double *__restrict__ s, double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = W[i + i * n] * s[i] * s[i];
+}
+
+__global__ void sub_from_kernel(int64_t n, const double *__restrict__ a, double *__restrict__ b) {
+  // b = a - b
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i] - b[i];
+}
+
+inline unsigned g1(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + 255) / 256); }
+
+void make_B(cudaStream_t st, const double *K, int64_t n, const double *s, double *B) {
+  dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
+  make_B_kernel<<<g, 256, 0, st>>>(K, n, s, B);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// one B-factorisation: B = I + S K S, L = chol(B), alpha = S L^-T L^-1 S z,
+// fnew = K alpha; returns 0 or the non-PD pivot
+// ---------------------------------------------------------------------------
+struct Work {
+  DBuf K, t1, t2, red, logdet_part, ll_part, tmpv;
+  IBuf status, flags;
+};
+
+int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
+                         double *fnew, double *logdetL) {
+  gpgp_ctx *ctx = m->ctx;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = m->n;
+  GPGP_CUDA(cudaMemsetAsync(w.status.p, 0, sizeof(int), st));
+  vec_rsqrt(st, n, m->V.p, m->s.p);
+  make_B(st, w.K.p, n, m->s.p, m->L.p);
+  {
+    Phase ph(ctx, GPGP_PHASE_POTRF);
+    potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
+  }
+  {
+    Phase ph(ctx, GPGP_PHASE_SOLVE);
+    gauss_alpha_prep<<<g1(n), 256, 0, st>>>(n, m->s.p, zvec, w.t1.p);
+    GPGP_CHECK_LAUNCH();
+    trsv_lower(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, w.status.p);
+    trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, w.status.p);
+    vec_mul(st, n, m->s.p, w.t1.p, alpha);
+    gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+  }
+  const int64_t nblk = (n + NB - 1) / NB;
+  sum_vec(st, w.logdet_part.p, nblk, logdetL);
+  int hstatus = 0;
+  GPGP_CUDA(cudaMemcpyAsync(&hstatus, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GPGP_CUDA(cudaStreamSynchronize(st));
+  m->have_binv_diag = false;
+  return hstatus;
+}
+
+// diag(B^-1) = column sums of squares of L^-1 (one triangular inverse).
+void compute_binv_diag(gpgp_model *m) {
+  cudaStream_t st = m->ctx->stream;
+  const int64_t n = m->n;
+  DBuf Wt, tmp;
+  Wt.alloc(st, (size_t)n * n);
+  tmp.alloc(st, (size_t)NB * n);
+  IBuf status;
+  status.alloc(st, 1);
+  GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+  {
+    Phase ph(m->ctx, GPGP_PHASE_TRTRI);
+    trtri_lower(st, m->L.p, n, n, m->Winv.p, Wt.p, n, tmp.p, status.p);
+  }
+  m->binv_diag.alloc(st, n);
+  col_sumsq_lower(st, Wt.p, n, n, m->binv_diag.p);
+  m->have_binv_diag = true;
+}
+
+gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
+  gpgp_ctx *ctx = m->ctx;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = m->n;
+  const double *trials = m->has_trials ? m->trials.p : nullptr;
+  const double *offset = m->has_offset ? m->offset.p : nullptr;
+  Work w;
+  w.K.alloc(st, (size_t)n * n);
+  w.t1.alloc(st, n);
+  w.t2.alloc(st, n);
+  w.red.alloc(st, 256);
+  w.logdet_part.alloc(st, (n + NB - 1) / NB + 1);
+  w.tmpv.alloc(st, n);
+  w.status.alloc(st, 1);
+  w.flags.alloc(st, 1);
+  m->L.alloc(st, (size_t)n * n);
+  m->Winv.alloc(st, (size_t)((n + NB - 1) / NB) * NB * NB);
+  m->s.alloc(st, n);
+  m->alpha.alloc(st, n);
+  m->fmean.alloc(st, n);
+  m->z.alloc(st, n);
+  m->V.alloc(st, n);
+  // K = eval_cf(x, x) + jitter I, stored in full (R/gp_fit.R:91-96)
+  {
+    Phase ph(ctx, GPGP_PHASE_COV);
+    cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
+               m->opts.jitter, nullptr);
+  }
+  double *red = w.red.p;  // [0..63] partials, [64] result, [100..] scalars
+  double *logdetL = red + 100;
+  res->iters = 0;
+  res->converged = 1;
+  res->quad_ok = 1;
+  res->info = 0;
+  if (m->approx.kind == GPGP_APPROX_LAPLACE) {
+    int maxiter = m->lik.kind == GPGP_LIK_GAUSSIAN ? 1 : std::max(1, m->approx.maxiter);
+    GPGP_CUDA(cudaMemsetAsync(m->fmean.p, 0, n * sizeof(double), st));
+    DBuf fnew;
+    fnew.alloc(st, n);
+    double diff = 0.0;
+    int it = 0;
+    for (it = 1; it <= maxiter; ++it) {
+      lik_pseudodata_la(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, m->z.p, m->V.p);
+      GPGP_CUDA(cudaMemsetAsync(w.flags.p, 0, sizeof(int), st));
+      check_positive_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, w.flags.p);
+      GPGP_CHECK_LAUNCH();
+      int hflags = 0;
+      GPGP_CUDA(cudaMemcpyAsync(&hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      GPGP_CUDA(cudaStreamSynchronize(st));
+      if (hflags) {
+        res->status = GPGP_EUNSUPPORTED;
+        res->log_evidence = -INFINITY;
+        return fail(ctx, GPGP_EUNSUPPORTED,
+                    "non-log-concave branch (some pseudo-variance <= 0, R/laplace.R:40-117) is "
+                    "not implemented");
+      }
+      int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL);
+      if (info != 0) {
+        res->status = GPGP_ENOT_PD;
+        res->info = info;
+        res->log_evidence = -INFINITY;
+        return fail(ctx, GPGP_ENOT_PD, "Cholesky factorisation: matrix is not positive definite");
+      }
+      max_abs_diff(st, n, m->fmean.p, fnew.p, red);
+      diff = read_scalar(ctx, red + 64);
+      GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (diff < m->approx.tol) break;
+    }
+    if (it > maxiter) it = maxiter;
+    res->iters = it;
+    if (maxiter > 1 && it == maxiter && !(diff < m->approx.tol)) res->converged = 0;
+    // LML = loglik(f) - 0.5 f^T alpha - 0.5 (C_logdet - V_logdet), C_logdet - V_logdet = 2 sum log L_ii
+    lik_loglik(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, red + 101, red);
+    dot_partial(st, n, m->fmean.p, m->alpha.p, red + 110);  // result at red + 174
+    double ll = read_scalar(ctx, red + 101);
+    double fa = read_scalar(ctx, red + 174);
+    double ld = read_scalar(ctx, logdetL);
+    m->log_evidence = ll - 0.5 * fa - 0.5 * (2.0 * ld);
+    res->log_evidence = m->log_evidence;
+    res->status = GPGP_OK;
+    return GPGP_OK;
+  }
+  // ---------------- EP (R/ep.R:286-330) ----------------
+  const int q = m->approx.quad_order;
+  if (q < 1 || q > 64) return fail(ctx, GPGP_EINVAL, "quad_order must be in 1..64");
+  std::vector<double> hx, hw;
+  gauss_hermite(q, &hx, &hw);
+  DBuf ghx, ghw;
+  copy_in(st, ghx, hx.data(), q, false);
+  copy_in(st, ghw, hw.data(), q, false);
+  DBuf fm_old, fv_old, z_old, P_old, logC, terms, fnew;
+  fm_old.alloc(st, n);
+  fv_old.alloc(st, n);
+  z_old.alloc(st, n);
+  P_old.alloc(st, n);
+  logC.alloc(st, n);
+  terms.alloc(st, n);
+  fnew.alloc(st, n);
+  m->fvar.alloc(st, n);
+  m->cav_mean.alloc(st, n);
+  m->cav_var.alloc(st, n);
+  GPGP_CUDA(cudaMemsetAsync(fm_old.p, 0, n * sizeof(double), st));
+  GPGP_CUDA(cudaMemsetAsync(z_old.p, 0, n * sizeof(double), st));
+  GPGP_CUDA(cudaMemsetAsync(P_old.p, 0, n * sizeof(double), st));
+  cov_diag(st, m->dk, 0xffffffffu, m->F.p, n, m->F.p, n, n, fv_old.p);
+  // fvar_old = diag(K) with K = eval_cf(x, x) + jitter I (R/ep.R:295)
+  add_scalar_kernel<<<g1(n), 256, 0, st>>>(n, m->opts.jitter, fv_old.p);
+  GPGP_CHECK_LAUNCH();
+  const int maxiter = std::max(1, m->approx.maxiter);
+  const double tol = m->approx.tol;
+  double diff_old = INFINITY, diff_new = INFINITY;
+  double damp = m->approx.damping;
+  int it = 0;
+  int last_flags = 0;
+  double lml = -INFINITY;
+  for (it = 1; it <= maxiter; ++it) {
+    GPGP_CUDA(cudaMemsetAsync(w.flags.p, 0, sizeof(int), st));
+    lik_ep_sites(st, m->lk, n, q, ghx.p, ghw.p, fm_old.p, fv_old.p, z_old.p, P_old.p, m->y.p,
+                 trials, offset, damp, m->z.p, m->V.p, logC.p, m->cav_mean.p, m->cav_var.p,
+                 w.flags.p);
+    int hflags = 0;
+    GPGP_CUDA(cudaMemcpyAsync(&hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GPGP_CUDA(cudaStreamSynchronize(st));
+    last_flags = hflags;
+    if (hflags & 2) {  // NA in sites (R/ep.R:30-32)
+      res->iters = it;
+      res->quad_ok = (hflags & 1) ? 0 : 1;
+      res->status = GPGP_ENAN;
+      m->log_evidence = -INFINITY;
+      res->log_evidence = -INFINITY;
+      GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fm_old.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      m->fitted = 1;
+      return GPGP_OK;
+    }
+    if (hflags & 4) {
+      res->status = GPGP_EUNSUPPORTED;
+      return fail(ctx, GPGP_EUNSUPPORTED,
+                  "non-log-concave EP branch (some site variance <= 0, R/ep.R:50-138) is not "
+                  "implemented");
+    }
+    int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL);
+    if (info != 0) {
+      res->status = GPGP_ENOT_PD;
+      res->info = info;
+      return fail(ctx, GPGP_ENOT_PD, "Cholesky factorisation: matrix is not positive definite");
+    }
+    GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    compute_binv_diag(m);
+    ep_fvar_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, m->binv_diag.p, m->fvar.p);
+    GPGP_CHECK_LAUNCH();
+    // evidence: -0.5 C_logdet - 0.5 z^T alpha + sum(site terms), C_logdet = 2 sum log L_ii + sum log V
+    ep_site_terms_kernel<<<g1(n), 256, 0, st>>>(n, logC.p, m->cav_var.p, m->cav_mean.p, m->z.p,
+                                                 m->V.p, terms.p);
+    GPGP_CHECK_LAUNCH();
+    sum_vec(st, terms.p, n, red + 102);
+    log_vec_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, terms.p);
+    GPGP_CHECK_LAUNCH();
+    sum_vec(st, terms.p, n, red + 103);
+    dot_partial(st, n, m->z.p, m->alpha.p, red + 110);
+    max_abs_diff(st, n, fm_old.p, m->fmean.p, red);
+    diff_new = read_scalar(ctx, red + 64);
+    const double sterm = read_scalar(ctx, red + 102);
+    const double slogV = read_scalar(ctx, red + 103);
+    const double za = read_scalar(ctx, red + 174);
+    const double ldL = read_scalar(ctx, logdetL);
+    lml = -0.5 * (2.0 * ldL + slogV) - 0.5 * za + sterm;
+    if (diff_new > diff_old) {
+      damp = damp * m->approx.damping;
+      continue;
+    }
+    damp = std::max(damp, m->approx.damping_min);
+    GPGP_CUDA(cudaMemcpyAsync(fm_old.p, m->fmean.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GPGP_CUDA(cudaMemcpyAsync(fv_old.p, m->fvar.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GPGP_CUDA(cudaMemcpyAsync(z_old.p, m->z.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    recip_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, P_old.p);
+    GPGP_CHECK_LAUNCH();
+    diff_old = diff_new;
+    if (diff_new < tol) break;
+  }
+  if (it > maxiter) it = maxiter;
+  res->iters = it;
+  res->quad_ok = (last_flags & 1) ? 0 : 1;
+  res->status = GPGP_OK;
+  if (maxiter > 1 && it == maxiter) {  // R/ep.R:322-325
+    lml = -INFINITY;
+    res->converged = 0;
+    res->status = GPGP_EMAXITER;
+  }
+  if (!res->quad_ok) lml = -INFINITY;  // R/ep.R:326-328
+  m->log_evidence = lml;
+  res->log_evidence = lml;
+  return GPGP_OK;
+}
+
+gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                       const gpgp_method *method, const gpgp_approx *approx,
+                       const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                       const double *y, const double *trials, const double *offset,
+                       gpgp_model **model, gpgp_fit_result *result, bool on_device) {
+  if (!ctx || !k || !lik || !method || !approx || !opts || !x || !y || !model || !result)
+    return fail(ctx, GPGP_EINVAL, "null argument");
+  if (n < 1 || d < 1) return fail(ctx, GPGP_EINVAL, "n and d must be positive");
+  std::memset(result, 0, sizeof(*result));
+  *model = nullptr;
+  if (lik->kind == GPGP_LIK_GAUSSIAN && approx->kind == GPGP_APPROX_EP)
+    return fail(ctx, GPGP_EINVAL,
+                "approx_ep disabled for lik_gaussian: use approx_laplace (R/gp.R:54-56)");
+  if (lik->kind == GPGP_LIK_BETABINOM)
+    return fail(ctx, GPGP_EUNSUPPORTED, "lik_betabinom is not implemented on the device");
+  if (lik->kind == GPGP_LIK_BINOMIAL && !trials)
+    return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial likelihood");
+  if (method->kind != GPGP_METHOD_FULL)
+    return fail(ctx, GPGP_EUNSUPPORTED, "method_fitc is not available in this build");
+  if (opts->precision != GPGP_PREC_FP64)
+    return fail(ctx, GPGP_EUNSUPPORTED, "mixed precision is not available in this build");
+  std::unique_ptr<gpgp_model> m(new gpgp_model());
+  m->ctx = ctx;
+  m->spec = *k;
+  m->lik = *lik;
+  m->lk = make_likdev(*lik);
+  m->method = *method;
+  m->approx = *approx;
+  m->opts = *opts;
+  m->n = n;
+  m->d = d;
+  std::string err;
+  gpgp_status st = build_dev_kernel(k, d, &m->dk, &m->prep, &err);
+  if (st != GPGP_OK) return fail(ctx, st, err);
+  cudaStream_t s = ctx->stream;
+  copy_in(s, m->x, x, (size_t)n * d, on_device);
+  copy_in(s, m->y, y, n, on_device);
+  if (trials) {
+    copy_in(s, m->trials, trials, n, on_device);
+    m->has_trials = true;
+  }
+  if (offset) {
+    copy_in(s, m->offset, offset, n, on_device);
+    m->has_offset = true;
+  }
+  m->F.alloc(s, (size_t)n * std::max(1, m->dk.nfeat));
+  prep_features(s, m->dk, m->prep, m->x.p, n, n, m->F.p, n);
+  st = fit_full(m.get(), result);
+  if (st != GPGP_OK) {
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    return st;
+  }
+  m->fitted = 1;
+  GPGP_CUDA(cudaStreamSynchronize(s));
+  *model = m.release();
+  return GPGP_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// exported functions
+// ===========================================================================
+extern "C" {
+
+const char *gpgp_status_string(gpgp_status s) {
+  switch (s) {
+    case GPGP_OK: return "ok";
+    case GPGP_ENOT_PD: return "matrix not positive definite";
+    case GPGP_ENAN: return "NaN encountered";
+    case GPGP_EMAXITER: return "maximum number of iterations reached";
+    case GPGP_EUNSUPPORTED: return "unsupported";
+    case GPGP_EOOM: return "out of device memory";
+    case GPGP_ETIMEOUT: return "device wait timed out";
+    case GPGP_ECUDA: return "CUDA error";
+    case GPGP_EINVAL: return "invalid argument";
+    case GPGP_ENOT_FITTED: return "model not fitted";
+    case GPGP_EBUSY: return "busy";
+  }
+  return "unknown";
+}
+
+const char *gpgp_last_error(const gpgp_ctx *ctx) {
+  return ctx ? ctx->last_error.c_str() : tl_error.c_str();
+}
+
+int64_t gpgp_launch_count(const gpgp_ctx *) { return g_launches; }
+
+gpgp_status gpgp_create(gpgp_ctx **out, int device) {
+  if (!out) return GPGP_EINVAL;
+  *out = nullptr;
+  std::unique_ptr<gpgp_ctx> c(new gpgp_ctx());
+  gpgp_status st = guarded(nullptr, [&]() -> gpgp_status {
+    int ndev = 0;
+    GPGP_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(nullptr, GPGP_EINVAL, "no such CUDA device");
+    GPGP_CUDA(cudaSetDevice(device));
+    c->device = device;
+    GPGP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    GPGP_CUDA(cudaMallocHost((void **)&c->h_pinned, 64 * sizeof(double)));
+    return GPGP_OK;
+  });
+  if (st == GPGP_OK) *out = c.release();
+  return st;
+}
+
+gpgp_status gpgp_destroy(gpgp_ctx *ctx) {
+  if (!ctx) return GPGP_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  delete ctx;
+  return GPGP_OK;
+}
+
+gpgp_status gpgp_sync(gpgp_ctx *ctx) {
+  if (!ctx) return GPGP_EINVAL;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaStreamSynchronize(ctx->stream));
+    return GPGP_OK;
+  });
+}
+
+void *gpgp_stream(gpgp_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+gpgp_status gpgp_profile_enable(gpgp_ctx *ctx, int32_t on) {
+  if (!ctx) return GPGP_EINVAL;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    prof_collect(ctx);
+    for (int i = 0; i < GPGP_NPHASE; ++i) {
+      ctx->prof_ms[i] = 0.0;
+      ctx->prof_calls[i] = 0;
+    }
+    ctx->prof = on != 0;
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_profile_read(gpgp_ctx *ctx, double *ms, int64_t *calls) {
+  if (!ctx) return GPGP_EINVAL;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    prof_collect(ctx);
+    for (int i = 0; i < GPGP_NPHASE; ++i) {
+      if (ms) ms[i] = ctx->prof_ms[i];
+      if (calls) calls[i] = ctx->prof_calls[i];
+    }
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_eval_cf(gpgp_ctx *ctx, const gpgp_kernel *k, const double *x1, int64_t n1,
+                         const double *x2, int64_t n2, int32_t d, int32_t diag_only,
+                         uint32_t group_mask, double *out) {
+  if (!ctx || !k || !x1 || !x2 || !out || n1 < 0 || n2 < 0 || d < 1)
+    return fail(ctx, GPGP_EINVAL, "invalid argument");
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    DevKernel dk;
+    std::vector<HostTermPrep> prep;
+    std::string err;
+    gpgp_status st = build_dev_kernel(k, d, &dk, &prep, &err);
+    if (st != GPGP_OK) return fail(ctx, st, err);
+    cudaStream_t s = ctx->stream;
+    const uint32_t gm = group_mask ? group_mask : 0xffffffffu;
+    DBuf dx1, dx2, F1, F2, o;
+    copy_in(s, dx1, x1, (size_t)n1 * d, false);
+    copy_in(s, dx2, x2, (size_t)n2 * d, false);
+    F1.alloc(s, (size_t)std::max<int64_t>(n1, 1) * dk.nfeat);
+    F2.alloc(s, (size_t)std::max<int64_t>(n2, 1) * dk.nfeat);
+    prep_features(s, dk, prep, dx1.p, n1, n1, F1.p, std::max<int64_t>(n1, 1));
+    prep_features(s, dk, prep, dx2.p, n2, n2, F2.p, std::max<int64_t>(n2, 1));
+    size_t cnt;
+    if (diag_only) {
+      const int64_t nd = std::min(n1, n2);
+      cnt = nd;
+      o.alloc(s, std::max<size_t>(cnt, 1));
+      cov_diag(s, dk, gm, F1.p, std::max<int64_t>(n1, 1), F2.p, std::max<int64_t>(n2, 1), nd, o.p);
+    } else {
+      cnt = (size_t)n1 * n2;
+      o.alloc(s, std::max<size_t>(cnt, 1));
+      cov_matrix(s, dk, gm, F1.p, std::max<int64_t>(n1, 1), n1, F2.p, std::max<int64_t>(n2, 1), n2,
+                 o.p, std::max<int64_t>(n1, 1), COV_FULL, 0, 0, 0.0, nullptr);
+    }
+    if (cnt) GPGP_CUDA(cudaMemcpyAsync(out, o.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    return GPGP_OK;
+  });
+}
+
+static gpgp_ctx *default_ctx(gpgp_status *st) {
+  static std::mutex mu;
+  static gpgp_ctx *ctx = nullptr;
+  std::lock_guard<std::mutex> g(mu);
+  if (!ctx) *st = gpgp_create(&ctx, 0);
+  else *st = GPGP_OK;
+  return ctx;
+}
+
+static gpgp_status one_term(int kind, const double *x1, int64_t n1, const double *x2, int64_t n2,
+                            int32_t d, double lscale, double magn, double sigma0, double sigma,
+                            int32_t diag_only, double *out) {
+  gpgp_status st;
+  gpgp_ctx *ctx = default_ctx(&st);
+  if (st != GPGP_OK) return st;
+  gpgp_kernel k;
+  std::memset(&k, 0, sizeof(k));
+  k.nterms = 1;
+  k.ngroups = 1;
+  k.term[0].kind = kind;
+  k.term[0].lscale = lscale;
+  k.term[0].magn = magn;
+  k.term[0].sigma0 = sigma0;
+  k.term[0].sigma = sigma;
+  return gpgp_eval_cf(ctx, &k, x1, n1, x2, n2, d, diag_only, 0, out);
+}
+
+gpgp_status gpgp_cf_sexp(const double *x1, int64_t n1, const double *x2, int64_t n2, int32_t d,
+                         double lscale, double magn, int32_t diag_only, double *out) {
+  return one_term(GPGP_CF_SEXP, x1, n1, x2, n2, d, lscale, magn, 0, 0, diag_only, out);
+}
+gpgp_status gpgp_cf_matern32(const double *x1, int64_t n1, const double *x2, int64_t n2,
+                             int32_t d, double lscale, double magn, int32_t diag_only,
+                             double *out) {
+  return one_term(GPGP_CF_MATERN32, x1, n1, x2, n2, d, lscale, magn, 0, 0, diag_only, out);
+}
+gpgp_status gpgp_cf_matern52(const double *x1, int64_t n1, const double *x2, int64_t n2,
+                             int32_t d, double lscale, double magn, int32_t diag_only,
+                             double *out) {
+  return one_term(GPGP_CF_MATERN52, x1, n1, x2, n2, d, lscale, magn, 0, 0, diag_only, out);
+}
+gpgp_status gpgp_cf_nn(const double *x1, int64_t n1, const double *x2, int64_t n2, int32_t d,
+                       double sigma0, double sigma, double magn, int32_t diag_only, double *out) {
+  return one_term(GPGP_CF_NN, x1, n1, x2, n2, d, 1.0, magn, sigma0, sigma, diag_only, out);
+}
+
+gpgp_status gpgp_fit(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                     const gpgp_method *method, const gpgp_approx *approx,
+                     const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                     const double *y, const double *trials, const double *offset,
+                     gpgp_model **model, gpgp_fit_result *result) {
+  return guarded(ctx, [&]() {
+    if (ctx) GPGP_CUDA(cudaSetDevice(ctx->device));
+    return fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
+                      result, false);
+  });
+}
+
+gpgp_status gpgp_fit_dev(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                         const gpgp_method *method, const gpgp_approx *approx,
+                         const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                         const double *y, const double *trials, const double *offset,
+                         gpgp_model **model, gpgp_fit_result *result) {
+  return guarded(ctx, [&]() {
+    if (ctx) GPGP_CUDA(cudaSetDevice(ctx->device));
+    return fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
+                      result, true);
+  });
+}
+
+gpgp_status gpgp_model_free(gpgp_model *model) {
+  if (!model) return GPGP_OK;
+  cudaSetDevice(model->ctx->device);
+  delete model;  // buffers are released on the context's stream
+  return GPGP_OK;
+}
+
+gpgp_status gpgp_model_get(gpgp_model *m, int32_t field, double *out) {
+  if (!m || !out) return GPGP_EINVAL;
+  return guarded(m->ctx, [&]() -> gpgp_status {
+    const double *src = nullptr;
+    switch (field) {
+      case GPGP_FIELD_ALPHA: src = m->alpha.p; break;
+      case GPGP_FIELD_FMEAN: src = m->fmean.p; break;
+      case GPGP_FIELD_Z: src = m->z.p; break;
+      case GPGP_FIELD_V: src = m->V.p; break;
+      case GPGP_FIELD_FVAR: src = m->fvar.p; break;
+      case GPGP_FIELD_CAVITY_MEAN: src = m->cav_mean.p; break;
+      case GPGP_FIELD_CAVITY_VAR: src = m->cav_var.p; break;
+      default: return fail(m->ctx, GPGP_EINVAL, "unknown field");
+    }
+    if (!src) return fail(m->ctx, GPGP_EINVAL, "field not available for this model");
+    GPGP_CUDA(cudaSetDevice(m->ctx->device));
+    GPGP_CUDA(cudaMemcpyAsync(out, src, m->n * sizeof(double), cudaMemcpyDeviceToHost,
+                              m->ctx->stream));
+    GPGP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return GPGP_OK;
+  });
+}
+
+static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32_t group_mask,
+                             double *mean, double *var, bool on_device) {
+  if (!m || !xt || !mean || mt < 0) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
+  if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  gpgp_ctx *ctx = m->ctx;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int64_t n = m->n;
+    const uint32_t gm = group_mask ? group_mask : 0xffffffffu;
+    if (mt == 0) return GPGP_OK;
+    DBuf dxt, Ft, dmean, dvar;
+    copy_in(s, dxt, xt, (size_t)mt * m->d, on_device);
+    Ft.alloc(s, (size_t)mt * std::max(1, m->dk.nfeat));
+    prep_features(s, m->dk, m->prep, dxt.p, mt, mt, Ft.p, mt);
+    double *mout = mean, *vout = var;
+    if (!on_device) {
+      dmean.alloc(s, mt);
+      mout = dmean.p;
+      if (var) {
+        dvar.alloc(s, mt);
+        vout = dvar.p;
+      }
+    }
+    // mean = Kt alpha (R/gp_pred.R:209), fused: Kt is never stored
+    {
+      Phase ph(ctx, GPGP_PHASE_PRED_MEAN);
+      cov_matvec(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, mout);
+    }
+    if (var) {
+      Phase ph(ctx, GPGP_PHASE_PRED_VAR);
+      // var = diag(Ktt) - colSums((C_chol^-1 Kt^T)^2), C_chol^-1 = L^-1 diag(s)  (R/gp_pred.R:216-228)
+      const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(mt, (int64_t)(1ll << 28) / std::max<int64_t>(n, 1)));
+      DBuf R, tmp, csum, kdiag;
+      R.alloc(s, (size_t)n * chunk);
+      tmp.alloc(s, (size_t)NB * chunk);
+      csum.alloc(s, mt);
+      kdiag.alloc(s, mt);
+      IBuf status;
+      status.alloc(s, 1);
+      GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+      for (int64_t c0 = 0; c0 < mt; c0 += chunk) {
+        const int64_t mc = std::min(chunk, mt - c0);
+        cov_matrix(s, m->dk, gm, m->F.p, n, n, Ft.p + c0, mt, mc, R.p, n, COV_ROWSCALE, 0, 0, 0.0,
+                   m->s.p);
+        trsm_lower(s, m->L.p, n, n, m->Winv.p, R.p, mc, n, tmp.p, status.p);
+        col_sumsq(s, R.p, n, mc, n, csum.p + c0);
+      }
+      cov_diag(s, m->dk, gm, Ft.p, mt, Ft.p, mt, mt, kdiag.p);
+      sub_from_kernel<<<g1(mt), 256, 0, s>>>(mt, kdiag.p, csum.p);
+      GPGP_CHECK_LAUNCH();
+      GPGP_CUDA(cudaMemcpyAsync(vout, csum.p, mt * sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    }
+    if (!on_device)
+      GPGP_CUDA(cudaMemcpyAsync(mean, mout, mt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_pred(gpgp_model *m, const double *xt, int64_t mt, uint32_t group_mask,
+                      double *mean, double *var) {
+  return pred_impl(m, xt, mt, group_mask, mean, var, false);
+}
+
+gpgp_status gpgp_pred_dev(gpgp_model *m, const double *xt, int64_t mt, uint32_t group_mask,
+                          double *mean, double *var) {
+  return pred_impl(m, xt, mt, group_mask, mean, var, true);
+}
+
+gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *loo_sum) {
+  if (!m || !loos) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
+  if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (quad_order < 1 || quad_order > 64) return fail(m->ctx, GPGP_EINVAL, "quad_order must be in 1..64");
+  gpgp_ctx *ctx = m->ctx;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int64_t n = m->n;
+    DBuf lmean, lvar, out, ghx, ghw, red;
+    const double *mp, *vp;
+    if (m->approx.kind == GPGP_APPROX_EP) {
+      if (!m->cav_mean.p) return fail(ctx, GPGP_ENOT_FITTED, "EP fit has no cavity moments");
+      mp = m->cav_mean.p;
+      vp = m->cav_var.p;
+    } else {
+      if (!m->have_binv_diag) compute_binv_diag(m);
+      lmean.alloc(s, n);
+      lvar.alloc(s, n);
+      loo_laplace_kernel<<<g1(n), 256, 0, s>>>(n, m->opts.jitter, m->fmean.p, m->z.p, m->V.p,
+                                               m->binv_diag.p, lmean.p, lvar.p);
+      GPGP_CHECK_LAUNCH();
+      mp = lmean.p;
+      vp = lvar.p;
+    }
+    std::vector<double> hx, hw;
+    gauss_hermite(quad_order, &hx, &hw);
+    copy_in(s, ghx, hx.data(), quad_order, false);
+    copy_in(s, ghw, hw.data(), quad_order, false);
+    out.alloc(s, n);
+    lik_loo_gh(s, m->lk, n, quad_order, ghx.p, ghw.p, mp, vp, m->y.p,
+               m->has_trials ? m->trials.p : nullptr, m->has_offset ? m->offset.p : nullptr, out.p);
+    GPGP_CUDA(cudaMemcpyAsync(loos, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    if (loo_sum) {
+      double acc = 0.0;
+      for (int64_t i = 0; i < n; ++i) acc += loos[i];
+      *loo_sum = acc;
+    }
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_sigma) {
+  if (!m || !grad_terms) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
+  if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (m->lik.kind != GPGP_LIK_GAUSSIAN || m->method.kind != GPGP_METHOD_FULL)
+    return fail(m->ctx, GPGP_EUNSUPPORTED, "gradient needs lik_gaussian and method_full");
+  gpgp_ctx *ctx = m->ctx;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int64_t n = m->n;
+    DBuf Wt, Bi, tmp, part, g, dg, red;
+    IBuf status;
+    status.alloc(s, 1);
+    GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+    Wt.alloc(s, (size_t)n * n);
+    tmp.alloc(s, (size_t)NB * n);
+    {
+      Phase ph(ctx, GPGP_PHASE_TRTRI);
+      trtri_lower(s, m->L.p, n, n, m->Winv.p, Wt.p, n, tmp.p, status.p);
+    }
+    Bi.alloc(s, (size_t)n * n);
+    {
+      // B^-1 = W^T W (lower part), W = L^-1
+      Phase ph(ctx, GPGP_PHASE_LAUUM);
+      gemm64(s, true, false, n, n, n, 1.0, Wt.p, n, Wt.p, n, 0.0, Bi.p, n, true, 1);
+    }
+    Wt.reset();
+    // tr(C^-1) = sum_i s_i^2 Binv_ii
+    dg.alloc(s, n);
+    diag_scaled_kernel<<<g1(n), 256, 0, s>>>(n, Bi.p, m->s.p, dg.p);
+    GPGP_CHECK_LAUNCH();
+    red.alloc(s, 256);
+    sum_vec(s, dg.p, n, red.p + 200);
+    dot_partial(s, n, m->alpha.p, m->alpha.p, red.p);
+    dim3 gg((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
+    grad_w_kernel<<<gg, 256, 0, s>>>(n, m->alpha.p, m->s.p, Bi.p);
+    GPGP_CHECK_LAUNCH();
+    part.alloc(s, cov_grad_partials(n));
+    g.alloc(s, GPGP_MAX_TERMS * GPGP_TERM_NPARAM);
+    gpgp_status st;
+    {
+      Phase ph(ctx, GPGP_PHASE_GRAD);
+      st = cov_grad_contract(s, m->dk, m->F.p, n, n, Bi.p, n, part.p, g.p);
+    }
+    if (st != GPGP_OK) return fail(ctx, st, "gradient contraction failed");
+    std::vector<double> hg(m->dk.nterms * GPGP_TERM_NPARAM);
+    GPGP_CUDA(cudaMemcpyAsync(hg.data(), g.p, hg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    double h2[2];
+    GPGP_CUDA(cudaMemcpyAsync(&h2[0], red.p + 200, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaMemcpyAsync(&h2[1], red.p + 64, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < hg.size(); ++i) grad_terms[i] = 0.5 * hg[i];
+    if (grad_lik_sigma) {
+      const double s2 = m->lik.sigma * m->lik.sigma;
+      *grad_lik_sigma = s2 * (h2[1] - h2[0]);
+    }
+    return GPGP_OK;
+  });
+}
+
+}  // extern "C"

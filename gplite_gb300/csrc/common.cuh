@@ -1,0 +1,188 @@
+// Internal declarations shared by the libgpgp translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "gpgp.h"
+
+namespace gpgp {
+
+// ---------------------------------------------------------------------------
+// error handling: every CUDA call is checked; failures turn into GPGP_ECUDA
+// with the message kept on the context (never abort, never trap).
+// ---------------------------------------------------------------------------
+struct CudaError {
+  cudaError_t err;
+  const char *what;
+  int line;
+};
+
+#define GPGP_CUDA(call)                                                   \
+  do {                                                                    \
+    cudaError_t e__ = (call);                                             \
+    if (e__ != cudaSuccess) throw ::gpgp::CudaError{e__, #call, __LINE__}; \
+  } while (0)
+
+// Number of kernel launches issued through the library (all contexts).
+extern int64_t g_launches;
+#define GPGP_LAUNCHED() (++::gpgp::g_launches)
+#define GPGP_CHECK_LAUNCH()              \
+  do {                                   \
+    GPGP_LAUNCHED();                     \
+    GPGP_CUDA(cudaPeekAtLastError());    \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// covariance program on the device
+// ---------------------------------------------------------------------------
+// Features: every term reads its own columns of a feature matrix F (rows =
+// points, column-major with leading dimension ld). prep_features() writes
+// them: the term's input columns (vars subset), normalised when asked; for a
+// periodic term the columns are [sin(w x), cos(w x), x] with w = 2*pi/period.
+struct DevTerm {
+  int kind;      // gpgp_cf_kind of the (base) kernel
+  int group;     // product group
+  int periodic;  // 1: features are [sin, cos, raw]
+  int off;       // first feature column of this term
+  int nv;        // number of input columns used
+  int dt;        // feature columns read by the kernel (nv, or 2*nv if periodic)
+  double m2;     // magn^2
+  double c1;     // sexp: 1/lscale^2; matern32/52: sqrt(3|5)/lscale; nn: sigma0^2*sigma^2
+  double c2;     // nn: sigma^2; periodic: w = 2*pi/period
+};
+
+struct DevKernel {
+  int nterms;
+  int ngroups;
+  int nfeat;     // total feature columns
+  DevTerm t[GPGP_MAX_TERMS];
+};
+
+// Host-side description of where each term's inputs come from.
+struct HostTermPrep {
+  int nv;
+  int vars[GPGP_MAX_VARS];
+  int normalize;
+  int periodic;
+  double means[GPGP_MAX_VARS];
+  double scales[GPGP_MAX_VARS];
+  double w;
+};
+
+gpgp_status build_dev_kernel(const gpgp_kernel *k, int d, DevKernel *dk,
+                             std::vector<HostTermPrep> *prep, std::string *err);
+
+// Feature matrix F (n x nfeat, leading dimension ldf) from x (n x d, ldx).
+void prep_features(cudaStream_t s, const DevKernel &dk, const std::vector<HostTermPrep> &prep,
+                   const double *x, int64_t n, int64_t ldx, double *F, int64_t ldf);
+
+// Output modes of the covariance tile generator.
+enum CovMode {
+  COV_FULL = 0,     // out = K(x1, x2) (+ jitter on the diagonal when sym)
+  COV_B = 1,        // out = I + s_i s_j (K + jitter I)_ij  (lower triangle, sym only)
+  COV_ROWSCALE = 2  // out_ij = s_i K(x1_i, x2_j) (cross, no jitter)
+};
+
+// out (n1 x n2, ldo). sym: x1 == x2 (only lower tiles evaluated; upper mirrored
+// when mirror = 1). s: per-row scale (COV_B, COV_ROWSCALE) or null.
+void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+                int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2, double *out,
+                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale);
+
+// out[i] = K(x1_i, x2_i) for i < n (diagonal).
+void cov_diag(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+              int64_t ld1, const double *F2, int64_t ld2, int64_t n, double *out);
+
+// out[i] = sum_j K(x1_i, x2_j) v_j for i < n1 (fused, K never stored).
+void cov_matvec(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+                int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2,
+                const double *v, double *out);
+
+// Gradient contraction: g[t*5 + p] = sum_{i,j} W_ij dK_ij / dlog(theta_{t,p}) over the
+// symmetric W given by its lower triangle (ldw); partial sums per tile in part,
+// reduced in a fixed order. Returns EUNSUPPORTED for parameters without a derivative.
+gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double *F, int64_t ldf,
+                              int64_t n, const double *W, int64_t ldw, double *part, double *g);
+int64_t cov_grad_partials(int64_t n);
+
+// ---------------------------------------------------------------------------
+// dense FP64 linear algebra (column-major)
+// ---------------------------------------------------------------------------
+constexpr int NB = 64;  // block size of the blocked factorisations
+
+// C = alpha * op(A) op(B) + beta * C. lower_only: only tiles on/below the
+// diagonal of C are computed (SYRK-style). tri_k: A and B are triangular so
+// that terms with k < max(row, col) vanish (lauum of a lower factor).
+void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+            const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+            int64_t ldc, bool lower_only = false, int tri_mode = 0);
+
+// Blocked right-looking Cholesky of the lower triangle of A (n x n, lda), in
+// place. Winv receives the inverses of the NB x NB diagonal factors
+// (nblocks * NB * NB); logdet_part the per-block sums of log L_jj; status[0]
+// the first failing pivot (1-based, 0 = OK). Later kernels of the same
+// sequence see a non-zero status and return without work.
+void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
+           int *status);
+
+// Triangular solves with the blocked factor (lower L, diagonal inverses Winv).
+// b is consumed as workspace; x receives the solution (x != b).
+void trsv_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                double *b, double *x, const int *status);    // x = L^-1 b
+void trsv_lower_t(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                  double *b, double *x, const int *status);  // x = L^-T b
+// B <- L^-1 B (n x m, ldb); tmp holds NB * m doubles.
+void trsm_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                double *B, int64_t m, int64_t ldb, double *tmp, const int *status);
+// Wout = L^-1 (lower, strict upper = 0); tmp holds NB * n doubles.
+void trtri_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                 double *Wout, int64_t ldw, double *tmp, const int *status);
+// out[j] = sum_i W_ij^2 (column norms of a lower-triangular W) = diag(W^T W).
+void col_sumsq_lower(cudaStream_t s, const double *W, int64_t n, int64_t ldw, double *out);
+// out[j] = sum_i B_ij^2 for an n x m dense B.
+void col_sumsq(cudaStream_t s, const double *B, int64_t n, int64_t m, int64_t ldb, double *out);
+// y = A x with symmetric A given by its full storage (n x n).
+void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, const double *A,
+            int64_t lda, const double *x, double beta, double *y);
+// Sum of logdet partials (fixed order) -> out[0].
+void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out);
+
+// ---------------------------------------------------------------------------
+// likelihood kernels
+// ---------------------------------------------------------------------------
+struct LikDev {
+  int kind, link;
+  double sigma, phi;
+};
+// Laplace pseudo data (R/lik.R:188-201): z, V from f.
+void lik_pseudodata_la(cudaStream_t s, const LikDev &lk, int64_t n, const double *f,
+                       const double *y, const double *trials, const double *offset, double *z,
+                       double *V);
+// sum_i loglik(f_i) -> partial sums, reduced later
+void lik_loglik(cudaStream_t s, const LikDev &lk, int64_t n, const double *f, const double *y,
+                const double *trials, const double *offset, double *out_scalar, double *part);
+// EP site update (R/lik.R:207-270) for all sites; writes z, V, logC, cavity
+// moments; flags[0] |= 1 on NaN quadrature, flags[0] |= 2 on NaN sites.
+void lik_ep_sites(cudaStream_t s, const LikDev &lk, int64_t n, int q, const double *ghx,
+                  const double *ghw, const double *fmean, const double *fvar, const double *z_old,
+                  const double *P_old, const double *y, const double *trials,
+                  const double *offset, double damping, double *z, double *V, double *logC,
+                  double *cav_mean, double *cav_var, int *flags);
+// LOO log predictive densities by GH quadrature (R/gp_loo.R:90-96).
+void lik_loo_gh(cudaStream_t s, const LikDev &lk, int64_t n, int q, const double *ghx,
+                const double *ghw, const double *mean, const double *var, const double *y,
+                const double *trials, const double *offset, double *loos);
+
+// Elementwise helpers.
+void vec_axpby(cudaStream_t s, int64_t n, double a, const double *x, double b, double *y);
+void vec_mul(cudaStream_t s, int64_t n, const double *a, const double *b, double *out);
+void vec_rsqrt(cudaStream_t s, int64_t n, const double *v, double *out);  // 1/sqrt(v)
+void dot_partial(cudaStream_t s, int64_t n, const double *a, const double *b, double *out);
+void max_abs_diff(cudaStream_t s, int64_t n, const double *a, const double *b, double *out);
+
+// GH nodes/weights of order q (R/quadrature.R:28-34), host computation.
+void gauss_hermite(int q, std::vector<double> *x, std::vector<double> *w);
+
+}  // namespace gpgp

@@ -1,0 +1,609 @@
+// Covariance functions on the GPU: feature preparation, tile generation,
+// fused kernel-matrix x vector, diagonal, and the gradient contraction.
+//
+// The per-pair formulas restate src/cf.cpp:9-162 (sexp, matern32, matern52,
+// nn) and R/cf.R:413-497 (const, lin, periodic, sums and products); inputs
+// are prepared as in prepare_inputmat (R/misc.R:17-31).
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace gpgp {
+
+int64_t g_launches = 0;
+
+static const double kPi = 3.14159265358979323846;
+
+gpgp_status build_dev_kernel(const gpgp_kernel *k, int d, DevKernel *dk,
+                             std::vector<HostTermPrep> *prep, std::string *err) {
+  if (!k || k->nterms < 1 || k->nterms > GPGP_MAX_TERMS || k->ngroups < 1 ||
+      k->ngroups > k->nterms || d < 1) {
+    *err = "invalid kernel: nterms/ngroups/d out of range";
+    return GPGP_EINVAL;
+  }
+  std::memset(dk, 0, sizeof(*dk));
+  prep->clear();
+  dk->nterms = k->nterms;
+  dk->ngroups = k->ngroups;
+  int off = 0, last_group = -1;
+  for (int t = 0; t < k->nterms; ++t) {
+    const gpgp_cf_term &T = k->term[t];
+    if (T.kind < GPGP_CF_CONST || T.kind > GPGP_CF_NN) {
+      *err = "invalid kernel: unknown term kind";
+      return GPGP_EINVAL;
+    }
+    if (T.group < 0 || T.group >= k->ngroups || T.group < last_group ||
+        (T.group > last_group + 1)) {
+      *err = "invalid kernel: groups must be contiguous and numbered 0..ngroups-1";
+      return GPGP_EINVAL;
+    }
+    last_group = T.group;
+    HostTermPrep hp;
+    std::memset(&hp, 0, sizeof(hp));
+    int nv = T.nvars > 0 ? T.nvars : d;
+    if (nv > GPGP_MAX_VARS) {
+      *err = "invalid kernel: more than GPGP_MAX_VARS input columns in a term";
+      return GPGP_EINVAL;
+    }
+    hp.nv = nv;
+    for (int v = 0; v < nv; ++v) {
+      int c = T.nvars > 0 ? T.vars[v] : v;
+      if (c < 0 || c >= d) {
+        *err = "invalid kernel: vars index out of range";
+        return GPGP_EINVAL;
+      }
+      hp.vars[v] = c;
+      hp.means[v] = T.means[v];
+      hp.scales[v] = T.scales[v];
+    }
+    hp.periodic = T.periodic ? 1 : 0;
+    // cf_periodic never normalises (R/cf.R:173-184, learn_scales.cf_periodic R/cf.R:852)
+    hp.normalize = (T.normalize && !T.periodic) ? 1 : 0;
+    DevTerm &D = dk->t[t];
+    D.kind = T.kind;
+    D.group = T.group;
+    D.periodic = hp.periodic;
+    D.off = off;
+    D.nv = nv;
+    D.dt = hp.periodic ? 2 * nv : nv;
+    D.m2 = T.magn * T.magn;
+    if (hp.periodic) {
+      if (!(T.period > 0)) {
+        *err = "invalid kernel: period must be positive";
+        return GPGP_EINVAL;
+      }
+      hp.w = 2.0 * kPi / T.period;
+      D.c2 = hp.w;
+    }
+    switch (T.kind) {
+      case GPGP_CF_SEXP:
+        D.c1 = 1.0 / (T.lscale * T.lscale);
+        break;
+      case GPGP_CF_MATERN32:
+        D.c1 = sqrt(3.0) / T.lscale;
+        break;
+      case GPGP_CF_MATERN52:
+        D.c1 = sqrt(5.0) / T.lscale;
+        break;
+      case GPGP_CF_NN:
+        D.c1 = T.sigma0 * T.sigma0 * T.sigma * T.sigma;
+        if (!hp.periodic) D.c2 = T.sigma * T.sigma;
+        break;
+      default:
+        break;
+    }
+    if (T.kind == GPGP_CF_NN && hp.periodic) {
+      *err = "periodic wrapper around cf_nn is not supported";
+      return GPGP_EUNSUPPORTED;
+    }
+    off += hp.periodic ? 3 * nv : nv;
+    prep->push_back(hp);
+  }
+  if (last_group != k->ngroups - 1) {
+    *err = "invalid kernel: ngroups does not match the groups used";
+    return GPGP_EINVAL;
+  }
+  if (off > 64) {
+    *err = "invalid kernel: more than 64 feature columns in total";
+    return GPGP_EINVAL;
+  }
+  dk->nfeat = off;
+  return GPGP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// feature preparation
+// ---------------------------------------------------------------------------
+struct FeatCol {
+  int src;   // input column
+  int mode;  // 0 raw, 1 normalised, 2 sin(w x), 3 cos(w x)
+  double mean, scale, w;
+};
+struct FeatTable {
+  int ncol;
+  FeatCol c[64];
+};
+
+__global__ void prep_features_kernel(FeatTable tab, const double *__restrict__ x, int64_t n,
+                                     int64_t ldx, double *__restrict__ F, int64_t ldf) {
+  int col = blockIdx.y;
+  const FeatCol fc = tab.c[col];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = x[i + fc.src * ldx];
+    double o;
+    if (fc.mode == 1)
+      o = (v - fc.mean) / fc.scale;
+    else if (fc.mode == 2)
+      o = sin(fc.w * v);
+    else if (fc.mode == 3)
+      o = cos(fc.w * v);
+    else
+      o = v;
+    F[i + col * ldf] = o;
+  }
+}
+
+void prep_features(cudaStream_t s, const DevKernel &dk, const std::vector<HostTermPrep> &prep,
+                   const double *x, int64_t n, int64_t ldx, double *F, int64_t ldf) {
+  FeatTable tab;
+  std::memset(&tab, 0, sizeof(tab));
+  int c = 0;
+  for (int t = 0; t < dk.nterms; ++t) {
+    const HostTermPrep &hp = prep[t];
+    if (hp.periodic) {
+      // cbind(sin(2*pi/period * x), cos(2*pi/period * x)) (R/cf.R:482-483), then raw
+      // columns for the period derivative
+      for (int v = 0; v < hp.nv; ++v) tab.c[c++] = FeatCol{hp.vars[v], 2, 0.0, 1.0, hp.w};
+      for (int v = 0; v < hp.nv; ++v) tab.c[c++] = FeatCol{hp.vars[v], 3, 0.0, 1.0, hp.w};
+      for (int v = 0; v < hp.nv; ++v) tab.c[c++] = FeatCol{hp.vars[v], 0, 0.0, 1.0, 0.0};
+    } else {
+      for (int v = 0; v < hp.nv; ++v)
+        tab.c[c++] = FeatCol{hp.vars[v], hp.normalize ? 1 : 0, hp.means[v], hp.scales[v], 0.0};
+    }
+  }
+  tab.ncol = c;
+  if (n == 0 || c == 0) return;
+  int64_t bx = std::min<int64_t>((n + 255) / 256, 4096);
+  dim3 grid((unsigned)bx, (unsigned)c);
+  prep_features_kernel<<<grid, 256, 0, s>>>(tab, x, n, ldx, F, ldf);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// per-pair evaluation
+// ---------------------------------------------------------------------------
+// fi / fj point at the term's first feature of points i and j (stride 1).
+__device__ __forceinline__ double term_value(const DevTerm &T, const double *fi,
+                                             const double *fj) {
+  switch (T.kind) {
+    case GPGP_CF_CONST:
+      return T.m2;
+    case GPGP_CF_LIN: {
+      double dot = 0.0;
+      for (int c = 0; c < T.dt; ++c) dot += fi[c] * fj[c];
+      return T.m2 * dot;
+    }
+    case GPGP_CF_NN: {
+      double a = 0.0, b = 0.0, cc = 0.0;
+      for (int c = 0; c < T.dt; ++c) {
+        a += fi[c] * fj[c];
+        b += fi[c] * fi[c];
+        cc += fj[c] * fj[c];
+      }
+      a = T.c1 + T.c2 * a;
+      b = T.c1 + T.c2 * b;
+      cc = T.c1 + T.c2 * cc;
+      return T.m2 * (2.0 / 3.14159265358979323846) * asin(2.0 * a / sqrt((1.0 + 2.0 * b) * (1.0 + 2.0 * cc)));
+    }
+    default: {
+      double r2 = 0.0;
+      for (int c = 0; c < T.dt; ++c) {
+        double df = fi[c] - fj[c];
+        r2 += df * df;
+      }
+      if (T.kind == GPGP_CF_SEXP) return T.m2 * exp(-0.5 * r2 * T.c1);
+      double a = T.c1 * sqrt(r2);
+      if (T.kind == GPGP_CF_MATERN32) return T.m2 * (1.0 + a) * exp(-a);
+      return T.m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp(-a);
+    }
+  }
+}
+
+// K(i, j) = sum over selected groups of the product of the group's terms.
+__device__ __forceinline__ double kernel_value(const DevKernel &dk, uint32_t gmask,
+                                               const double *fi, const double *fj) {
+  double sum = 0.0, prod = 1.0;
+  int g = dk.t[0].group;
+  for (int t = 0; t < dk.nterms; ++t) {
+    const DevTerm &T = dk.t[t];
+    if (T.group != g) {
+      if (gmask & (1u << g)) sum += prod;
+      prod = 1.0;
+      g = T.group;
+    }
+    prod *= term_value(T, fi + T.off, fj + T.off);
+  }
+  if (gmask & (1u << g)) sum += prod;
+  return sum;
+}
+
+// ---------------------------------------------------------------------------
+// tile generator
+// ---------------------------------------------------------------------------
+constexpr int CT = 64;  // tile edge
+
+__device__ __forceinline__ void tri_index(int64_t idx, int64_t *bi, int64_t *bj) {
+  // idx -> (bi, bj) with bi >= bj, row-major over the lower triangle of tiles
+  int64_t b = (int64_t)((sqrt(8.0 * (double)idx + 1.0) - 1.0) * 0.5);
+  while (b * (b + 1) / 2 > idx) --b;
+  while ((b + 1) * (b + 2) / 2 <= idx) ++b;
+  *bi = b;
+  *bj = idx - b * (b + 1) / 2;
+}
+
+__device__ __forceinline__ void load_feats(double *dst, int lds, const double *F, int64_t ld,
+                                           int64_t row0, int64_t n, int nfeat) {
+  for (int idx = threadIdx.x; idx < CT * nfeat; idx += blockDim.x) {
+    int r = idx % CT, c = idx / CT;
+    int64_t row = row0 + r;
+    dst[r * lds + c] = row < n ? F[row + c * ld] : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1, int64_t ld1, int64_t n1,
+                                const double *__restrict__ F2, int64_t ld2, int64_t n2,
+                                double *__restrict__ out, int64_t ldo, int mode, int sym,
+                                int mirror, double jitter, const double *__restrict__ scale) {
+  extern __shared__ double sm[];
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  double *Fi = sm;
+  double *Fj = sm + CT * lds;
+  double *Tt = sm + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  int64_t bi, bj;
+  if (sym)
+    tri_index(blockIdx.x, &bi, &bj);
+  else {
+    bi = blockIdx.x;
+    bj = blockIdx.y;
+  }
+  const int64_t i0 = bi * CT, j0 = bj * CT;
+  load_feats(Fi, lds, F1, ld1, i0, n1, nf);
+  load_feats(Fj, lds, F2, ld2, j0, n2, nf);
+  __syncthreads();
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  const double si = (mode == COV_ROWSCALE && i < n1) ? scale[i] : 1.0;
+  const bool do_mirror = sym && mirror && bi != bj;
+#pragma unroll 1
+  for (int q = 0; q < CT / 4; ++q) {
+    const int c = cb + 4 * q;
+    const int64_t j = j0 + c;
+    double v = 0.0;
+    if (i < n1 && j < n2) {
+      v = kernel_value(dk, gmask, Fi + r * lds, Fj + c * lds);
+      if (sym && i == j) v += jitter;
+      if (mode == COV_ROWSCALE) v = si * v;
+      out[i + j * ldo] = v;
+    }
+    if (do_mirror) Tt[c * (CT + 1) + r] = v;
+  }
+  if (do_mirror) {
+    __syncthreads();
+    // transposed tile: rows j0.., cols i0..
+#pragma unroll 1
+    for (int q = 0; q < CT / 4; ++q) {
+      const int rr = threadIdx.x % CT;  // row inside the transposed tile (j index)
+      const int cc = threadIdx.x / CT + 4 * q;  // col (i index)
+      const int64_t jj = j0 + rr, ii = i0 + cc;
+      if (jj < n2 && ii < n1) out[jj + ii * ldo] = Tt[rr * (CT + 1) + cc];
+    }
+  }
+}
+
+void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+                int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2, double *out,
+                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale) {
+  if (n1 == 0 || n2 == 0) return;
+  const int lds = (dk.nfeat | 1);
+  size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   2 * CT * 65 * 8 + CT * (CT + 1) * 8));
+    attr_set = true;
+  }
+  const int64_t T1 = (n1 + CT - 1) / CT, T2 = (n2 + CT - 1) / CT;
+  if (sym) {
+    int64_t nt = T1 * (T1 + 1) / 2;
+    cov_tile_kernel<<<(unsigned)nt, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out,
+                                                    ldo, mode, 1, mirror, jitter, scale);
+  } else {
+    dim3 grid((unsigned)T1, (unsigned)T2);
+    cov_tile_kernel<<<grid, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo,
+                                            mode, 0, 0, 0.0, scale);
+  }
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// diagonal
+// ---------------------------------------------------------------------------
+__global__ void cov_diag_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1,
+                                int64_t ld1, const double *__restrict__ F2, int64_t ld2,
+                                int64_t n, double *__restrict__ out) {
+  double fi[64], fj[64];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    for (int c = 0; c < dk.nfeat; ++c) {
+      fi[c] = F1[i + c * ld1];
+      fj[c] = F2[i + c * ld2];
+    }
+    out[i] = kernel_value(dk, gmask, fi, fj);
+  }
+}
+
+void cov_diag(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+              int64_t ld1, const double *F2, int64_t ld2, int64_t n, double *out) {
+  if (n == 0) return;
+  int64_t b = std::min<int64_t>((n + 127) / 128, 8192);
+  cov_diag_kernel<<<(unsigned)b, 128, 0, s>>>(dk, group_mask, F1, ld1, F2, ld2, n, out);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// fused K x v
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cov_matvec_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1, int64_t ld1, int64_t n1,
+                                  const double *__restrict__ F2, int64_t ld2, int64_t n2,
+                                  const double *__restrict__ v, double *__restrict__ out) {
+  extern __shared__ double sm[];
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  double *Fi = sm;
+  double *Fj = sm + CT * lds;
+  double *vj = sm + 2 * CT * lds;
+  double *red = vj + CT;  // 4 x CT partials
+  const int64_t i0 = (int64_t)blockIdx.x * CT;
+  load_feats(Fi, lds, F1, ld1, i0, n1, nf);
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  double acc = 0.0;
+  for (int64_t j0 = 0; j0 < n2; j0 += CT) {
+    __syncthreads();
+    load_feats(Fj, lds, F2, ld2, j0, n2, nf);
+    if (threadIdx.x < CT) vj[threadIdx.x] = (j0 + threadIdx.x < n2) ? v[j0 + threadIdx.x] : 0.0;
+    __syncthreads();
+    if (i0 + r < n1) {
+#pragma unroll 1
+      for (int q = 0; q < CT / 4; ++q) {
+        const int c = cb * (CT / 4) + q;
+        if (j0 + c < n2) acc += kernel_value(dk, gmask, Fi + r * lds, Fj + c * lds) * vj[c];
+      }
+    }
+  }
+  red[cb * CT + r] = acc;
+  __syncthreads();
+  if (threadIdx.x < CT && i0 + threadIdx.x < n1) {
+    double t = red[threadIdx.x];
+    for (int k = 1; k < 4; ++k) t += red[k * CT + threadIdx.x];
+    out[i0 + threadIdx.x] = t;
+  }
+}
+
+void cov_matvec(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
+                int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2,
+                const double *v, double *out) {
+  if (n1 == 0) return;
+  const int lds = (dk.nfeat | 1);
+  size_t smem = (size_t)(2 * CT * lds + CT + 4 * CT) * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (2 * CT * 65 + 5 * CT) * 8));
+    attr_set = true;
+  }
+  unsigned nb = (unsigned)((n1 + CT - 1) / CT);
+  cov_matvec_kernel<<<nb, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, v, out);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// gradient contraction
+// ---------------------------------------------------------------------------
+// Derivatives of one term with respect to the log of its parameters:
+// slot 0 lscale, 1 magn, 2 sigma0, 3 sigma, 4 period. fi/fj point at the
+// term's features; for periodic terms fi[2*nv + k] are the raw inputs.
+__device__ __forceinline__ double term_value_grad(const DevTerm &T, const double *fi,
+                                                  const double *fj, double dv[5]) {
+  dv[0] = dv[1] = dv[2] = dv[3] = dv[4] = 0.0;
+  double k;
+  switch (T.kind) {
+    case GPGP_CF_CONST:
+      k = T.m2;
+      dv[1] = 2.0 * k;
+      return k;
+    case GPGP_CF_LIN: {
+      double dot = 0.0;
+      for (int c = 0; c < T.dt; ++c) dot += fi[c] * fj[c];
+      k = T.m2 * dot;
+      dv[1] = 2.0 * k;
+      if (T.periodic) {
+        // sum_k cos(w (x_k - y_k)) -> d/dlog p = sum_k w d_k sin(w d_k)
+        double acc = 0.0;
+        for (int c = 0; c < T.nv; ++c) {
+          double dd = fi[2 * T.nv + c] - fj[2 * T.nv + c];
+          double sn = fi[c] * fj[T.nv + c] - fi[T.nv + c] * fj[c];  // sin(w dd)
+          acc += T.c2 * dd * sn;
+        }
+        dv[4] = T.m2 * acc;
+      }
+      return k;
+    }
+    case GPGP_CF_NN: {
+      double a = 0.0, b = 0.0, cc = 0.0;
+      for (int c = 0; c < T.dt; ++c) {
+        a += fi[c] * fj[c];
+        b += fi[c] * fi[c];
+        cc += fj[c] * fj[c];
+      }
+      a = T.c1 + T.c2 * a;
+      b = T.c1 + T.c2 * b;
+      cc = T.c1 + T.c2 * cc;
+      const double q = sqrt((1.0 + 2.0 * b) * (1.0 + 2.0 * cc));
+      const double u = 2.0 * a / q;
+      k = T.m2 * (2.0 / 3.14159265358979323846) * asin(u);
+      const double dk_du = T.m2 * (2.0 / 3.14159265358979323846) / sqrt(1.0 - u * u);
+      // d/dlog sigma0: da = db = dc = 2 s0
+      const double ds0 = 2.0 * T.c1;
+      double du = 2.0 * ds0 / q - u * (ds0 / (1.0 + 2.0 * b) + ds0 / (1.0 + 2.0 * cc));
+      dv[2] = dk_du * du;
+      // d/dlog sigma: da = 2a, db = 2b, dc = 2c
+      du = 4.0 * a / q - u * (2.0 * b / (1.0 + 2.0 * b) + 2.0 * cc / (1.0 + 2.0 * cc));
+      dv[3] = dk_du * du;
+      dv[1] = 2.0 * k;
+      return k;
+    }
+    default: {
+      double r2 = 0.0;
+      for (int c = 0; c < T.dt; ++c) {
+        double df = fi[c] - fj[c];
+        r2 += df * df;
+      }
+      double dk_dr2;
+      if (T.kind == GPGP_CF_SEXP) {
+        k = T.m2 * exp(-0.5 * r2 * T.c1);
+        dv[0] = k * r2 * T.c1;
+        dk_dr2 = -0.5 * T.c1 * k;
+      } else {
+        const double a = T.c1 * sqrt(r2);
+        const double e = exp(-a);
+        if (T.kind == GPGP_CF_MATERN32) {
+          k = T.m2 * (1.0 + a) * e;
+          dv[0] = T.m2 * a * a * e;
+          dk_dr2 = -0.5 * T.m2 * T.c1 * T.c1 * e;
+        } else {
+          k = T.m2 * (1.0 + a + a * a * (1.0 / 3.0)) * e;
+          dv[0] = T.m2 * a * a * (1.0 + a) * (1.0 / 3.0) * e;
+          dk_dr2 = -T.m2 * T.c1 * T.c1 * (1.0 / 6.0) * (1.0 + a) * e;
+        }
+      }
+      dv[1] = 2.0 * k;
+      if (T.periodic) {
+        // r2 = sum_k 2 - 2 cos(w d_k); d r2 / dlog p = -w sum_k 2 d_k sin(w d_k)
+        double acc = 0.0;
+        for (int c = 0; c < T.nv; ++c) {
+          double dd = fi[2 * T.nv + c] - fj[2 * T.nv + c];
+          double sn = fi[c] * fj[T.nv + c] - fi[T.nv + c] * fj[c];
+          acc += 2.0 * dd * sn;
+        }
+        dv[4] = dk_dr2 * (-T.c2 * acc);
+      }
+      return k;
+    }
+  }
+}
+
+constexpr int GT = 64;
+
+__global__ void __launch_bounds__(256) cov_grad_kernel(DevKernel dk, const double *__restrict__ F, int64_t ldf, int64_t n,
+                                const double *__restrict__ W, int64_t ldw,
+                                double *__restrict__ part) {
+  extern __shared__ double sm[];
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  double *Fi = sm;
+  double *Fj = sm + GT * lds;
+  double *red = sm + 2 * GT * lds;  // 256 doubles
+  int64_t bi, bj;
+  tri_index(blockIdx.x, &bi, &bj);
+  const int64_t i0 = bi * GT, j0 = bj * GT;
+  load_feats(Fi, lds, F, ldf, i0, n, nf);
+  load_feats(Fj, lds, F, ldf, j0, n, nf);
+  __syncthreads();
+  const int np = dk.nterms * GPGP_TERM_NPARAM;
+  double acc[GPGP_MAX_TERMS * GPGP_TERM_NPARAM];
+  for (int p = 0; p < np; ++p) acc[p] = 0.0;
+  const int r = threadIdx.x % GT;
+  const int cb = threadIdx.x / GT;
+  const int64_t i = i0 + r;
+  double kv[GPGP_MAX_TERMS];
+  double dv[GPGP_MAX_TERMS][GPGP_TERM_NPARAM];
+#pragma unroll 1
+  for (int q = 0; q < GT / 4; ++q) {
+    const int c = cb + 4 * q;
+    const int64_t j = j0 + c;
+    if (i >= n || j >= n || j > i) continue;
+    const double w = W[i + j * ldw] * (i == j ? 1.0 : 2.0);
+    for (int t = 0; t < dk.nterms; ++t)
+      kv[t] = term_value_grad(dk.t[t], Fi + r * lds + dk.t[t].off, Fj + c * lds + dk.t[t].off,
+                              dv[t]);
+    for (int t = 0; t < dk.nterms; ++t) {
+      double others = 1.0;
+      for (int u = 0; u < dk.nterms; ++u)
+        if (u != t && dk.t[u].group == dk.t[t].group) others *= kv[u];
+      const double f = w * others;
+      for (int p = 0; p < GPGP_TERM_NPARAM; ++p) acc[t * GPGP_TERM_NPARAM + p] += f * dv[t][p];
+    }
+  }
+  // block reduction per parameter, fixed order
+  for (int p = 0; p < np; ++p) {
+    red[threadIdx.x] = acc[p];
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * np + p] = red[0];
+    __syncthreads();
+  }
+}
+
+__global__ void reduce_partials_kernel(const double *__restrict__ part, int64_t nblocks, int np,
+                                       double *__restrict__ g) {
+  // one warp per parameter, fixed summation order
+  __shared__ double red[256];
+  for (int p = 0; p < np; ++p) {
+    double acc = 0.0;
+    for (int64_t b = threadIdx.x; b < nblocks; b += blockDim.x) acc += part[b * np + p];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) g[p] = red[0];
+    __syncthreads();
+  }
+}
+
+int64_t cov_grad_partials(int64_t n) {
+  int64_t T = (n + GT - 1) / GT;
+  return T * (T + 1) / 2 * GPGP_MAX_TERMS * GPGP_TERM_NPARAM;
+}
+
+gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double *F, int64_t ldf,
+                              int64_t n, const double *W, int64_t ldw, double *part, double *g) {
+  const int lds = (dk.nfeat | 1);
+  size_t smem = (size_t)(2 * GT * lds + 256) * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (2 * GT * 65 + 256) * 8));
+    attr_set = true;
+  }
+  int64_t T = (n + GT - 1) / GT;
+  int64_t nt = T * (T + 1) / 2;
+  cov_grad_kernel<<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+  GPGP_CHECK_LAUNCH();
+  reduce_partials_kernel<<<1, 256, 0, s>>>(part, nt, dk.nterms * GPGP_TERM_NPARAM, g);
+  GPGP_CHECK_LAUNCH();
+  return GPGP_OK;
+}
+
+}  // namespace gpgp

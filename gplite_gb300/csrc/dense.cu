@@ -1,0 +1,504 @@
+// Dense FP64 linear algebra for the GP hot path (column-major, lower factors).
+//
+// Replaces the LAPACK/BLAS calls the reference makes from R: chol (dpotrf,
+// R/laplace.R:28, R/ep.R:38, R/linear_algebra.R:28), forwardsolve/backsolve
+// (dtrsv/dtrsm, R/laplace.R:29, R/gp_pred.R:218) and %*% (dgemm/dgemv,
+// R/laplace.R:30, R/gp_pred.R:209).
+//
+// The factorisation is blocked right-looking with NB = 64: the diagonal block
+// is factored by one CTA in shared memory, which also inverts it; the panel
+// below is the product with that inverse (stable here because every diagonal
+// block of B = I + V^-1/2 K V^-1/2 has eigenvalues >= 1); the trailing update
+// is a lower-only GEMM. Only the trailing update is a contraction worth the
+// tensor cores; on this part the plain FP64 path runs it on the FP64 pipe.
+#include <math.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace gpgp {
+
+// ---------------------------------------------------------------------------
+// FP64 GEMM: C = alpha op(A) op(B) + beta C, 64x64 tiles, 4x4 per thread
+// ---------------------------------------------------------------------------
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64_t K, double alpha,
+                                                     const double *__restrict__ A, int64_t lda,
+                                                     const double *__restrict__ B, int64_t ldb,
+                                                     double beta, double *__restrict__ C,
+                                                     int64_t ldc, int lower_only, int tri_mode) {
+  const int64_t bm = blockIdx.x, bn = blockIdx.y;
+  const int64_t row0 = bm * GBM, col0 = bn * GBN;
+  if (lower_only && col0 > row0 + GBM - 1) return;
+  __shared__ double As[GBK][GBM + 1];
+  __shared__ double Bs[GBK][GBN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  int64_t kstart = 0;
+  if (tri_mode == 1) kstart = (row0 / GBK) * GBK;  // W^T W with W lower: k >= row
+  for (int64_t k0 = kstart; k0 < K; k0 += GBK) {
+    // load A tile: op(A) is M x K
+#pragma unroll
+    for (int e = 0; e < (GBM * GBK) / 256; ++e) {
+      int idx = tid + e * 256;
+      int r, kk;
+      if (!TA) {
+        r = idx % GBM;
+        kk = idx / GBM;
+      } else {
+        kk = idx % GBK;
+        r = idx / GBK;
+      }
+      int64_t gr = row0 + r, gk = k0 + kk;
+      double v = 0.0;
+      if (gr < M && gk < K) v = TA ? A[gk + gr * lda] : A[gr + gk * lda];
+      As[kk][r] = v;
+    }
+    // load B tile: op(B) is K x N
+#pragma unroll
+    for (int e = 0; e < (GBN * GBK) / 256; ++e) {
+      int idx = tid + e * 256;
+      int c, kk;
+      if (!TB) {
+        kk = idx % GBK;
+        c = idx / GBK;
+      } else {
+        c = idx % GBN;
+        kk = idx / GBN;
+      }
+      int64_t gc = col0 + c, gk = k0 + kk;
+      double v = 0.0;
+      if (gc < N && gk < K) v = TB ? B[gc + gk * ldb] : B[gk + gc * ldb];
+      Bs[kk][c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = As[kk][tx + 16 * q];
+        b[q] = Bs[kk][ty + 16 * q];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int64_t r = row0 + tx + 16 * p, c = col0 + ty + 16 * q;
+      if (r < M && c < N && (!lower_only || r >= c)) {
+        double *dst = C + r + c * ldc;
+        *dst = (beta == 0.0) ? alpha * acc[p][q] : alpha * acc[p][q] + beta * *dst;
+      }
+    }
+  }
+}
+
+void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+            const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+            int64_t ldc, bool lower_only, int tri_mode) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid((unsigned)((M + GBM - 1) / GBM), (unsigned)((N + GBN - 1) / GBN));
+  int lo = lower_only ? 1 : 0;
+  if (!ta && !tb)
+    gemm64_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
+  else if (!ta && tb)
+    gemm64_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
+  else if (ta && !tb)
+    gemm64_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
+  else
+    gemm64_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// diagonal block: factor + invert in shared memory (one CTA)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
+                                                         double *__restrict__ Winv,
+                                                         double *__restrict__ logdet_part,
+                                                         int *__restrict__ status, int64_t k0) {
+  __shared__ double S[NB][NB + 1];
+  __shared__ double Wsm[NB][NB + 1];
+  __shared__ int failed;
+  if (*(volatile int *)status != 0) return;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    int r = idx % NB, c = idx / NB;
+    S[r][c] = (r < kb && c < kb && r >= c) ? A[r + c * lda] : 0.0;
+    Wsm[r][c] = 0.0;
+  }
+  if (tid == 0) failed = 0;
+  __syncthreads();
+  for (int j = 0; j < kb; ++j) {
+    if (tid == 0) {
+      double d = S[j][j];
+      if (!(d > 0.0) || !isfinite(d)) {
+        failed = 1;
+        atomicCAS(status, 0, (int)(k0 + j + 1));
+      } else {
+        S[j][j] = sqrt(d);
+      }
+    }
+    __syncthreads();
+    if (failed) return;
+    const double piv = S[j][j];
+    for (int r = j + 1 + tid; r < kb; r += 256) S[r][j] = S[r][j] / piv;
+    __syncthreads();
+    const int m = kb - j - 1;
+    for (int idx = tid; idx < m * m; idx += 256) {
+      int r = j + 1 + idx % m, c = j + 1 + idx / m;
+      if (r >= c) S[r][c] -= S[r][j] * S[c][j];
+    }
+    __syncthreads();
+  }
+  // write the factor back (lower part of the block)
+  for (int idx = tid; idx < kb * kb; idx += 256) {
+    int r = idx % kb, c = idx / kb;
+    if (r >= c) A[r + c * lda] = S[r][c];
+  }
+  // inverse of the lower factor, one column per thread (forward substitution)
+  if (tid < kb) {
+    const int c = tid;
+    Wsm[c][c] = 1.0 / S[c][c];
+    for (int r = c + 1; r < kb; ++r) {
+      double sum = 0.0;
+      for (int k = c; k < r; ++k) sum = fma(S[r][k], Wsm[k][c], sum);
+      Wsm[r][c] = -sum / S[r][r];
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    int r = idx % NB, c = idx / NB;
+    Winv[r + c * NB] = Wsm[r][c];
+  }
+  if (tid == 0) {
+    double ls = 0.0;
+    for (int j = 0; j < kb; ++j) ls += log(S[j][j]);
+    *logdet_part = ls;
+  }
+}
+
+// panel: L21 = A21 * W^T for 64 rows per CTA (in place)
+__global__ void __launch_bounds__(256) potrf_panel_kernel(double *__restrict__ A21, int64_t m, int kb,
+                                                          int64_t lda, const double *__restrict__ W,
+                                                          const int *__restrict__ status) {
+  __shared__ double P[NB][NB + 1];
+  __shared__ double Ws[NB][NB + 1];
+  if (*(volatile const int *)status != 0) return;
+  const int64_t r0 = (int64_t)blockIdx.x * NB;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    int r = idx % NB, c = idx / NB;
+    P[r][c] = (r0 + r < m && c < kb) ? A21[(r0 + r) + c * lda] : 0.0;
+    Ws[r][c] = W[r + c * NB];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    int r = idx % NB, c = idx / NB;
+    if (r0 + r < m && c < kb) {
+      double sum = 0.0;
+      for (int k = 0; k <= c; ++k) sum = fma(P[r][k], Ws[c][k], sum);
+      A21[(r0 + r) + c * lda] = sum;
+    }
+  }
+}
+
+void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
+           int *status) {
+  for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    double *Akk = A + k0 + k0 * lda;
+    double *W = Winv + blk * NB * NB;
+    potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0);
+    GPGP_CHECK_LAUNCH();
+    const int64_t m = n - k0 - kb;
+    if (m > 0) {
+      double *A21 = A + (k0 + kb) + k0 * lda;
+      potrf_panel_kernel<<<(unsigned)((m + NB - 1) / NB), 256, 0, s>>>(A21, m, kb, lda, W, status);
+      GPGP_CHECK_LAUNCH();
+      double *A22 = A + (k0 + kb) + (k0 + kb) * lda;
+      gemm64(s, false, true, m, m, kb, -1.0, A21, lda, A21, lda, 1.0, A22, lda, true, 0);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves with one right-hand side
+// ---------------------------------------------------------------------------
+// Step k of the forward solve: every CTA recomputes xk = W_kk b_k (64x64), CTA 0
+// stores it into xo, and each CTA updates its 256-row slice of b below the block.
+__global__ void __launch_bounds__(256) trsv_fwd_step(const double *__restrict__ L, int64_t n, int64_t lda,
+                                                     const double *__restrict__ W, int64_t k0, int kb,
+                                                     double *__restrict__ b, double *__restrict__ xo,
+                                                     const int *__restrict__ status) {
+  __shared__ double bk[NB];
+  __shared__ double xk[NB];
+  if (*(volatile const int *)status != 0) return;
+  const int tid = threadIdx.x;
+  if (tid < NB) bk[tid] = tid < kb ? b[k0 + tid] : 0.0;
+  __syncthreads();
+  if (tid < NB) {
+    double s = 0.0;
+    for (int c = 0; c <= tid && c < kb; ++c) s = fma(W[tid + c * NB], bk[c], s);
+    xk[tid] = tid < kb ? s : 0.0;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && tid < kb) xo[k0 + tid] = xk[tid];
+  const int64_t r = k0 + kb + (int64_t)blockIdx.x * 256 + tid;
+  if (r < n) {
+    double s = 0.0;
+    for (int c = 0; c < kb; ++c) s = fma(L[r + (k0 + c) * lda], xk[c], s);
+    b[r] -= s;
+  }
+}
+
+void trsv_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                double *b, double *x, const int *status) {
+  // b is consumed (rows below the current block are updated in place); x receives L^-1 b
+  for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    const int64_t rest = n - k0 - kb;
+    unsigned g = (unsigned)std::max<int64_t>(1, (rest + 255) / 256);
+    trsv_fwd_step<<<g, 256, 0, s>>>(L, n, lda, Winv + blk * NB * NB, k0, kb, b, x, status);
+    GPGP_CHECK_LAUNCH();
+  }
+}
+
+// Backward step: x_k = W_kk^T b_k, then b[0:k0] -= L[k-block rows, 0:k0]^T x_k.
+__global__ void __launch_bounds__(256) trsv_bwd_step(const double *__restrict__ L, int64_t lda,
+                                                     const double *__restrict__ W, int64_t k0, int kb,
+                                                     double *__restrict__ b, double *__restrict__ xo,
+                                                     const int *__restrict__ status) {
+  __shared__ double bk[NB];
+  __shared__ double xk[NB];
+  if (*(volatile const int *)status != 0) return;
+  const int tid = threadIdx.x;
+  if (tid < NB) bk[tid] = tid < kb ? b[k0 + tid] : 0.0;
+  __syncthreads();
+  if (tid < NB) {
+    double s = 0.0;
+    for (int r = tid; r < kb; ++r) s = fma(W[r + tid * NB], bk[r], s);
+    xk[tid] = tid < kb ? s : 0.0;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && tid < kb) xo[k0 + tid] = xk[tid];
+  // one warp per column c < k0
+  const int lane = tid & 31, warp = tid >> 5;
+  const int64_t c = (int64_t)blockIdx.x * 8 + warp;
+  if (c < k0) {
+    double s = 0.0;
+    for (int r = lane; r < kb; r += 32) s = fma(L[(k0 + r) + c * lda], xk[r], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) b[c] -= s;
+  }
+}
+
+void trsv_lower_t(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                  double *b, double *x, const int *status) {
+  // b is consumed; x receives L^-T b
+  const int64_t nblk = (n + NB - 1) / NB;
+  for (int64_t blk = nblk - 1; blk >= 0; --blk) {
+    const int64_t k0 = blk * NB;
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    unsigned g = (unsigned)std::max<int64_t>(1, (k0 + 7) / 8);
+    trsv_bwd_step<<<g, 256, 0, s>>>(L, lda, Winv + blk * NB * NB, k0, kb, b, x, status);
+    GPGP_CHECK_LAUNCH();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// multi-RHS solve and triangular inverse
+// ---------------------------------------------------------------------------
+void trsm_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                double *B, int64_t m, int64_t ldb, double *tmp, const int *status) {
+  // right-looking: X_k = W_kk B_k; B_rest -= L_rest,k X_k. tmp holds NB x m.
+  (void)status;
+  for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    double *Bk = B + k0;
+    gemm64(s, false, false, kb, m, kb, 1.0, Winv + blk * NB * NB, NB, Bk, ldb, 0.0, tmp, NB);
+    GPGP_CUDA(cudaMemcpy2DAsync(Bk, ldb * sizeof(double), tmp, NB * sizeof(double),
+                                kb * sizeof(double), m, cudaMemcpyDeviceToDevice, s));
+    const int64_t rest = n - k0 - kb;
+    if (rest > 0)
+      gemm64(s, false, false, rest, m, kb, -1.0, L + (k0 + kb) + k0 * lda, lda, tmp, NB, 1.0,
+             B + k0 + kb, ldb);
+  }
+}
+
+__global__ void set_identity_kernel(double *W, int64_t n, int64_t ldw) {
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      W[i + j * ldw] = (i == j) ? 1.0 : 0.0;
+}
+
+void trtri_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                 double *Wout, int64_t ldw, double *tmp, const int *status) {
+  // Wout = L^-1 by a triangular solve against I that skips the zero columns:
+  // for block row k, X_k = W_kk B_k[:, 0:k0+kb] and B_rest[:, 0:k0+kb] -= L_rest,k X_k.
+  // tmp holds NB x n. The strict upper triangle of Wout stays exactly zero.
+  (void)status;
+  if (n == 0) return;
+  dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
+  set_identity_kernel<<<g, 256, 0, s>>>(Wout, n, ldw);
+  GPGP_CHECK_LAUNCH();
+  for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    const int64_t ncol = k0 + kb;
+    double *Bk = Wout + k0;
+    gemm64(s, false, false, kb, ncol, kb, 1.0, Winv + blk * NB * NB, NB, Bk, ldw, 0.0, tmp, NB);
+    GPGP_CUDA(cudaMemcpy2DAsync(Bk, ldw * sizeof(double), tmp, NB * sizeof(double),
+                                kb * sizeof(double), ncol, cudaMemcpyDeviceToDevice, s));
+    const int64_t rest = n - ncol;
+    if (rest > 0)
+      gemm64(s, false, false, rest, ncol, kb, -1.0, L + ncol + k0 * lda, lda, tmp, NB, 1.0,
+             Wout + ncol, ldw);
+  }
+}
+
+// column sums of squares of a lower-triangular W (diag of W^T W)
+__global__ void col_sumsq_lower_kernel(const double *__restrict__ W, int64_t n, int64_t ldw,
+                                       double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= n) return;
+  double s = 0.0;
+  for (int64_t r = c + lane; r < n; r += 32) {
+    double v = W[r + c * ldw];
+    s = fma(v, v, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[c] = s;
+}
+
+void col_sumsq_lower(cudaStream_t s, const double *W, int64_t n, int64_t ldw, double *out) {
+  if (n == 0) return;
+  col_sumsq_lower_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(W, n, ldw, out);
+  GPGP_CHECK_LAUNCH();
+}
+
+__global__ void col_sumsq_kernel(const double *__restrict__ B, int64_t n, int64_t m, int64_t ldb,
+                                 double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= m) return;
+  double s = 0.0;
+  for (int64_t r = lane; r < n; r += 32) {
+    double v = B[r + c * ldb];
+    s = fma(v, v, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[c] = s;
+}
+
+void col_sumsq(cudaStream_t s, const double *B, int64_t n, int64_t m, int64_t ldb, double *out) {
+  if (m == 0) return;
+  col_sumsq_kernel<<<(unsigned)((m * 32 + 255) / 256), 256, 0, s>>>(B, n, m, ldb, out);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// GEMV with a deterministic two-stage reduction over column chunks
+// ---------------------------------------------------------------------------
+constexpr int GV_ROWS = 256, GV_COLS = 1024;
+
+__global__ void gemv_n_kernel(int64_t M, int64_t N, const double *__restrict__ A, int64_t lda,
+                              const double *__restrict__ x, double *__restrict__ part) {
+  const int64_t r = (int64_t)blockIdx.x * GV_ROWS + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * GV_COLS;
+  const int64_t c1 = (c0 + GV_COLS < N) ? c0 + GV_COLS : N;
+  if (r >= M) return;
+  double s = 0.0;
+  for (int64_t c = c0; c < c1; ++c) s = fma(A[r + c * lda], x[c], s);
+  part[r + blockIdx.y * M] = s;
+}
+
+__global__ void gemv_t_kernel(int64_t M, int64_t N, const double *__restrict__ A, int64_t lda,
+                              const double *__restrict__ x, double *__restrict__ y, double alpha,
+                              double beta) {
+  // y[c] = alpha * sum_r A[r, c] x[r] + beta y[c]; one warp per column
+  const int lane = threadIdx.x & 31;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= N) return;
+  double s = 0.0;
+  for (int64_t r = lane; r < M; r += 32) s = fma(A[r + c * lda], x[r], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) y[c] = (beta == 0.0) ? alpha * s : alpha * s + beta * y[c];
+}
+
+__global__ void gemv_reduce_kernel(int64_t M, int nchunk, const double *__restrict__ part,
+                                   double alpha, double beta, double *__restrict__ y) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  double s = 0.0;
+  for (int k = 0; k < nchunk; ++k) s += part[r + k * M];
+  y[r] = (beta == 0.0) ? alpha * s : alpha * s + beta * y[r];
+}
+
+// scratch for the row-major partials lives right after y's owner provides; we
+// allocate a small cached buffer per process for it.
+static double *g_gemv_part = nullptr;
+static size_t g_gemv_part_n = 0;
+
+void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, const double *A,
+            int64_t lda, const double *x, double beta, double *y) {
+  if (trans) {
+    if (N == 0) return;
+    gemv_t_kernel<<<(unsigned)((N * 32 + 255) / 256), 256, 0, s>>>(M, N, A, lda, x, y, alpha, beta);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
+  if (M == 0) return;
+  const int nchunk = (int)std::max<int64_t>(1, (N + GV_COLS - 1) / GV_COLS);
+  size_t need = (size_t)M * nchunk;
+  if (need > g_gemv_part_n) {
+    if (g_gemv_part) GPGP_CUDA(cudaFreeAsync(g_gemv_part, s));
+    GPGP_CUDA(cudaMallocAsync((void **)&g_gemv_part, need * sizeof(double), s));
+    g_gemv_part_n = need;
+  }
+  dim3 grid((unsigned)((M + GV_ROWS - 1) / GV_ROWS), (unsigned)nchunk);
+  gemv_n_kernel<<<grid, GV_ROWS, 0, s>>>(M, N, A, lda, x, g_gemv_part);
+  GPGP_CHECK_LAUNCH();
+  gemv_reduce_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(M, nchunk, g_gemv_part, alpha,
+                                                                  beta, y);
+  GPGP_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__global__ void sum_vec_kernel(const double *__restrict__ v, int64_t n, double *__restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) s += v[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out) {
+  sum_vec_kernel<<<1, 256, 0, s>>>(v, n, out);
+  GPGP_CHECK_LAUNCH();
+}
+
+}  // namespace gpgp

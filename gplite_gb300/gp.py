@@ -1,0 +1,560 @@
+"""gplite's user API on top of libgpgp: gp_init, gp_fit, gp_energy, gp_pred,
+gp_loo, gp_compare, gp_optim, get_param / set_param.
+
+Same names, argument meanings, defaults and error behaviour as the R package
+(R/gp.R:52-205, R/gp_fit.R:54-60, R/gp_pred.R:88-122, R/gp_loo.R:73-175,
+R/gp_optim.R:63-160); the numerical work of fit / pred / LOO runs in the CUDA
+library through the C ABI (include/gpgp.h). Only O(p) host logic (parameter
+packing, priors, learn_scales, the optimiser loop) runs in Python.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+
+import numpy as np
+
+from . import _lib as L
+from .objects import (GRAD_SLOT, Cf, approx_ep, approx_laplace, cf_sexp, lik_gaussian,
+                      method_full)
+
+JITTER_DEFAULT = 1e-6  # get_jitter (R/gp.R:276-281)
+
+
+class GP:
+    """A GP model (the reference's list of class "gp", R/gp.R:57-69)."""
+
+    def __init__(self, cfs, lik, method, approx):
+        self.cfs = cfs
+        self.lik = lik
+        self.method = method
+        self.approx = approx
+        self.fitted = False
+        self.fit = None
+        self.x = None
+        self._model = None
+
+    def __del__(self):
+        self._free()
+
+    def _free(self):
+        m = getattr(self, "_model", None)
+        if m:
+            try:
+                L.load().gpgp_model_free(m)
+            except Exception:
+                pass
+        self._model = None
+
+    def __repr__(self):
+        return ("Likelihood:\n  %r\nCovariance functions:\n%s\nMethod:\n  %r\nLatent approximation:\n  %r"
+                % (self.lik, "\n".join("  %r" % c for c in self.cfs), self.method, self.approx))
+
+
+def gp_init(cfs=None, lik=None, method=None, approx=None) -> GP:
+    """gp_init (R/gp.R:52-71)."""
+    cfs = cf_sexp() if cfs is None else cfs
+    lik = lik_gaussian() if lik is None else lik
+    method = method_full() if method is None else method
+    approx = approx_laplace() if approx is None else approx
+    if lik.kind == "gaussian" and approx.kind == "ep":
+        raise ValueError("approx_ep disabled for lik_gaussian: use approx_laplace instead, because it "
+                         "gives exact results")
+    if isinstance(cfs, Cf):
+        cfs = [cfs]
+    return GP(list(cfs), lik, method, approx)
+
+
+# ----------------------------------------------------------------------------
+# parameters (R/gp.R:149-169)
+# ----------------------------------------------------------------------------
+
+def get_param(gp):
+    """get_param.gp: log-parameters, cfs in order then the likelihood; returns (names, values)."""
+    names, vals = [], []
+    for c in gp.cfs:
+        n_, v_ = c.get_param()
+        names += n_
+        vals += v_
+    n_, v_ = gp.lik.get_param()
+    return names + n_, np.array(vals + v_, dtype=np.float64)
+
+
+def set_param(gp, param):
+    """set_param.gp: sets log-parameters and marks the model as needing a refit."""
+    param = list(np.asarray(param, dtype=np.float64).ravel())
+    j = 0
+    for c in gp.cfs:
+        j += c.set_param(param[j:])
+    j += gp.lik.set_param(param[j:])
+    if j != len(param):
+        raise ValueError("expected %d parameters, got %d" % (j, len(param)))
+    gp.fitted = False
+    return gp
+
+
+def lpdf_prior(gp):
+    return sum(c.lpdf_prior() for c in gp.cfs) + gp.lik.lpdf_prior()
+
+
+def _dlpdf_prior(gp):
+    out = []
+    for c in gp.cfs:
+        out += c.dlpdf_prior()
+    return np.array(out + gp.lik.dlpdf_prior(), dtype=np.float64)
+
+
+# ----------------------------------------------------------------------------
+# translation to the C ABI
+# ----------------------------------------------------------------------------
+
+def _flat_terms(gp):
+    """(group, cf) for every device term, in parameter order."""
+    out = []
+    for g, c in enumerate(gp.cfs):
+        for t in (c.cfs if c.kind == "prod" else [c]):
+            out.append((g, t))
+    return out
+
+
+def _fill_term(T, g, c, d):
+    T.group = g
+    periodic = c.kind == "periodic"
+    base = c.base if periodic else c
+    T.kind = L.CF_KIND[base.kind]
+    T.periodic = 1 if periodic else 0
+    T.normalize = 1 if (getattr(c, "normalize", False) and c.means is not None and not periodic) else 0
+    if c.vars is not None:
+        if len(c.vars) > L.MAX_VARS:
+            raise ValueError("too many vars in one covariance function")
+        T.nvars = len(c.vars)
+        for i, v in enumerate(c.vars):
+            if not 0 <= v < d:
+                raise ValueError("vars index %d out of range for d = %d" % (v, d))
+            T.vars[i] = v
+    else:
+        T.nvars = 0
+    if T.normalize:
+        for i, (mu, sd) in enumerate(zip(np.atleast_1d(c.means), np.atleast_1d(c.scales))):
+            T.means[i] = mu
+            T.scales[i] = sd
+    T.lscale = getattr(base, "lscale", 1.0)
+    T.magn = getattr(base, "magn", 1.0)
+    T.sigma0 = getattr(base, "sigma0", 0.0)
+    T.sigma = getattr(base, "sigma", 0.0)
+    T.period = getattr(c, "period", 1.0)
+
+
+def kernel_struct(cfs, d):
+    gp = GP(cfs, None, None, None)
+    terms = _flat_terms(gp)
+    if len(terms) > L.MAX_TERMS:
+        raise ValueError("at most %d covariance terms are supported" % L.MAX_TERMS)
+    k = L.Kernel()
+    k.nterms = len(terms)
+    k.ngroups = len(cfs)
+    for i, (g, c) in enumerate(terms):
+        _fill_term(k.term[i], g, c, d)
+    return k
+
+
+def _lik_struct(lik):
+    s = L.Lik()
+    s.kind = L.LIK_KIND[lik.kind]
+    s.link = L.LINK[lik.link]
+    s.sigma = getattr(lik, "sigma", 0.0)
+    s.phi = getattr(lik, "phi", 0.0)
+    return s
+
+
+def _approx_struct(gp):
+    a = L.Approx()
+    ap = gp.approx
+    a.kind = L.APPROX[ap.kind]
+    a.maxiter = ap.maxiter
+    if ap.kind == "laplace":
+        a.tol = ap.tol
+    else:  # fit_ep.method_full / method_fitc (R/gp_fit.R:150-161, R/ep.R:333-335)
+        a.tol = 1e-4 if gp.method.kind == "full" else 1e-3
+        a.damping = ap.damping
+        a.damping_min = 0.1
+        a.quad_order = ap.quad_order
+    return a
+
+
+def _as_x(x):
+    x = np.asarray(x, dtype=np.float64)
+    return x.reshape(-1, 1) if x.ndim == 1 else x
+
+
+def learn_scales(gp, x):
+    """learn_scales.gp (R/cf.R:831-855)."""
+    for c in gp.cfs:
+        c.learn_scales(x)
+
+
+# ----------------------------------------------------------------------------
+# fit / energy
+# ----------------------------------------------------------------------------
+
+def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", device=0):
+    """gp_fit (R/gp_fit.R:54-60): posterior approximation with the current hyperparameters."""
+    x = _as_x(x)
+    y = np.ascontiguousarray(y, dtype=np.float64).ravel()
+    n, d = x.shape
+    if len(y) != n:
+        raise ValueError("x and y have different numbers of rows")
+    if gp.lik.kind == "binomial" and trials is None:
+        raise ValueError("trials must be provided for the binomial likelihood.")
+    learn_scales(gp, x)
+    lib = L.load()
+    ctx = L.default_context(device)
+    k = kernel_struct(gp.cfs, d)
+    lk = _lik_struct(gp.lik)
+    me = L.Method()
+    me.kind = L.METHOD[gp.method.kind]
+    ind = None
+    if gp.method.kind == "fitc":
+        if gp.method.inducing is None:
+            raise NotImplementedError("method_fitc needs explicit inducing points (k-means placement "
+                                      "is not implemented)")
+        ind = L.fortran(gp.method.inducing)
+        me.num_inducing = ind.shape[0]
+        me.inducing = ind.ctypes.data
+    ap = _approx_struct(gp)
+    op = L.FitOpts()
+    op.jitter = JITTER_DEFAULT if jitter is None else float(jitter)
+    op.precision = L.PRECISION[precision]
+    op.refine_iters = 2
+    xf = L.fortran(x)
+    tr = None if trials is None else np.ascontiguousarray(trials, dtype=np.float64)
+    of = None if offset is None else np.ascontiguousarray(np.broadcast_to(offset, (n,)), dtype=np.float64)
+    h = C.c_void_p()
+    res = L.FitResult()
+    gp._free()
+    st = lib.gpgp_fit(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf), n, d,
+                      L.ptr(y), L.ptr(tr), L.ptr(of), C.byref(h), C.byref(res))
+    L.check(st, ctx.h)
+    if res.status == L.EMAXITER and gp.approx.kind == "ep":
+        warnings.warn("Maximum number of iterations in EP reached")
+    elif res.converged == 0 and gp.approx.kind == "laplace":
+        warnings.warn("Maximum number of iterations in Laplace reached")
+    gp._model = h
+    gp.x = x
+    gp.fit = dict(type="analytic", log_evidence=res.log_evidence, iters=res.iters,
+                  quad_ok=bool(res.quad_ok), status=res.status, jitter=op.jitter, n=n,
+                  y=y, trials=tr, offset=of)
+    gp.fitted = True
+    return gp
+
+
+def _is_fitted(gp):
+    """is_fitted.gp (R/gp.R:191-205)."""
+    found = isinstance(gp.fit, dict) and gp.fit.get("type") == "analytic"
+    if found and not gp.fitted:
+        raise RuntimeError("The GP object seems to contain a posterior fit, but is not refitted after "
+                           "setting new hyperparameter values. Please refit using gp_fit after calling "
+                           "set_param.")
+    return found
+
+
+def gp_energy(gp, include_prior=True):
+    """gp_energy (R/gp.R:138-147): -log evidence - log prior."""
+    if not _is_fitted(gp):
+        raise RuntimeError("The GP must be fitted. Call gp_fit first.")
+    e = -gp.fit["log_evidence"]
+    if include_prior:
+        e = e - lpdf_prior(gp)
+    return e
+
+
+def model_field(gp, name):
+    """Copy a resident vector of the fit (alpha, fmean, z, V, fvar, cavity_mean, cavity_var)."""
+    if not _is_fitted(gp):
+        raise RuntimeError("The GP must be fitted. Call gp_fit first.")
+    out = np.empty(gp.fit["n"])
+    st = L.load().gpgp_model_get(gp._model, L.FIELD[name], L.ptr(out))
+    L.check(st, None)
+    return out
+
+
+def gp_energy_grad(gp, include_prior=True):
+    """Gradient of gp_energy with respect to the log-parameters (get_param order).
+
+    New functionality: the reference optimises without gradients. It is
+    -(1/2) tr((alpha alpha^T - C^-1) dC/dtheta) - dlog prior/dtheta, computed on
+    the device for lik_gaussian with method_full.
+    """
+    if not _is_fitted(gp):
+        raise RuntimeError("The GP must be fitted. Call gp_fit first.")
+    terms = _flat_terms(gp)
+    gt = np.zeros(len(terms) * L.TERM_NPARAM)
+    gs = C.c_double(0.0)
+    st = L.load().gpgp_model_grad(gp._model, L.ptr(gt), C.byref(gs))
+    L.check(st, None)
+    g = []
+    for ti, (grp, c) in enumerate(terms):
+        if c.kind == "periodic":
+            if not c.is_fixed("period"):
+                g.append(gt[ti * L.TERM_NPARAM + GRAD_SLOT["period"]])
+            for nme in c.base.param_names():
+                g.append(gt[ti * L.TERM_NPARAM + GRAD_SLOT[nme]])
+        else:
+            for nme in c.param_names():
+                g.append(gt[ti * L.TERM_NPARAM + GRAD_SLOT[nme]])
+    if gp.lik.kind == "gaussian" and not gp.lik.is_fixed("sigma"):
+        g.append(gs.value)
+    g = -np.array(g, dtype=np.float64)
+    if include_prior:
+        g = g - _dlpdf_prior(gp)
+    return g
+
+
+# ----------------------------------------------------------------------------
+# prediction (R/gp_pred.R:88-156)
+# ----------------------------------------------------------------------------
+
+def _group_mask(gp, cfind):
+    if cfind is None:
+        return 0
+    m = 0
+    for k in np.atleast_1d(cfind):
+        m |= 1 << int(k)
+    return m
+
+
+def _eval_cf(cfs, x1, x2, diag_only=False, cfind_mask=0, device=0):
+    x1 = _as_x(x1)
+    x2 = _as_x(x2)
+    d = x1.shape[1]
+    k = kernel_struct(cfs, d)
+    n1, n2 = x1.shape[0], x2.shape[0]
+    out = np.empty(min(n1, n2)) if diag_only else np.empty((n1, n2), order="F")
+    ctx = L.default_context(device)
+    a, b = L.fortran(x1), L.fortran(x2)
+    st = L.load().gpgp_eval_cf(ctx.h, C.byref(k), L.ptr(a), n1, L.ptr(b), n2, d, int(diag_only),
+                               cfind_mask, out.ctypes.data_as(C.c_void_p))
+    L.check(st, ctx.h)
+    return out
+
+
+def eval_cf(cfs, x1, x2, cfind=None, diag_only=False):
+    """eval_cf.list (R/cf.R:402-411) on the device; cfs is a covariance function or a list."""
+    if isinstance(cfs, Cf):
+        cfs = [cfs]
+    mask = 0 if cfind is None else sum(1 << int(k) for k in np.atleast_1d(cfind))
+    return _eval_cf(list(cfs), x1, x2, diag_only, mask)
+
+
+def gp_pred(gp, xnew, var=False, quantiles=None, transform=False, cfind=None, jitter=None,
+            quad_order=15, offset=None):
+    """gp_pred (R/gp_pred.R:88-122)."""
+    from scipy.stats import norm
+
+    xnew = _as_x(xnew)
+    if quantiles is not None or transform:
+        var = True
+    m = xnew.shape[0]
+    if not _is_fitted(gp):
+        # gp_pred_prior.method_full / method_fitc (R/gp_pred.R:142-184)
+        pred = dict(mean=np.zeros(m))
+        if var:
+            if gp.method.kind == "fitc" and gp.method.inducing is None:
+                raise RuntimeError("Inducing points not set yet.")
+            if gp.method.kind == "fitc":
+                raise NotImplementedError("prior prediction with method_fitc")
+            pred["var"] = eval_cf(gp.cfs, xnew, xnew, cfind, diag_only=True)
+    else:
+        mean = np.empty(m)
+        vv = np.empty(m) if var else None
+        xf = L.fortran(xnew)
+        st = L.load().gpgp_pred(gp._model, L.ptr(xf), m, _group_mask(gp, cfind), L.ptr(mean), L.ptr(vv))
+        L.check(st, None)
+        pred = dict(mean=mean)
+        if var:
+            pred["var"] = vv
+    if offset is not None:
+        pred["mean"] = pred["mean"] + offset
+    if quantiles is not None:
+        q = np.stack([norm.ppf(qq, loc=pred["mean"], scale=np.sqrt(pred["var"])) for qq in quantiles], 1)
+        if transform:
+            q = gp.lik.response(q)
+        pred["quantiles"] = q
+    if transform:
+        x, w = gauss_hermite_points(quad_order)
+        fg = x[None, :] * np.sqrt(pred["var"])[:, None] + pred["mean"][:, None]
+        ft = gp.lik.response(fg)
+        mt = ft @ w
+        pred["mean"] = mt
+        pred["var"] = ((ft - mt[:, None]) ** 2) @ w
+    return pred
+
+
+def gauss_hermite_points(p):
+    """gauss_hermite_points (R/quadrature.R:28-34) on the host (used by transform)."""
+    c = np.zeros((p + 1, p + 1))
+    c[0, 0] = 1.0
+    if p >= 1:
+        c[1, 1] = 1.0
+    for i in range(2, p + 1):
+        c[i, 1:] = c[i - 1, :-1]
+        c[i, :] -= (i - 1) * c[i - 2, :]
+    x = np.sort(np.real(np.roots(c[p, ::-1])))
+    for _ in range(3):
+        x = x - np.polyval(c[p, ::-1], x) / np.polyval(np.polyder(c[p, ::-1]), x)
+    w = math.factorial(p) / (p * p * np.polyval(c[p - 1, ::-1], x) ** 2)
+    return x, w
+
+
+# ----------------------------------------------------------------------------
+# LOO (R/gp_loo.R:73-175)
+# ----------------------------------------------------------------------------
+
+def gp_loo(gp, x, y, quadrature=True, quad_order=11, draws=4000, jitter=None, seed=None, **kw):
+    """gp_loo (R/gp_loo.R:73-109) with Gauss-Hermite quadrature, on the fitted data."""
+    if not _is_fitted(gp):
+        raise RuntimeError("The provied GP model is not fitted. Please call gp_fit (or gp_optim) first.")
+    if not quadrature:
+        raise NotImplementedError("Monte Carlo LOO (quadrature = FALSE) is not implemented")
+    x = _as_x(x)
+    y = np.asarray(y, dtype=np.float64).ravel()
+    if x.shape != gp.x.shape or not np.array_equal(x, gp.x) or not np.array_equal(y, gp.fit["y"]):
+        raise ValueError("gp_loo on the device uses the data the model was fitted to")
+    n = len(y)
+    loos = np.empty(n)
+    s = C.c_double(0.0)
+    st = L.load().gpgp_loo(gp._model, int(quad_order), L.ptr(loos), C.byref(s))
+    L.check(st, None)
+    return dict(loo=float(loos.sum()), sd=float(n * (np.std(loos, ddof=1) / math.sqrt(n))), loos=loos)
+
+
+def gp_compare(*loos, ref=None):
+    """gp_compare (R/gp_loo.R:149-175): LOO differences and their standard errors."""
+    vals = np.array([r["loo"] for r in loos])
+    if ref is None:
+        ref = int(np.argmax(vals))
+    n = len(loos[0]["loos"])
+    res = np.zeros((len(loos), 2))
+    for i, r in enumerate(loos):
+        dd = r["loos"] - loos[ref]["loos"]
+        res[i, 0] = n * dd.mean()
+        res[i, 1] = n * (np.std(dd, ddof=1) / math.sqrt(n))
+    return res
+
+
+# ----------------------------------------------------------------------------
+# optimisation (R/gp_optim.R:63-160)
+# ----------------------------------------------------------------------------
+
+def _nelder_mead(fn, x0, reltol, maxit, fnscale):
+    """Nelder-Mead in the form of R's optim defaults (reflection 1, contraction 0.5,
+    expansion 2, initial step 10% of the largest |x0| component or 0.1,
+    convergence when the simplex spread is below reltol * (|f_low| + reltol) on
+    the fnscale-scaled objective)."""
+    n = len(x0)
+    f = lambda p: fn(p) / fnscale  # noqa: E731
+    step = 0.1 * max(np.max(np.abs(x0)), 1.0) if n else 0.1
+    P = [np.array(x0, dtype=np.float64)]
+    for i in range(n):
+        p = P[0].copy()
+        p[i] += step
+        P.append(p)
+    F = [f(p) for p in P]
+    evals = n + 1
+    conv = 1
+    while evals < maxit:
+        order = np.argsort(F)
+        P = [P[i] for i in order]
+        F = [F[i] for i in order]
+        if F[-1] <= F[0] + reltol * (abs(F[0]) + reltol):
+            conv = 0
+            break
+        cen = np.mean(P[:-1], axis=0)
+        xr = cen + (cen - P[-1])
+        fr = f(xr)
+        evals += 1
+        if fr < F[0]:
+            xe = cen + 2.0 * (cen - P[-1])
+            fe = f(xe)
+            evals += 1
+            if fe < fr:
+                P[-1], F[-1] = xe, fe
+            else:
+                P[-1], F[-1] = xr, fr
+        elif fr < F[-2]:
+            P[-1], F[-1] = xr, fr
+        else:
+            if fr < F[-1]:
+                P[-1], F[-1] = xr, fr
+            xc = cen + 0.5 * (P[-1] - cen)
+            fc = f(xc)
+            evals += 1
+            if fc < F[-1]:
+                P[-1], F[-1] = xc, fc
+            else:
+                for i in range(1, n + 1):
+                    P[i] = P[0] + 0.5 * (P[i] - P[0])
+                    F[i] = f(P[i])
+                    evals += 1
+    i = int(np.argmin(F))
+    return P[i], F[i] * fnscale, conv
+
+
+def _check_convergence(lossfun, loss_opt, param_opt, delta=1e-1, tol=1e-2):
+    """check_convergence (R/gp_optim.R:127-160): +-delta probes per parameter."""
+    for k in range(len(param_opt)):
+        dp = np.zeros(len(param_opt))
+        dp[k] = delta
+        if loss_opt - min(lossfun(param_opt + dp), lossfun(param_opt - dp)) > tol:
+            return False, ("Not all hyperparameters have reached convergence within tolerance "
+                           "tol_param = %f. Try increasing the number of restarts, or reducing tol." % delta)
+    return True, "Optimization converged."
+
+
+def gp_optim(gp, x, y, tol=1e-4, tol_param=1e-1, maxiter=500, restarts=1, verbose=True, warnings_=True,
+             method="nelder-mead", **fit_args):
+    """gp_optim (R/gp_optim.R:63-125). method="nelder-mead" follows the reference;
+    method="lbfgs" uses the device energy gradient (lik_gaussian, method_full)."""
+    it = [0]
+
+    def energy(param):
+        set_param(gp, param)
+        try:
+            gp_fit(gp, x, y, **fit_args)
+        except np.linalg.LinAlgError:
+            return np.inf
+        e = gp_energy(gp)
+        if verbose:
+            print(" ".join("%8.2f" % p for p in param), "%10.2f" % e, "%9d" % it[0])
+        it[0] += 1
+        return e
+
+    _, p0 = get_param(gp)
+    n = len(np.atleast_1d(y))
+    if method == "lbfgs":
+        from scipy.optimize import minimize
+
+        def fg(param):
+            e = energy(param)
+            return e, gp_energy_grad(gp)
+
+        r = minimize(fg, p0, jac=True, method="L-BFGS-B", options=dict(maxiter=maxiter, ftol=tol / n))
+        p_opt, e_opt = r.x, r.fun
+    else:
+        p_opt, e_opt, conv = _nelder_mead(energy, p0, tol, maxiter, n)
+        if conv == 1 and warnings_:
+            warnings.warn("Maximum number of iterations reached, optimization may not have converged.")
+    set_param(gp, p_opt)
+    gp_fit(gp, x, y, **fit_args)
+    if warnings_:
+        ok, msg = _check_convergence(energy, e_opt, p_opt, delta=tol_param)
+        set_param(gp, p_opt)
+        gp_fit(gp, x, y, **fit_args)
+        if not ok:
+            if restarts > 0:
+                return gp_optim(gp, x, y, tol=tol, tol_param=tol_param, maxiter=maxiter,
+                                restarts=restarts - 1, verbose=verbose, warnings_=warnings_,
+                                method=method, **fit_args)
+            warnings.warn(msg)
+    return gp

@@ -1,0 +1,258 @@
+/*
+ * gpgp.h -- C ABI of the GB300 Gaussian-process library (libgpgp.so).
+ *
+ * This is the drop-in boundary for gplite's GP hot path. The R package
+ * gplite binds exactly four native routines today (src/RcppExports.cpp:76-87:
+ * _gplite_cf_sexp_c, _gplite_cf_matern32_c, _gplite_cf_matern52_c,
+ * _gplite_cf_nn_c); everything else is R calling LAPACK. The functions below
+ * keep those four covariance routines (gpgp_cf_*) and add whole-fit entry
+ * points that replace the S3 seams fit_model / gp_pred_post / loo_posteriors
+ * (R/gp_fit.R:62-188, R/gp_pred.R:129-296, R/gp_loo.R:111-133), so that the
+ * covariance, Cholesky, solves and evidence never leave the GPU.
+ *
+ * Conventions
+ *  - Matrices are column-major double, like R matrices: x is n-by-d with
+ *    element (i, k) at x[i + k*n].
+ *  - Host-pointer entry points copy inputs in and results out; *_dev entry
+ *    points take device pointers that stay owned by the caller.
+ *  - The library owns device memory of contexts and models. A context is
+ *    bound to one device and one stream and is not thread-safe; use one
+ *    context per host thread.
+ *  - Every call returns a gpgp_status; no call aborts or traps. Numerical
+ *    failures the reference maps to log_evidence = -Inf (non-PD factor,
+ *    NaN sites, EP max-iterations) are reported in gpgp_fit_result and the
+ *    log_evidence field, exactly where the reference does.
+ */
+#ifndef GPGP_H
+#define GPGP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPGP_MAX_VARS 16
+#define GPGP_MAX_TERMS 16
+#define GPGP_TERM_NPARAM 5 /* lscale, magn, sigma0, sigma, period */
+
+typedef enum gpgp_status {
+  GPGP_OK = 0,
+  GPGP_ENOT_PD = 1,       /* Cholesky met a non-positive pivot (see result.info) */
+  GPGP_ENAN = 2,          /* NaN/Inf in inputs or in site parameters */
+  GPGP_EMAXITER = 3,      /* iteration limit reached (Laplace / EP) */
+  GPGP_EUNSUPPORTED = 4,  /* combination not implemented (e.g. non-log-concave branch) */
+  GPGP_EOOM = 5,          /* device allocation failed or budget exceeded */
+  GPGP_ETIMEOUT = 6,      /* a bounded device wait ran out */
+  GPGP_ECUDA = 7,         /* CUDA runtime error (message in gpgp_last_error) */
+  GPGP_EINVAL = 8,        /* invalid argument */
+  GPGP_ENOT_FITTED = 9,   /* model handle has no fit */
+  GPGP_EBUSY = 10         /* server queue full / request not finished */
+} gpgp_status;
+
+/* Covariance function kinds (R/cf.R:92-195, src/cf.cpp). cf_periodic is a
+ * flag on a term (inputs mapped to sin/cos of 2*pi*x/period, R/cf.R:478-489)
+ * whose kind is that of its base kernel; cf_prod is expressed with groups. */
+typedef enum gpgp_cf_kind {
+  GPGP_CF_CONST = 0,
+  GPGP_CF_LIN = 1,
+  GPGP_CF_SEXP = 2,
+  GPGP_CF_MATERN32 = 3,
+  GPGP_CF_MATERN52 = 4,
+  GPGP_CF_NN = 5
+} gpgp_cf_kind;
+
+/* One covariance term. Terms with the same group id are multiplied
+ * (eval_cf.cf_prod, R/cf.R:491-497); groups are summed (eval_cf.list,
+ * R/cf.R:402-411). Group ids are 0..ngroups-1 and terms of one group are
+ * contiguous. Parameter values are natural (not log). */
+typedef struct gpgp_cf_term {
+  int32_t kind;      /* gpgp_cf_kind (of the base kernel when periodic) */
+  int32_t group;     /* product group == index of the cf in the gp's cfs list */
+  int32_t periodic;  /* 1: cf_periodic wrapping this base kernel */
+  int32_t normalize; /* 1: (x - means) / scales before use (R/misc.R:17-31) */
+  int32_t nvars;     /* number of input columns used; 0 = all d columns */
+  int32_t vars[GPGP_MAX_VARS];     /* 0-based column indices */
+  double means[GPGP_MAX_VARS];     /* learn_scales output (R/cf.R:836-845) */
+  double scales[GPGP_MAX_VARS];
+  double lscale, magn, sigma0, sigma, period;
+} gpgp_cf_term;
+
+typedef struct gpgp_kernel {
+  int32_t nterms;
+  int32_t ngroups;
+  gpgp_cf_term term[GPGP_MAX_TERMS];
+} gpgp_kernel;
+
+typedef enum gpgp_lik_kind {
+  GPGP_LIK_GAUSSIAN = 0,
+  GPGP_LIK_BERNOULLI = 1,
+  GPGP_LIK_BINOMIAL = 2,
+  GPGP_LIK_POISSON = 3,
+  GPGP_LIK_BETABINOM = 4
+} gpgp_lik_kind;
+
+typedef enum gpgp_link {
+  GPGP_LINK_IDENTITY = 0,
+  GPGP_LINK_LOGIT = 1,
+  GPGP_LINK_PROBIT = 2,
+  GPGP_LINK_LOG = 3
+} gpgp_link;
+
+/* Likelihood (R/lik.R:44-90). */
+typedef struct gpgp_lik {
+  int32_t kind;
+  int32_t link;
+  double sigma; /* lik_gaussian noise sd */
+  double phi;   /* lik_betabinom over-dispersion */
+} gpgp_lik;
+
+typedef enum gpgp_method_kind { GPGP_METHOD_FULL = 0, GPGP_METHOD_FITC = 1 } gpgp_method_kind;
+
+/* Method (R/method.R:105-125). For FITC the inducing inputs are given
+ * explicitly (M-by-d column-major, host memory for gpgp_fit, device memory
+ * for gpgp_fit_dev). */
+typedef struct gpgp_method {
+  int32_t kind;
+  int32_t num_inducing;
+  const double *inducing;
+} gpgp_method;
+
+typedef enum gpgp_approx_kind { GPGP_APPROX_LAPLACE = 0, GPGP_APPROX_EP = 1 } gpgp_approx_kind;
+
+/* Latent approximation (R/approx.R:60-75); EP also uses damping_min and tol
+ * (R/gp_fit.R:150-161: damping_min 0.1, tol 1e-4 full / 1e-3 FITC). */
+typedef struct gpgp_approx {
+  int32_t kind;
+  int32_t maxiter;
+  double tol;
+  double damping;
+  double damping_min;
+  int32_t quad_order;
+} gpgp_approx;
+
+typedef enum gpgp_precision {
+  GPGP_PREC_FP64 = 0,  /* plain: FP64 throughout */
+  GPGP_PREC_MIXED = 1  /* BF16-split tensor-core updates, FP64 diagonal blocks,
+                          FP64 log-determinant and FP64 iterative refinement */
+} gpgp_precision;
+
+typedef struct gpgp_fit_opts {
+  double jitter;        /* diagonal jitter (R/gp.R:276-281 default 1e-6) */
+  int32_t precision;    /* gpgp_precision */
+  int32_t refine_iters; /* FP64 iterative-refinement steps for alpha (mixed) */
+} gpgp_fit_opts;
+
+typedef struct gpgp_fit_result {
+  double log_evidence; /* -Inf where the reference returns -Inf */
+  int32_t status;      /* gpgp_status of the numerical outcome */
+  int32_t iters;       /* Laplace / EP iterations used */
+  int64_t info;        /* first non-PD pivot (1-based) when status == GPGP_ENOT_PD */
+  int32_t quad_ok;     /* EP quadrature produced no NaN (R/lik.R:250-257) */
+  int32_t converged;   /* 0 if the iteration limit was reached */
+} gpgp_fit_result;
+
+typedef struct gpgp_ctx gpgp_ctx;
+typedef struct gpgp_model gpgp_model;
+
+/* ---- context ---------------------------------------------------------- */
+gpgp_status gpgp_create(gpgp_ctx **ctx, int device);
+gpgp_status gpgp_destroy(gpgp_ctx *ctx);
+const char *gpgp_status_string(gpgp_status s);
+const char *gpgp_last_error(const gpgp_ctx *ctx);
+/* Kernel launches issued by this context since creation (evidence counter). */
+int64_t gpgp_launch_count(const gpgp_ctx *ctx);
+/* Synchronise the context's stream. */
+gpgp_status gpgp_sync(gpgp_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void *gpgp_stream(gpgp_ctx *ctx);
+
+/* ---- live profiling: CUDA events recorded on the context's stream around
+ *      each phase of the hot path; read back as total milliseconds and
+ *      call counts per phase. Enabling resets the accumulators. ----------- */
+typedef enum gpgp_phase {
+  GPGP_PHASE_COV = 0,      /* covariance matrix generation */
+  GPGP_PHASE_POTRF = 1,    /* blocked Cholesky */
+  GPGP_PHASE_SOLVE = 2,    /* triangular solves for alpha, K alpha */
+  GPGP_PHASE_TRTRI = 3,    /* triangular inverse */
+  GPGP_PHASE_LAUUM = 4,    /* B^-1 = L^-T L^-1 */
+  GPGP_PHASE_GRAD = 5,     /* gradient contraction */
+  GPGP_PHASE_PRED_MEAN = 6,
+  GPGP_PHASE_PRED_VAR = 7, /* cross covariance + multi-RHS solve */
+  GPGP_NPHASE = 8
+} gpgp_phase;
+gpgp_status gpgp_profile_enable(gpgp_ctx *ctx, int32_t on);
+gpgp_status gpgp_profile_read(gpgp_ctx *ctx, double *ms, int64_t *calls);
+
+/* ---- covariance routines: replace src/cf.cpp:9-162 (registered at
+ *      src/RcppExports.cpp:76-87). Host buffers; x1 n1-by-d, x2 n2-by-d
+ *      column-major; out n1-by-n2 column-major, or min(n1,n2) if diag_only.
+ *      They run on an internal context for device 0. ---------------------- */
+gpgp_status gpgp_cf_sexp(const double *x1, int64_t n1, const double *x2, int64_t n2, int32_t d,
+                         double lscale, double magn, int32_t diag_only, double *out);
+gpgp_status gpgp_cf_matern32(const double *x1, int64_t n1, const double *x2, int64_t n2,
+                             int32_t d, double lscale, double magn, int32_t diag_only,
+                             double *out);
+gpgp_status gpgp_cf_matern52(const double *x1, int64_t n1, const double *x2, int64_t n2,
+                             int32_t d, double lscale, double magn, int32_t diag_only,
+                             double *out);
+gpgp_status gpgp_cf_nn(const double *x1, int64_t n1, const double *x2, int64_t n2, int32_t d,
+                       double sigma0, double sigma, double magn, int32_t diag_only, double *out);
+
+/* eval_cf.list (R/cf.R:402-411) for a whole kernel; group_mask selects the
+ * cfs (bit g = group g; 0 = all), like the cfind argument. Host buffers. */
+gpgp_status gpgp_eval_cf(gpgp_ctx *ctx, const gpgp_kernel *k, const double *x1, int64_t n1,
+                         const double *x2, int64_t n2, int32_t d, int32_t diag_only,
+                         uint32_t group_mask, double *out);
+
+/* ---- fit: replaces gp_fit -> fit_model (R/gp_fit.R:54-188) ------------- */
+/* Host buffers: x n-by-d, y n, trials n or NULL, offset n or NULL. The model
+ * keeps x, y, the factor and the site parameters resident on the device. */
+gpgp_status gpgp_fit(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                     const gpgp_method *method, const gpgp_approx *approx,
+                     const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                     const double *y, const double *trials, const double *offset,
+                     gpgp_model **model, gpgp_fit_result *result);
+/* Same, with x, y, trials, offset (and method->inducing) in device memory. */
+gpgp_status gpgp_fit_dev(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                         const gpgp_method *method, const gpgp_approx *approx,
+                         const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                         const double *y, const double *trials, const double *offset,
+                         gpgp_model **model, gpgp_fit_result *result);
+gpgp_status gpgp_model_free(gpgp_model *model);
+
+/* Gradient of log_evidence with respect to the log of every term parameter
+ * (GPGP_TERM_NPARAM slots per term, order lscale, magn, sigma0, sigma,
+ * period; unused slots are 0) and of log lik->sigma. Gaussian likelihood,
+ * full method. This is tr((alpha alpha^T - C^-1) dC/dtheta)/2; the reference
+ * has no gradient (it optimises with Nelder-Mead, R/gp_optim.R:94). */
+gpgp_status gpgp_model_grad(gpgp_model *model, double *grad_terms, double *grad_lik_sigma);
+
+/* Copy a resident model vector out to host memory (length n unless noted). */
+typedef enum gpgp_model_field {
+  GPGP_FIELD_ALPHA = 0,
+  GPGP_FIELD_FMEAN = 1,
+  GPGP_FIELD_Z = 2,
+  GPGP_FIELD_V = 3,
+  GPGP_FIELD_FVAR = 4,        /* EP posterior marginal variances */
+  GPGP_FIELD_CAVITY_MEAN = 5, /* EP */
+  GPGP_FIELD_CAVITY_VAR = 6   /* EP */
+} gpgp_model_field;
+gpgp_status gpgp_model_get(gpgp_model *model, int32_t field, double *out);
+
+/* ---- prediction: replaces gp_pred_post.method_full / method_fitc
+ *      (R/gp_pred.R:202-296). xt m-by-d; mean m; var m or NULL. ---------- */
+gpgp_status gpgp_pred(gpgp_model *model, const double *xt, int64_t m, uint32_t group_mask,
+                      double *mean, double *var);
+gpgp_status gpgp_pred_dev(gpgp_model *model, const double *xt, int64_t m, uint32_t group_mask,
+                          double *mean, double *var);
+
+/* ---- LOO: replaces loo_posteriors + the quadrature of gp_loo
+ *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
+gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPGP_H */

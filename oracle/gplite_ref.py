@@ -1,0 +1,1012 @@
+"""FP64 NumPy/SciPy restatement of gplite's GP hot path (TEST INFRASTRUCTURE ONLY).
+
+Every function restates one reference function, named in its docstring by
+file:line of the R package gplite 0.13.0 (paths relative to the package root).
+Matrices follow R's conventions: inputs are n-by-d, column-major semantics are
+irrelevant here because NumPy holds the values; ``chol`` is R's upper factor,
+``t(chol(B))`` the lower one. Formula order follows the reference (B
+factorisation, log-evidence expression), not textbook shortcuts, so that the
+CUDA library can be held to 1e-10 against it.
+
+Objects are duck-typed: a covariance function is any object with attributes
+``kind`` ('const', 'lin', 'sexp', 'matern32', 'matern52', 'nn', 'periodic',
+'prod'), ``vars`` (None or 0-based column indices), ``normalize``, ``means``,
+``scales``, ``priors`` (dict name -> prior) and its parameters by name
+(``lscale``, ``magn``, ``sigma0``, ``sigma``, ``period``); ``base`` for
+periodic, ``cfs`` for products. A likelihood has ``kind`` ('gaussian',
+'bernoulli', 'binomial', 'betabinom', 'poisson'), ``link`` and its parameters.
+The constructors at the bottom build such objects without the product package.
+
+Parity: see the package docstring (pinned to the reference's closed-form
+known-answer tests; Laplace/EP/FITC values partially unpinned).
+"""
+from __future__ import annotations
+
+import math
+import warnings
+from types import SimpleNamespace
+
+import numpy as np
+from scipy import linalg as sla
+from scipy import special as sps
+
+# ----------------------------------------------------------------------------
+# parameters (R/cf.R:283-396, R/lik.R:118-168, R/gp.R:149-165, R/misc.R:33-56)
+# ----------------------------------------------------------------------------
+
+PARAM_NAMES = {
+    "const": ["magn"],
+    "lin": ["magn"],
+    "sexp": ["lscale", "magn"],
+    "matern32": ["lscale", "magn"],
+    "matern52": ["lscale", "magn"],
+    "nn": ["sigma0", "sigma", "magn"],
+    "periodic": ["period"],
+    "gaussian": ["sigma"],
+    "bernoulli": [],
+    "binomial": [],
+    "betabinom": ["phi"],
+    "poisson": [],
+}
+
+
+def _is_fixed(obj, name):
+    """is_fixed (R/misc.R:33-39)."""
+    pr = getattr(obj, "priors", {}) or {}
+    p = pr.get(name)
+    return p is not None and p.kind == "fixed"
+
+
+def _obj_name(obj, is_lik=False):
+    return ("lik_" if is_lik else "cf_") + obj.kind
+
+
+def get_param_cf(cf):
+    """get_param.cf / .cf_periodic / .cf_prod (R/cf.R:313-344)."""
+    if cf.kind == "prod":
+        names, vals = [], []
+        for c in cf.cfs:
+            n_, v_ = get_param_cf(c)
+            names += n_
+            vals += v_
+        return names, vals
+    if cf.kind == "periodic":
+        n_, v_ = get_param_cf(cf.base)
+        n_ = ["cf_periodic." + s.split(".", 1)[1] for s in n_]
+        if not _is_fixed(cf, "period"):
+            n_ = ["cf_periodic.period"] + n_
+            v_ = [math.log(cf.period)] + v_
+        return n_, v_
+    names, vals = [], []
+    for nm in PARAM_NAMES[cf.kind]:
+        if _is_fixed(cf, nm):
+            continue
+        names.append(_obj_name(cf) + "." + nm)
+        vals.append(math.log(getattr(cf, nm)))
+    return names, vals
+
+
+def get_param_lik(lik):
+    """get_param.lik (R/lik.R:146-155)."""
+    names, vals = [], []
+    for nm in PARAM_NAMES[lik.kind]:
+        if _is_fixed(lik, nm):
+            continue
+        names.append(_obj_name(lik, True) + "." + nm)
+        vals.append(math.log(getattr(lik, nm)))
+    return names, vals
+
+
+def get_param(gp):
+    """get_param.gp (R/gp.R:149-155): cfs in declared order, then likelihood."""
+    names, vals = [], []
+    for cf in gp.cfs:
+        n_, v_ = get_param_cf(cf)
+        names += n_
+        vals += v_
+    n_, v_ = get_param_lik(gp.lik)
+    return names + n_, np.array(vals + v_, dtype=np.float64)
+
+
+def _set_param_cf(cf, vals):
+    """set_param.cf / .cf_periodic / .cf_prod (R/cf.R:348-396). Returns #consumed."""
+    if cf.kind == "prod":
+        j = 0
+        for c in cf.cfs:
+            j += _set_param_cf(c, vals[j:])
+        return j
+    if cf.kind == "periodic":
+        j = 0
+        if not _is_fixed(cf, "period"):
+            cf.period = math.exp(vals[0])
+            j = 1
+        return j + _set_param_cf(cf.base, vals[j:])
+    j = 0
+    for nm in PARAM_NAMES[cf.kind]:
+        if _is_fixed(cf, nm):
+            continue
+        setattr(cf, nm, math.exp(vals[j]))
+        j += 1
+    return j
+
+
+def set_param(gp, vals):
+    """set_param.gp (R/gp.R:158-165); marks the model as not fitted."""
+    vals = list(np.asarray(vals, dtype=np.float64))
+    j = 0
+    for cf in gp.cfs:
+        j += _set_param_cf(cf, vals[j:])
+    for nm in PARAM_NAMES[gp.lik.kind]:
+        if _is_fixed(gp.lik, nm):
+            continue
+        setattr(gp.lik, nm, math.exp(vals[j]))
+        j += 1
+    gp.fitted = False
+    return gp
+
+
+# ----------------------------------------------------------------------------
+# priors (R/priors.R:96-112)
+# ----------------------------------------------------------------------------
+
+def lpdf_prior_one(prior, param):
+    """lpdf_prior.prior_* (R/priors.R:96-112)."""
+    if prior is None or prior.kind in ("fixed", "logunif"):
+        return 0.0
+    if prior.kind == "half_t":
+        theta = math.exp(param)
+        df, sc = prior.df, prior.scale
+        t = theta / sc
+        # stats::dt(t, df, log=TRUE)
+        ldt = (sps.gammaln((df + 1) / 2) - sps.gammaln(df / 2) - 0.5 * math.log(df * math.pi)
+               - (df + 1) / 2 * math.log1p(t * t / df))
+        return math.log(2) - math.log(sc) + ldt + param
+    if prior.kind == "lognormal":
+        return -0.5 * math.log(2 * math.pi) - math.log(prior.scale) - 0.5 * ((param - prior.loc) / prior.scale) ** 2
+    raise ValueError(prior.kind)
+
+
+def _lpdf_prior_cf(cf):
+    """lpdf_prior.cf / .cf_prod / .cf_periodic (R/cf.R:503-528)."""
+    if cf.kind == "prod":
+        return sum(_lpdf_prior_cf(c) for c in cf.cfs)
+    if cf.kind == "periodic":
+        lp = 0.0
+        if not _is_fixed(cf, "period"):
+            lp += lpdf_prior_one(cf.priors.get("period"), math.log(cf.period))
+        return lp + _lpdf_prior_cf(cf.base)
+    lp = 0.0
+    for nm in PARAM_NAMES[cf.kind]:
+        if _is_fixed(cf, nm):
+            continue
+        lp += lpdf_prior_one(cf.priors.get(nm), math.log(getattr(cf, nm)))
+    return lp
+
+
+def lpdf_prior(gp):
+    """lpdf_prior.gp (R/gp.R:167-169)."""
+    lp = sum(_lpdf_prior_cf(cf) for cf in gp.cfs)
+    for nm in PARAM_NAMES[gp.lik.kind]:
+        if not _is_fixed(gp.lik, nm):
+            lp += lpdf_prior_one(gp.lik.priors.get(nm), math.log(getattr(gp.lik, nm)))
+    return lp
+
+
+# ----------------------------------------------------------------------------
+# inputs and covariance functions (R/misc.R:17-31, R/cf.R:402-497, src/cf.cpp)
+# ----------------------------------------------------------------------------
+
+def as_matrix(x):
+    x = np.asarray(x, dtype=np.float64)
+    return x.reshape(-1, 1) if x.ndim == 1 else x
+
+
+def prepare_inputmat(cf, x):
+    """prepare_inputmat (R/misc.R:17-31): column subset, then (x - mean) / scale."""
+    x = as_matrix(x)
+    if cf.vars is not None:
+        x = x[:, list(cf.vars)]
+    if getattr(cf, "normalize", False) and getattr(cf, "means", None) is not None \
+            and getattr(cf, "scales", None) is not None:
+        x = (x - np.asarray(cf.means)) / np.asarray(cf.scales)
+    return x
+
+
+def learn_scales(cfs, x):
+    """learn_scales.cf / .cf_prod / .cf_periodic (R/cf.R:824-855): colMeans, sd (n-1)."""
+    x = as_matrix(x)
+    for cf in cfs:
+        if cf.kind == "prod":
+            learn_scales(cf.cfs, x)
+        elif cf.kind == "periodic":
+            continue
+        else:
+            xs = x if cf.vars is None else x[:, list(cf.vars)]
+            cf.means = xs.mean(axis=0)
+            cf.scales = xs.std(axis=0, ddof=1)
+
+
+def _sqdist(x1, x2):
+    # sum(square(x1.row(i) - x2.row(j))) accumulated over columns in order (src/cf.cpp:37)
+    r2 = np.zeros((x1.shape[0], x2.shape[0]))
+    for k in range(x1.shape[1]):
+        diff = x1[:, k][:, None] - x2[:, k][None, :]
+        r2 += diff * diff
+    return r2
+
+
+def _sqdist_diag(x1, x2):
+    n = min(x1.shape[0], x2.shape[0])
+    r2 = np.zeros(n)
+    for k in range(x1.shape[1]):
+        diff = x1[:n, k] - x2[:n, k]
+        r2 += diff * diff
+    return r2
+
+
+def cf_sexp_c(x1, x2, lscale, magn, diag_only=False):
+    """cf_sexp_c (src/cf.cpp:9-42)."""
+    r2 = _sqdist_diag(x1, x2) if diag_only else _sqdist(x1, x2)
+    return magn * magn * np.exp(-0.5 * r2 / (lscale * lscale))
+
+
+def cf_matern32_c(x1, x2, lscale, magn, diag_only=False):
+    """cf_matern32_c (src/cf.cpp:48-80)."""
+    r = np.sqrt(_sqdist_diag(x1, x2) if diag_only else _sqdist(x1, x2))
+    return magn * magn * (1.0 + math.sqrt(3.0) * r / lscale) * np.exp(-math.sqrt(3.0) * r / lscale)
+
+
+def cf_matern52_c(x1, x2, lscale, magn, diag_only=False):
+    """cf_matern52_c (src/cf.cpp:86-119)."""
+    r = np.sqrt(_sqdist_diag(x1, x2) if diag_only else _sqdist(x1, x2))
+    return magn * magn * (1.0 + math.sqrt(5.0) * r / lscale + 5.0 * r * r / (3.0 * lscale * lscale)) \
+        * np.exp(-math.sqrt(5.0) * r / lscale)
+
+
+def cf_nn_c(x1, x2, sigma0, sigma, magn, diag_only=False):
+    """cf_nn_c (src/cf.cpp:125-162)."""
+    s0 = sigma0 * sigma0 * sigma * sigma
+    a1 = x1 * sigma
+    a2 = x2 * sigma
+    if diag_only:
+        n = min(a1.shape[0], a2.shape[0])
+        a1, a2 = a1[:n], a2[:n]
+        a = s0 + (a1 * a2).sum(1)
+        b = s0 + (a1 * a1).sum(1)
+        c = s0 + (a2 * a2).sum(1)
+    else:
+        a = s0 + a1 @ a2.T
+        b = (s0 + (a1 * a1).sum(1))[:, None]
+        c = (s0 + (a2 * a2).sum(1))[None, :]
+    return magn * magn * (2.0 / math.pi) * np.arcsin(2 * a / np.sqrt((1 + 2 * b) * (1 + 2 * c)))
+
+
+def eval_cf_one(cf, x1, x2, diag_only=False):
+    """eval_cf.cf_* (R/cf.R:413-497)."""
+    if cf.kind == "prod":
+        K = 1.0
+        for c in cf.cfs:
+            K = K * eval_cf_one(c, x1, x2, diag_only)
+        return K
+    x1 = prepare_inputmat(cf, x1)
+    x2 = prepare_inputmat(cf, x2)
+    n1, n2 = x1.shape[0], x2.shape[0]
+    if cf.kind == "const":
+        if diag_only:
+            return np.full(min(n1, n2), cf.magn ** 2)
+        return np.full((n1, n2), cf.magn ** 2)
+    if cf.kind == "lin":
+        K = cf.magn ** 2 * (x1 @ x2.T)
+        return np.diag(K).copy() if diag_only else K
+    if cf.kind == "sexp":
+        return cf_sexp_c(x1, x2, cf.lscale, cf.magn, diag_only)
+    if cf.kind == "matern32":
+        return cf_matern32_c(x1, x2, cf.lscale, cf.magn, diag_only)
+    if cf.kind == "matern52":
+        return cf_matern52_c(x1, x2, cf.lscale, cf.magn, diag_only)
+    if cf.kind == "nn":
+        return cf_nn_c(x1, x2, cf.sigma0, cf.sigma, cf.magn, diag_only)
+    if cf.kind == "periodic":
+        w = 2 * math.pi / cf.period
+        t1 = np.hstack([np.sin(w * x1), np.cos(w * x1)])
+        t2 = np.hstack([np.sin(w * x2), np.cos(w * x2)])
+        return eval_cf_one(cf.base, t1, t2, diag_only)
+    raise ValueError(cf.kind)
+
+
+def eval_cf(cfs, x1, x2, cfind=None, diag_only=False):
+    """eval_cf.list (R/cf.R:402-411): sum over the selected covariance functions."""
+    idx = range(len(cfs)) if cfind is None else cfind
+    K = 0.0
+    for k in idx:
+        K = K + eval_cf_one(cfs[k], x1, x2, diag_only)
+    return K
+
+
+# ----------------------------------------------------------------------------
+# likelihoods (R/lik.R:188-498)
+# ----------------------------------------------------------------------------
+
+def add_offset(f, offset):
+    """add_offset (R/misc.R:6-15)."""
+    return f if offset is None else f + offset
+
+
+def get_response(lik, f):
+    """get_response.lik_* (R/lik.R:460-498)."""
+    if lik.kind == "gaussian":
+        return f
+    if lik.kind in ("bernoulli", "binomial", "betabinom"):
+        if lik.link == "probit":
+            return sps.ndtr(f)
+        if lik.link == "logit":
+            return 1 / (1 + np.exp(-f))
+        raise ValueError(lik.link)
+    if lik.kind == "poisson":
+        return np.exp(f)
+    raise ValueError(lik.kind)
+
+
+def _xlogy(x, y):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = x * np.log(y)
+    return np.where(x == 0, 0.0, out)
+
+
+def get_loglik(lik, f, y, trials=None, offset=None, sum_=True):
+    """get_loglik.lik_* (R/lik.R:301-366). dbinom/dpois/dnorm by closed form (R nmath agrees
+    to rounding away from the extreme tails)."""
+    f = add_offset(np.asarray(f, dtype=np.float64), offset)
+    y = np.asarray(y, dtype=np.float64)
+    if f.ndim == 2:
+        y = y[:, None]
+        if trials is not None:
+            trials = np.asarray(trials, dtype=np.float64)[:, None]
+    if lik.kind == "gaussian":
+        s = lik.sigma
+        ll = -math.log(s) - 0.5 * math.log(2 * math.pi) - 0.5 * ((y - f) / s) ** 2
+    elif lik.kind in ("bernoulli", "binomial"):
+        N = np.ones_like(y) if lik.kind == "bernoulli" else np.asarray(trials, dtype=np.float64)
+        mu = get_response(lik, f)
+        lch = sps.gammaln(N + 1) - sps.gammaln(y + 1) - sps.gammaln(N - y + 1)
+        ll = lch + _xlogy(y, mu) + _xlogy(N - y, 1 - mu)
+    elif lik.kind == "poisson":
+        mu = get_response(lik, f)
+        ll = _xlogy(y, mu) - mu - sps.gammaln(y + 1)
+    elif lik.kind == "betabinom":
+        N = np.asarray(trials, dtype=np.float64)
+        mu = get_response(lik, f)
+        a = mu / lik.phi
+        b = (1 - mu) / lik.phi
+        g = sps.gammaln
+        ll = (g(N + 1) - g(y + 1) - g(N - y + 1) + g(y + a) + g(N - y + b) - g(N + a + b)
+              + g(a + b) - g(a) - g(b))
+    else:
+        raise ValueError(lik.kind)
+    ll = np.broadcast_to(ll, f.shape).astype(np.float64)
+    return float(ll.sum()) if sum_ else ll
+
+
+def get_loglik_d(lik, f, y, trials=None, offset=None):
+    """get_loglik_d.lik_* (R/lik.R:372-443)."""
+    f = add_offset(np.asarray(f, dtype=np.float64), offset)
+    y = np.asarray(y, dtype=np.float64)
+    mu = get_response(lik, f)
+    if lik.kind in ("bernoulli", "binomial"):
+        N = np.ones_like(y) if lik.kind == "bernoulli" else np.asarray(trials, dtype=np.float64)
+        dmu = np.exp(-0.5 * f * f) / math.sqrt(2 * math.pi) if lik.link == "probit" else mu * (1 - mu)
+        return dmu * (y / mu - (N - y) / (1 - mu))
+    if lik.kind == "poisson":
+        return (y / mu - 1) * mu
+    if lik.kind == "betabinom":
+        N = np.asarray(trials, dtype=np.float64)
+        phi = lik.phi
+        a = mu / phi
+        b = (1 - mu) / phi
+        dmu = np.exp(-0.5 * f * f) / math.sqrt(2 * math.pi) if lik.link == "probit" else mu * (1 - mu)
+        dg = sps.digamma
+        return (dmu / phi) * (dg(y + a) - dg(N - y + b)) + (dmu / phi) * (-dg(a) + dg(b))
+    raise ValueError(lik.kind)
+
+
+def get_loglik_d2(lik, f, y, trials=None, offset=None, eps=1e-6):
+    """get_loglik_d2.lik (R/lik.R:449-454): forward finite difference of the gradient."""
+    g = get_loglik_d(lik, f, y, trials, offset)
+    ge = get_loglik_d(lik, f + eps, y, trials, offset)
+    return g, (ge - g) / eps
+
+
+def get_pseudodata_la(lik, f, y, trials=None, offset=None, min_abs_curvature=1e-12):
+    """get_pseudodata_la.lik_gaussian / .lik (R/lik.R:188-201)."""
+    n = len(y)
+    if lik.kind == "gaussian":
+        return np.asarray(y, dtype=np.float64).copy(), lik.sigma ** 2 * np.ones(n)
+    f = np.asarray(f, dtype=np.float64).ravel()
+    g, g2 = get_loglik_d2(lik, f, y, trials, offset)
+    g2 = np.sign(g2) * np.maximum(np.abs(g2), min_abs_curvature)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return f - g / g2, -1 / g2
+
+
+# ----------------------------------------------------------------------------
+# Gauss-Hermite quadrature (R/quadrature.R:1-44), logsumexp (R/gp_loo.R:136-144)
+# ----------------------------------------------------------------------------
+
+def hermite_polynomials(n):
+    """hermite_polynomials (R/quadrature.R:1-16): probabilists' He_k coefficients, row k."""
+    c = np.zeros((n + 1, n + 1))
+    c[0, 0] = 1
+    if n == 0:
+        return c
+    c[1, 1] = 1
+    for i in range(2, n + 1):
+        c[i, :] = np.concatenate([[0.0], c[i - 1, :n]]) - (i - 1) * c[i - 2, :]
+    return c
+
+
+def gauss_hermite_points(p):
+    """gauss_hermite_points (R/quadrature.R:28-34): nodes = real roots of He_p (polyroot),
+    weights = p! / (p^2 He_{p-1}(x)^2); weights sum to one (standard normal)."""
+    c = hermite_polynomials(p)
+    x = np.sort(np.real(np.roots(c[p, ::-1])))
+    # polish the roots with Newton steps on He_p (polyroot is accurate to rounding)
+    for _ in range(3):
+        v = np.polyval(c[p, ::-1], x)
+        dv = np.polyval(np.polyder(c[p, ::-1]), x)
+        x = x - v / dv
+    w = math.factorial(p) / (p * p * np.polyval(c[p - 1, ::-1], x) ** 2)
+    return x, w
+
+
+def gauss_hermite_points_scaled(mean, scale, order=7):
+    """gauss_hermite_points_scaled (R/quadrature.R:37-44): n-by-order grid mean + scale*x."""
+    x, w = gauss_hermite_points(order)
+    mean = np.asarray(mean, dtype=np.float64).ravel()
+    scale = np.asarray(scale, dtype=np.float64).ravel()
+    return x[None, :] * scale[:, None] + mean[:, None], w
+
+
+def logsumexp_rows(L, w=None):
+    """logsumexp applied per row (R/gp_loo.R:136-144)."""
+    c = L.max(axis=1)
+    if w is None:
+        w = np.ones(L.shape[1])
+    with np.errstate(invalid="ignore"):
+        return c + np.log((w[None, :] * np.exp(L - c[:, None])).sum(axis=1))
+
+
+# ----------------------------------------------------------------------------
+# Laplace, full method (R/laplace.R:13-39, 274-297)
+# ----------------------------------------------------------------------------
+
+def laplace_iter_full(lik, K, y, fhat_old, trials=None, offset=None):
+    """laplace_iter.method_full, log-concave branch (R/laplace.R:13-39)."""
+    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset)
+    n = len(z)
+    if not np.all(V > 0):
+        raise NotImplementedError("non-log-concave branch (R/laplace.R:40-117)")
+    sv = np.sqrt(1 / V)
+    B = np.eye(n) + sv[:, None] * (K * sv[None, :])
+    Lb = sla.cholesky(B, lower=False).T
+    C_chol = np.sqrt(V)[:, None] * Lb
+    alpha = sla.solve_triangular(C_chol.T, sla.solve_triangular(C_chol, z, lower=True), lower=False)
+    fhat_new = K @ alpha
+    C_logdet = 2 * np.log(np.diag(C_chol)).sum()
+    V_logdet = np.log(V).sum()
+    f_invK_f = fhat_new @ alpha
+    log_lik = get_loglik(lik, fhat_new, y, trials, offset)
+    lml = log_lik - 0.5 * f_invK_f - 0.5 * (C_logdet - V_logdet)
+    return dict(fmean=fhat_new, z=z, V=V, C_chol=C_chol, alpha=alpha, log_evidence=float(lml))
+
+
+def laplace_full(lik, K, y, maxiter=100, tol=1e-4, trials=None, offset=None):
+    """laplace.method_full (R/laplace.R:274-297): Newton iteration from f = 0."""
+    n = len(y)
+    fhat = np.zeros(n)
+    if lik.kind == "gaussian":
+        maxiter = 1
+    it = 0
+    for it in range(1, maxiter + 1):
+        fit = laplace_iter_full(lik, K, y, fhat, trials, offset)
+        diff = np.max(np.abs(fhat - fit["fmean"]))
+        fhat = fit["fmean"]
+        if diff < tol:
+            break
+    if maxiter > 1 and it == maxiter:
+        warnings.warn("Maximum number of iterations in Laplace reached, max delta f = %g" % diff)
+    fit["iters"] = it
+    return fit
+
+
+# ----------------------------------------------------------------------------
+# EP, full method (R/lik.R:207-270, R/ep.R:16-49, 286-330)
+# ----------------------------------------------------------------------------
+
+def get_tilted_moments(lik, post_mean, post_prec, z_old, P_old, y, quad_order, trials=None, offset=None):
+    """get_tilted_moments.lik (R/lik.R:237-270)."""
+    cavity_prec = post_prec - P_old
+    cavity_mean = 1 / cavity_prec * (post_mean * post_prec - z_old * P_old)
+    with np.errstate(invalid="ignore"):
+        fgrid, w = gauss_hermite_points_scaled(cavity_mean, np.sqrt(1 / cavity_prec), quad_order)
+        loglik = get_loglik(lik, fgrid, y, trials, offset, sum_=False)
+        lik_ = np.exp(loglik)
+    quad_ok = True
+    if np.any(np.isnan(lik_)):
+        lik_[np.isnan(lik_)] = 0
+        loglik[np.isnan(loglik)] = -np.inf
+        quad_ok = False
+    log_C = logsumexp_rows(loglik, w)
+    C = np.exp(log_C)
+    mean_t = (1 / C) * ((fgrid * lik_) @ w)
+    s2_t = (1 / C) * (((fgrid - mean_t[:, None]) ** 2 * lik_) @ w)
+    return dict(mean_tilted=mean_t, var_tilted=s2_t, log_C=log_C, mean_cavity=cavity_mean,
+                var_cavity=1 / cavity_prec, quad_ok=quad_ok)
+
+
+def get_pseudodata_ep(lik, post_mean, post_prec, z_old, P_old, y, quad_order=11, damping=0.5,
+                      trials=None, offset=None):
+    """get_pseudodata_ep.lik (R/lik.R:207-232): site update with damping."""
+    tm = get_tilted_moments(lik, post_mean, post_prec, z_old, P_old, y, quad_order, trials, offset)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        P_new = 1 / tm["var_tilted"] - 1 / tm["var_cavity"]
+        nu_new = tm["mean_tilted"] / tm["var_tilted"] - tm["mean_cavity"] / tm["var_cavity"]
+        nu_old = z_old * P_old
+        nu_new = damping * nu_new + (1 - damping) * nu_old
+        P_new = damping * P_new + (1 - damping) * P_old
+        return dict(z=(1 / P_new) * nu_new, var=1 / P_new, log_C=tm["log_C"],
+                    mean_cavity=tm["mean_cavity"], var_cavity=tm["var_cavity"], quad_ok=tm["quad_ok"])
+
+
+def ep_iter_full(lik, K, y, fmean_old, fvar_old, z_old, P_old, quad_order, damping,
+                 trials=None, offset=None):
+    """ep_iter.method_full, log-concave branch (R/ep.R:16-49, 140-145)."""
+    po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
+                           trials, offset)
+    z, V = po["z"], po["var"]
+    if np.any(np.isnan(V) | np.isnan(z)):
+        return dict(fmean=fmean_old, log_evidence=-np.inf, nan=True)
+    if not np.all(V > 0):
+        raise NotImplementedError("non-log-concave branch (R/ep.R:50-138)")
+    n = len(z)
+    sv = np.sqrt(1 / V)
+    B = np.eye(n) + sv[:, None] * (K * sv[None, :])
+    C_chol = np.sqrt(V)[:, None] * sla.cholesky(B, lower=False).T
+    alpha = sla.solve_triangular(C_chol.T, sla.solve_triangular(C_chol, z, lower=True), lower=False)
+    fmean_new = K @ alpha
+    CinvK = sla.solve_triangular(C_chol.T, sla.solve_triangular(C_chol, K, lower=True), lower=False)
+    fvar_new = V * np.diag(CinvK)
+    C_logdet = 2 * np.log(np.diag(C_chol)).sum()
+    z_invC_z = z @ alpha
+    vc, mc = po["var_cavity"], po["mean_cavity"]
+    lml = (-0.5 * C_logdet - 0.5 * z_invC_z + po["log_C"].sum()
+           + 0.5 * np.log(vc + V).sum() + 0.5 * ((mc - z) ** 2 / (vc + V)).sum())
+    return dict(fmean=fmean_new, fvar=fvar_new, cavity_mean=mc, cavity_var=vc, z=z, P=1 / V,
+                V=V, C_chol=C_chol, alpha=alpha, log_evidence=float(lml), quad_ok=po["quad_ok"])
+
+
+def ep_full(lik, K, y, maxiter=300, tol=1e-4, damping=0.9, damping_min=0.1, quad_order=11,
+            trials=None, offset=None):
+    """ep.method_full (R/ep.R:286-330): parallel EP with adaptive damping."""
+    n = len(y)
+    P_old = np.zeros(n)
+    z_old = np.zeros(n)
+    fmean_old = np.zeros(n)
+    fvar_old = np.diag(K).copy()
+    diff_old = np.inf
+    damp = damping
+    it = 0
+    diff_new = np.inf
+    fit = None
+    for it in range(1, maxiter + 1):
+        fit = ep_iter_full(lik, K, y, fmean_old, fvar_old, z_old, P_old, quad_order, damp, trials, offset)
+        if fit.get("nan"):
+            return fit
+        diff_new = np.max(np.abs(fmean_old - fit["fmean"]))
+        if diff_new > diff_old:
+            damp = damp * damping
+            continue
+        damp = max(damp, damping_min)
+        fmean_old, fvar_old, z_old, P_old = fit["fmean"], fit["fvar"], fit["z"], fit["P"]
+        diff_old = diff_new
+        if diff_new < tol:
+            break
+    if maxiter > 1 and it == maxiter:
+        fit["log_evidence"] = -np.inf
+        warnings.warn("Maximum number of iterations in EP reached, max delta f = %g" % diff_new)
+    if fit.get("quad_ok") is False:
+        fit["log_evidence"] = -np.inf
+    fit["iters"] = it
+    return fit
+
+
+# ----------------------------------------------------------------------------
+# inversion lemma (R/linear_algebra.R:3-143) and FITC (R/gp_fit.R:101-123,163-188,
+# R/laplace.R:122-152,299-325, R/ep.R:148-185,333-374)
+# ----------------------------------------------------------------------------
+
+def inv_lemma_get(K, U, D, logdet=True):
+    """inv_lemma_get (R/linear_algebra.R:3-43) with V = t(U)."""
+    D = np.asarray(D, dtype=np.float64).ravel()
+    inv_D_U = U / D[:, None]
+    VDU = U.T @ inv_D_U
+    VDU = 0.5 * (VDU + VDU.T)
+    L = sla.cholesky(K + VDU, lower=False).T
+    ld = None
+    if logdet:
+        ld = np.log(D).sum() - 2 * np.log(np.diag(sla.cholesky(K, lower=False))).sum() \
+            + 2 * np.log(np.diag(L)).sum()
+    return dict(chol=L, D=D, inv_D_U=inv_D_U, logdet=ld)
+
+
+def _chol_solve_lower(L, b):
+    return sla.solve_triangular(L.T, sla.solve_triangular(L, b, lower=True), lower=False)
+
+
+def inv_lemma_solve(obj, rhs, lhs=None, rhs_diag=False, lhs_diag=False, diag_only=False):
+    """inv_lemma_solve (R/linear_algebra.R:45-126), the cases the hot path uses."""
+    D, iDU, L = obj["D"], obj["inv_D_U"], obj["chol"]
+    if lhs is None:
+        if rhs_diag:
+            aux_right = iDU.T * rhs[None, :]
+            return np.diag(rhs / D) - iDU @ _chol_solve_lower(L, aux_right)
+        aux_right = iDU.T @ rhs
+        aux_left = rhs / D if rhs.ndim == 1 else rhs / D[:, None]
+        return aux_left - iDU @ _chol_solve_lower(L, aux_right)
+    if rhs_diag:
+        aux_right = iDU.T * rhs[None, :]
+        if lhs_diag:
+            if diag_only:
+                return lhs / D * rhs - ((lhs[:, None] * iDU).T * _chol_solve_lower(L, aux_right)).sum(0)
+            return np.diag(lhs / D * rhs) - (lhs[:, None] * iDU) @ _chol_solve_lower(L, aux_right)
+        return lhs * (rhs / D)[None, :] - (lhs @ iDU) @ _chol_solve_lower(L, aux_right)
+    aux_right = iDU.T @ rhs
+    if lhs_diag:
+        return (lhs / D)[:, None] * rhs - (lhs[:, None] * iDU) @ _chol_solve_lower(L, aux_right)
+    return lhs @ (rhs / D[:, None]) - (lhs @ iDU) @ _chol_solve_lower(L, aux_right)
+
+
+def fitc_prepare(cfs, x, z, jitter):
+    """The FITC set-up of fit_laplace.method_fitc / fit_ep.method_fitc (R/gp_fit.R:101-111,
+    163-173)."""
+    M = z.shape[0]
+    Kz = eval_cf(cfs, z, z) + jitter * np.eye(M)
+    Kxz = eval_cf(cfs, x, z)
+    Kz_chol = sla.cholesky(Kz, lower=False).T
+    K_diag = eval_cf(cfs, x, x, diag_only=True) + jitter
+    D = K_diag - (sla.solve_triangular(Kz_chol, Kxz.T, lower=True) ** 2).sum(0)
+    return Kz, Kxz, Kz_chol, K_diag, D
+
+
+def laplace_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fhat_old, trials=None, offset=None):
+    """laplace_iter.method_fitc, log-concave branch (R/laplace.R:122-152)."""
+    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset)
+    if not np.all(V > 0):
+        raise NotImplementedError("non-log-concave branch (R/laplace.R:153-232)")
+    S = D + V
+    Ci = inv_lemma_get(Kz, Kxz, S)
+    alpha = inv_lemma_solve(Ci, z)
+    fhat = Kxz @ _chol_solve_lower(Kz_chol, Kxz.T @ alpha) + D * alpha
+    invC_V_logdet = np.log(V).sum() - Ci["logdet"]
+    f_invK_f = fhat @ alpha
+    log_lik = get_loglik(lik, fhat, y, trials, offset)
+    lml = log_lik - 0.5 * f_invK_f + 0.5 * invC_V_logdet
+    return dict(fmean=fhat, z=z, V=V, Kz=Kz, Kxz=Kxz, Kz_chol=Kz_chol, C_inv=Ci, diag=D, alpha=alpha,
+                log_evidence=float(lml), log_post_unnorm=float(log_lik - 0.5 * f_invK_f))
+
+
+def laplace_fitc(lik, Kz, Kz_chol, Kxz, D, y, maxiter=100, tol=1e-4, trials=None, offset=None):
+    """laplace.method_fitc (R/laplace.R:299-325): stops on |delta log_post_unnorm| < tol."""
+    n = len(y)
+    fhat = np.zeros(n)
+    if lik.kind == "gaussian":
+        maxiter = 1
+    old = -np.inf
+    it = 0
+    for it in range(1, maxiter + 1):
+        fit = laplace_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fhat, trials, offset)
+        fhat = fit["fmean"]
+        d = fit["log_post_unnorm"] - old
+        old = fit["log_post_unnorm"]
+        if abs(d) < tol:
+            break
+    if maxiter > 1 and it == maxiter:
+        warnings.warn("Maximum number of iterations in Laplace reached")
+    fit["iters"] = it
+    return fit
+
+
+def ep_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fmean_old, fvar_old, z_old, P_old, quad_order, damping,
+                 trials=None, offset=None):
+    """ep_iter.method_fitc, log-concave branch (R/ep.R:148-185, 274-279)."""
+    po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
+                           trials, offset)
+    z, V = po["z"], po["var"]
+    if np.any(np.isnan(V) | np.isnan(z)):
+        return dict(fmean=fmean_old, log_evidence=-np.inf, nan=True)
+    if not np.all(V > 0):
+        raise NotImplementedError("non-log-concave branch (R/ep.R:186-272)")
+    S = D + V
+    Ci = inv_lemma_get(Kz, Kxz, S)
+    alpha = inv_lemma_solve(Ci, z)
+    inv_Kz_Kzx = _chol_solve_lower(Kz_chol, Kxz.T)
+    aux = inv_lemma_solve(Ci, V, inv_Kz_Kzx, rhs_diag=True)
+    diag1 = (Kxz.T * aux).sum(0)
+    diag2 = inv_lemma_solve(Ci, V, D, rhs_diag=True, lhs_diag=True, diag_only=True)
+    fvar = diag1 + diag2
+    fmean = Kxz @ _chol_solve_lower(Kz_chol, Kxz.T @ alpha) + D * alpha
+    vc, mc = po["var_cavity"], po["mean_cavity"]
+    lml = (-0.5 * Ci["logdet"] - 0.5 * z @ alpha + po["log_C"].sum()
+           + 0.5 * np.log(vc + V).sum() + 0.5 * ((mc - z) ** 2 / (vc + V)).sum())
+    return dict(fmean=fmean, fvar=fvar, cavity_mean=mc, cavity_var=vc, z=z, P=1 / V, V=V, Kz=Kz,
+                Kxz=Kxz, Kz_chol=Kz_chol, C_inv=Ci, diag=D, alpha=alpha, log_evidence=float(lml),
+                quad_ok=po["quad_ok"])
+
+
+def ep_fitc(lik, Kz, Kz_chol, Kxz, K_diag, D, y, damping=0.9, damping_min=0.1, maxiter=100, tol=1e-3,
+            quad_order=11, trials=None, offset=None):
+    """ep.method_fitc (R/ep.R:333-374)."""
+    n = len(y)
+    P_old = np.zeros(n)
+    z_old = np.zeros(n)
+    fmean_old = np.zeros(n)
+    fvar_old = K_diag.copy()
+    diff_old = np.inf
+    damp = damping
+    it = 0
+    diff_new = np.inf
+    fit = None
+    for it in range(1, maxiter + 1):
+        fit = ep_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fmean_old, fvar_old, z_old, P_old, quad_order,
+                           damp, trials, offset)
+        if fit.get("nan"):
+            return fit
+        diff_new = np.max(np.abs(fmean_old - fit["fmean"]))
+        if diff_new > diff_old:
+            damp = damp * damping
+            continue
+        damp = max(damp, damping_min)
+        fmean_old, fvar_old, z_old, P_old = fit["fmean"], fit["fvar"], fit["z"], fit["P"]
+        diff_old = diff_new
+        if diff_new < tol:
+            break
+    if maxiter > 1 and it == maxiter:
+        fit["log_evidence"] = -np.inf
+    if fit.get("quad_ok") is False:
+        fit["log_evidence"] = -np.inf
+    fit["iters"] = it
+    return fit
+
+
+# ----------------------------------------------------------------------------
+# gp_fit / gp_energy / gp_pred / gp_loo (R/gp_fit.R:54-188, R/gp.R:138-147,
+# R/gp_pred.R:88-296, R/gp_loo.R:73-133)
+# ----------------------------------------------------------------------------
+
+def gp_fit(gp, x, y, trials=None, offset=None, jitter=None):
+    """gp_fit (R/gp_fit.R:54-60) -> fit_laplace/fit_ep.method_full/fitc."""
+    x = as_matrix(x)
+    y = np.asarray(y, dtype=np.float64)
+    jitter = 1e-6 if jitter is None else jitter
+    learn_scales(gp.cfs, x)
+    n = len(y)
+    ap, me = gp.approx, gp.method
+    if ap.kind == "ep" and gp.lik.kind == "gaussian":
+        raise ValueError("approx_ep disabled for lik_gaussian")
+    if me.kind == "full":
+        K = eval_cf(gp.cfs, x, x) + jitter * np.eye(n)
+        if ap.kind == "laplace":
+            fit = laplace_full(gp.lik, K, y, ap.maxiter, ap.tol, trials, offset)
+        else:
+            fit = ep_full(gp.lik, K, y, maxiter=ap.maxiter, tol=1e-4, damping=ap.damping,
+                          damping_min=0.1, quad_order=ap.quad_order, trials=trials, offset=offset)
+    elif me.kind == "fitc":
+        z = as_matrix(me.inducing)
+        try:
+            Kz, Kxz, Kz_chol, K_diag, D = fitc_prepare(gp.cfs, x, z, jitter)
+            if ap.kind == "laplace":
+                fit = laplace_fitc(gp.lik, Kz, Kz_chol, Kxz, D, y, ap.maxiter, ap.tol, trials, offset)
+            else:
+                fit = ep_fitc(gp.lik, Kz, Kz_chol, Kxz, K_diag, D, y, damping=ap.damping, damping_min=0.1,
+                              maxiter=ap.maxiter, quad_order=ap.quad_order, trials=trials, offset=offset)
+        except np.linalg.LinAlgError:
+            fit = dict(log_evidence=-np.inf)
+    else:
+        raise ValueError(me.kind)
+    gp.x = x
+    gp.fit = fit
+    gp.fit_jitter = jitter
+    gp.fitted = True
+    return gp
+
+
+def gp_energy(gp, include_prior=True):
+    """gp_energy (R/gp.R:138-147)."""
+    if getattr(gp, "fit", None) is None:
+        raise RuntimeError("The GP must be fitted. Call gp_fit first.")
+    if not gp.fitted:
+        raise RuntimeError("The GP object seems to contain a posterior fit, but is not refitted")
+    e = -gp.fit["log_evidence"]
+    if include_prior:
+        e = e - lpdf_prior(gp)
+    return e
+
+
+def gp_pred_post_full(gp, xt, var=False, cfind=None):
+    """gp_pred_post.method_full (R/gp_pred.R:202-232), Cholesky branch."""
+    Kt = eval_cf(gp.cfs, xt, gp.x, cfind)
+    mean = Kt @ gp.fit["alpha"]
+    if not var:
+        return dict(mean=mean)
+    Ktt_diag = eval_cf(gp.cfs, xt, xt, cfind, diag_only=True)
+    aux = sla.solve_triangular(gp.fit["C_chol"], Kt.T, lower=True)
+    return dict(mean=mean, var=Ktt_diag - (aux * aux).sum(0))
+
+
+def gp_pred_post_fitc(gp, xt, var=False, train=False, cfind=None):
+    """gp_pred_post.method_fitc (R/gp_pred.R:234-296), var (not cov) branch."""
+    z = as_matrix(gp.method.inducing)
+    alpha = gp.fit["alpha"]
+    Ktz = eval_cf(gp.cfs, xt, z, cfind)
+    Kxz = gp.fit["Kxz"]
+    Kz_chol = gp.fit["Kz_chol"]
+    Dt = None
+    if var or train:
+        Dt = eval_cf(gp.cfs, xt, xt, cfind, diag_only=True)
+        Dt = Dt - (sla.solve_triangular(Kz_chol, Ktz.T, lower=True) ** 2).sum(0)
+    A1 = sla.solve_triangular(Kz_chol, Kxz.T, lower=True)
+    A2 = sla.solve_triangular(Kz_chol, Ktz.T, lower=True)
+    mean = A2.T @ (A1 @ alpha)
+    if train:
+        mean = mean + Dt * alpha
+    if not var:
+        return dict(mean=mean)
+    Ci = gp.fit["C_inv"]
+    Kz_inv_Ktz = _chol_solve_lower(Kz_chol, Ktz.T)
+    prior_var = (Ktz * Kz_inv_Ktz.T).sum(1) + Dt
+    if train:
+        aux = inv_lemma_solve(Ci, A1.T, A1) @ A2 + inv_lemma_solve(Ci, Dt, A1, rhs_diag=True)
+        d1 = (A2 * aux).sum(0)
+        d2 = (inv_lemma_solve(Ci, A1.T, Dt, lhs_diag=True) * A2.T).sum(1)
+        d3 = inv_lemma_solve(Ci, Dt, Dt, rhs_diag=True, lhs_diag=True, diag_only=True)
+        red = d1 + d2 + d3
+    else:
+        aux = inv_lemma_solve(Ci, A1.T, A1) @ A2
+        red = (A2 * aux).sum(0)
+    return dict(mean=mean, var=prior_var - red)
+
+
+def gp_pred(gp, xnew, var=False, quantiles=None, transform=False, cfind=None, quad_order=15,
+            offset=None):
+    """gp_pred (R/gp_pred.R:88-122) for fitted models; prior prediction (R/gp_pred.R:142-156)
+    when not fitted (full method)."""
+    xnew = as_matrix(xnew)
+    if quantiles is not None or transform:
+        var = True
+    if getattr(gp, "fit", None) is None:
+        mean = np.zeros(xnew.shape[0])
+        pred = dict(mean=mean)
+        if var:
+            pred["var"] = eval_cf(gp.cfs, xnew, xnew, cfind, diag_only=True)
+    else:
+        if not gp.fitted:
+            raise RuntimeError("The GP object seems to contain a posterior fit, but is not refitted")
+        if gp.method.kind == "full":
+            pred = gp_pred_post_full(gp, xnew, var, cfind)
+        else:
+            pred = gp_pred_post_fitc(gp, xnew, var, False, cfind)
+    pred["mean"] = add_offset(pred["mean"], offset)
+    if quantiles is not None:
+        from scipy.stats import norm
+        q = np.stack([norm.ppf(qq, loc=pred["mean"], scale=np.sqrt(pred["var"])) for qq in quantiles], 1)
+        if transform:
+            q = get_response(gp.lik, q)
+        pred["quantiles"] = q
+    if transform:
+        fg, w = gauss_hermite_points_scaled(pred["mean"], np.sqrt(pred["var"]), quad_order)
+        ft = get_response(gp.lik, fg)
+        mt = ft @ w
+        pred["mean"] = mt
+        pred["var"] = ((ft - mt[:, None]) ** 2) @ w
+    return pred
+
+
+def loo_posteriors(gp, x):
+    """loo_posteriors.approx_laplace / .approx_ep (R/gp_loo.R:119-133)."""
+    fit = gp.fit
+    if gp.approx.kind == "ep":
+        return fit["cavity_mean"], fit["cavity_var"]
+    fhat = np.asarray(fit["fmean"]).ravel()
+    z, V = fit["z"], fit["V"]
+    grad = (z - fhat) / V
+    if gp.method.kind == "full":
+        pv = gp_pred_post_full(gp, as_matrix(x), var=True)["var"]
+    else:
+        pv = gp_pred_post_fitc(gp, as_matrix(x), var=True, train=True)["var"]
+    loo_var = 1 / (1 / pv - 1 / V)
+    return fhat - loo_var * grad, loo_var
+
+
+def gp_loo(gp, x, y, quad_order=11, trials=None, offset=None):
+    """gp_loo (R/gp_loo.R:73-109), quadrature branch."""
+    if getattr(gp, "fit", None) is None or not gp.fitted:
+        raise RuntimeError("The provided GP model is not fitted.")
+    m, v = loo_posteriors(gp, x)
+    fg, w = gauss_hermite_points_scaled(m, np.sqrt(v), quad_order)
+    ll = get_loglik(gp.lik, fg, y, trials, offset, sum_=False)
+    loos = logsumexp_rows(ll, w)
+    n = len(y)
+    return dict(loo=float(loos.sum()), sd=float(n * (np.std(loos, ddof=1) / math.sqrt(n))), loos=loos)
+
+
+# ----------------------------------------------------------------------------
+# Constructors (R/cf.R:88-195, R/lik.R:44-90, R/method.R:105-125, R/approx.R:60-75,
+# R/priors.R:56-91, R/gp.R:52-71) -- plain namespaces for the oracle's own tests
+# ----------------------------------------------------------------------------
+
+def prior(kind, **kw):
+    return SimpleNamespace(kind=kind, **kw)
+
+
+def cf(kind, vars=None, normalize=False, priors=None, **params):
+    defaults = dict(const=dict(magn=1.0), lin=dict(magn=1.0), sexp=dict(lscale=0.3, magn=1.0),
+                    matern32=dict(lscale=0.3, magn=1.0), matern52=dict(lscale=0.3, magn=1.0),
+                    nn=dict(sigma0=1.0, sigma=3.0, magn=1.0), periodic=dict(period=1.0))[kind]
+    defaults.update(params)
+    o = SimpleNamespace(kind=kind, vars=vars, normalize=normalize, means=None, scales=None,
+                        priors=priors or {}, **defaults)
+    if kind == "nn" and "normalize" not in params and normalize is False:
+        pass
+    if kind == "periodic" and not hasattr(o, "base"):
+        o.base = cf("sexp")
+    return o
+
+
+def cf_periodic(period=1.0, base=None, vars=None, priors=None):
+    b = base if base is not None else cf("sexp")
+    b.normalize = False
+    b.vars = None
+    return SimpleNamespace(kind="periodic", vars=vars, normalize=False, means=None, scales=None,
+                           priors=priors or {}, period=period, base=b)
+
+
+def cf_prod(*cfs):
+    flat = []
+    for c in cfs:
+        flat += c.cfs if c.kind == "prod" else [c]
+    return SimpleNamespace(kind="prod", cfs=flat, vars=None, normalize=False, priors={})
+
+
+def lik(kind, link=None, priors=None, **params):
+    defaults = dict(gaussian=dict(sigma=0.5), bernoulli={}, binomial={}, betabinom=dict(phi=1.0),
+                    poisson={})[kind]
+    defaults.update(params)
+    dl = dict(gaussian="identity", bernoulli="logit", binomial="logit", betabinom="logit",
+              poisson="log")[kind]
+    return SimpleNamespace(kind=kind, link=link or dl, priors=priors or {}, **defaults)
+
+
+def method_full():
+    return SimpleNamespace(kind="full")
+
+
+def method_fitc(inducing):
+    inducing = as_matrix(inducing)
+    return SimpleNamespace(kind="fitc", inducing=inducing, num_inducing=inducing.shape[0])
+
+
+def approx_laplace(maxiter=30, tol=1e-4):
+    return SimpleNamespace(kind="laplace", maxiter=maxiter, tol=tol)
+
+
+def approx_ep(damping=0.9, quad_order=11, maxiter=100):
+    return SimpleNamespace(kind="ep", damping=damping, quad_order=quad_order, maxiter=maxiter)
+
+
+def gp_init(cfs, lik_, method=None, approx=None):
+    if not isinstance(cfs, (list, tuple)):
+        cfs = [cfs]
+    approx = approx or approx_laplace()
+    if approx.kind == "ep" and lik_.kind == "gaussian":
+        raise ValueError("approx_ep disabled for lik_gaussian")
+    return SimpleNamespace(cfs=list(cfs), lik=lik_, method=method or method_full(), approx=approx,
+                           fitted=False, fit=None, x=None)

@@ -1,0 +1,155 @@
+"""Pins the oracle (the CPU restatement of gplite) to the reference's own
+known-answer tests and to the committed golden fixtures. CPU only."""
+import copy
+import itertools
+import os
+import warnings
+
+import numpy as np
+import pytest
+from scipy import linalg as sla
+
+from oracle import gplite_ref as R
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def zoo():
+    return [R.cf("const"), R.cf("lin"), R.cf("sexp"), R.cf("matern32"), R.cf("matern52"),
+            R.cf("nn", normalize=True), R.cf_periodic()]
+
+
+def models():
+    z = zoo()
+    out = [[c] for c in z]
+    out += [[copy.deepcopy(a), copy.deepcopy(b)] for a, b in itertools.combinations(z, 2)]
+    out += [[R.cf_prod(copy.deepcopy(a), copy.deepcopy(b), copy.deepcopy(c))]
+            for a, b, c in itertools.combinations(z, 3)]
+    return out
+
+
+def data():
+    rng = np.random.default_rng(1234)
+    n, nt = 20, 30
+    x = rng.standard_normal(n)
+    xt = rng.standard_normal(nt)
+    y = x ** 2 + 0.2 * rng.standard_normal(n)
+    return x, xt, y
+
+
+def test_lml_closed_form():
+    """tests/testthat/test_basic.R:64-94 (rel 1e-3 there; exact algebra with the jitter here)."""
+    x, xt, y = data()
+    n = len(y)
+    rng = np.random.default_rng(2309)
+    for cfs in models():
+        gp = R.gp_init(cfs, R.lik("gaussian"))
+        _, p0 = R.get_param(gp)
+        for _ in range(3):
+            R.set_param(gp, p0 + 0.3 * rng.standard_normal(len(p0)))
+            gp = R.gp_fit(gp, x, y)
+            K = R.eval_cf(gp.cfs, x, x) + 1e-6 * np.eye(n)
+            Lc = np.linalg.cholesky(K + gp.lik.sigma ** 2 * np.eye(n))
+            aux = sla.solve_triangular(Lc, y, lower=True)
+            ref = -0.5 * aux @ aux - np.log(np.diag(Lc)).sum() - n / 2 * np.log(2 * np.pi)
+            assert abs(gp.fit["log_evidence"] - ref) <= 1e-9 * abs(ref)
+            # and within the reference's own tolerance of the jitter-free closed form
+            K0 = R.eval_cf(gp.cfs, x, x)
+            L0 = np.linalg.cholesky(K0 + gp.lik.sigma ** 2 * np.eye(n))
+            a0 = sla.solve_triangular(L0, y, lower=True)
+            ref0 = -0.5 * a0 @ a0 - np.log(np.diag(L0)).sum() - n / 2 * np.log(2 * np.pi)
+            assert abs(gp.fit["log_evidence"] - ref0) <= 1e-3 * abs(ref0)
+
+
+def test_pred_closed_form():
+    """tests/testthat/test_basic.R:99-132."""
+    x, xt, y = data()
+    n = len(y)
+    rng = np.random.default_rng(2209)
+    for cfs in models():
+        gp = R.gp_init(cfs, R.lik("gaussian"))
+        _, p0 = R.get_param(gp)
+        R.set_param(gp, p0 + 0.3 * rng.standard_normal(len(p0)))
+        gp = R.gp_fit(gp, x, y)
+        pred = R.gp_pred(gp, xt, var=True)
+        K = R.eval_cf(gp.cfs, x, x) + 1e-6 * np.eye(n)
+        Kt = R.eval_cf(gp.cfs, xt, x)
+        Ktt = R.eval_cf(gp.cfs, xt, xt)
+        Lc = np.linalg.cholesky(K + gp.lik.sigma ** 2 * np.eye(n))
+        alpha = sla.cho_solve((Lc, True), y)
+        aux = sla.solve_triangular(Lc, Kt.T, lower=True)
+        assert np.allclose(pred["mean"], Kt @ alpha, rtol=1e-9, atol=1e-12)
+        assert np.allclose(pred["var"], np.diag(Ktt - aux.T @ aux), rtol=1e-7, atol=1e-10)
+
+
+def test_normalization_invariance():
+    """tests/testthat/test_normalization.R:81-141."""
+    rng = np.random.default_rng(1234)
+    n, nt = 20, 30
+    x = 5 * (rng.standard_normal(n) - 1)
+    xn = (x - x.mean()) / x.std(ddof=1)
+    xt = 5 * (rng.standard_normal(nt) - 1)
+    xtn = (xt - x.mean()) / x.std(ddof=1)
+    y = 0.1 * x ** 2 + 0.2 * rng.standard_normal(n)
+    for kind in ["lin", "sexp", "matern32", "matern52", "nn"]:
+        g1 = R.gp_fit(R.gp_init([R.cf(kind, normalize=False)], R.lik("gaussian")), xn, y)
+        g2 = R.gp_fit(R.gp_init([R.cf(kind, normalize=True)], R.lik("gaussian")), x, y)
+        assert abs(g1.fit["log_evidence"] - g2.fit["log_evidence"]) <= 1e-10 * abs(g1.fit["log_evidence"])
+        p1 = R.gp_pred(g1, xtn, var=True)
+        p2 = R.gp_pred(g2, xt, var=True)
+        assert np.allclose(p1["mean"], p2["mean"], rtol=1e-9, atol=1e-12)
+        assert np.allclose(p1["var"], p2["var"], rtol=1e-9, atol=1e-12)
+
+
+def test_param_roundtrip():
+    """tests/testthat/test_param.R:73-85: get_param(set_param(gp, p)) == p."""
+    rng = np.random.default_rng(7)
+    for cfs in models():
+        gp = R.gp_init(cfs, R.lik("gaussian"))
+        names, p = R.get_param(gp)
+        q = p + rng.standard_normal(len(p))
+        R.set_param(gp, q)
+        names2, p2 = R.get_param(gp)
+        assert names == names2
+        assert np.allclose(p2, q, rtol=0, atol=1e-14)
+
+
+def test_gauss_hermite():
+    """R/quadrature.R: weights sum to one and integrate N(0,1) moments exactly."""
+    for q in (7, 11, 15):
+        xq, w = R.gauss_hermite_points(q)
+        assert abs(w.sum() - 1) < 1e-13
+        assert abs((w * xq ** 2).sum() - 1) < 1e-12
+        assert abs((w * xq ** 4).sum() - 3) < 1e-11
+        assert abs((w * xq).sum()) < 1e-13
+
+
+def test_golden_fixtures_reproduce():
+    """The oracle reproduces the committed golden fixtures bit for bit."""
+    g = np.load(os.path.join(GOLD, "c1_gauss_n200.npz"))
+    gp = R.gp_fit(R.gp_init([R.cf("sexp", lscale=0.3, magn=1.0)], R.lik("gaussian", sigma=0.1)),
+                  g["x"], g["y"])
+    assert gp.fit["log_evidence"] == float(g["lml"])
+    p = R.gp_pred(gp, g["xt"], var=True)
+    assert np.array_equal(p["mean"], g["mean"]) and np.array_equal(p["var"], g["var"])
+    gh = np.load(os.path.join(GOLD, "gh.npz"))
+    assert np.array_equal(R.gauss_hermite_points(11)[0], gh["x11"])
+
+
+def test_laplace_gaussian_is_exact_one_step():
+    """laplace.method_full forces maxiter = 1 for lik_gaussian (R/laplace.R:281-283)."""
+    x, _, y = data()
+    gp = R.gp_fit(R.gp_init([R.cf("sexp")], R.lik("gaussian")), x, y)
+    assert gp.fit["iters"] == 1
+
+
+def test_ep_and_laplace_agree_roughly():
+    """Laplace and EP evidences of a Bernoulli model are close (sanity of both restatements)."""
+    g = np.load(os.path.join(GOLD, "c3_bernoulli_n256.npz"))
+    assert abs(float(g["la_lml"]) - float(g["ep_lml"])) < 0.05 * abs(float(g["ep_lml"]))
+    assert int(g["ep_iters"]) > 1 and int(g["la_iters"]) > 1
+
+
+def test_gp_init_rejects_ep_gaussian():
+    with pytest.raises(ValueError):
+        R.gp_init([R.cf("sexp")], R.lik("gaussian"), approx=R.approx_ep())
