@@ -856,18 +856,14 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
     const int64_t n = m->n;
     const uint32_t gm = group_mask ? group_mask : 0xffffffffu;
     if (mt == 0) return GPGP_OK;
-    DBuf dxt, Ft, dmean, dvar;
+    DBuf dxt, Ft, dmean;
     copy_in(s, dxt, xt, (size_t)mt * m->d, on_device);
     Ft.alloc(s, (size_t)mt * std::max(1, m->dk.nfeat));
     prep_features(s, m->dk, m->prep, dxt.p, mt, mt, Ft.p, mt);
-    double *mout = mean, *vout = var;
+    double *mout = mean;
     if (!on_device) {
       dmean.alloc(s, mt);
       mout = dmean.p;
-      if (var) {
-        dvar.alloc(s, mt);
-        vout = dvar.p;
-      }
     }
     // mean = Kt alpha (R/gp_pred.R:209), fused: Kt is never stored
     {
@@ -896,7 +892,7 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       cov_diag(s, m->dk, gm, Ft.p, mt, Ft.p, mt, mt, kdiag.p);
       sub_from_kernel<<<g1(mt), 256, 0, s>>>(mt, kdiag.p, csum.p);
       GPGP_CHECK_LAUNCH();
-      GPGP_CUDA(cudaMemcpyAsync(vout, csum.p, mt * sizeof(double),
+      GPGP_CUDA(cudaMemcpyAsync(var, csum.p, mt * sizeof(double),
                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     }
     if (!on_device)

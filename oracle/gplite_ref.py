@@ -356,12 +356,15 @@ def _xlogy(x, y):
 def get_loglik(lik, f, y, trials=None, offset=None, sum_=True):
     """get_loglik.lik_* (R/lik.R:301-366). dbinom/dpois/dnorm by closed form (R nmath agrees
     to rounding away from the extreme tails)."""
-    f = add_offset(np.asarray(f, dtype=np.float64), offset)
+    f = np.asarray(f, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
-    if f.ndim == 2:
+    if f.ndim == 2:  # an n-by-q quadrature grid: per-observation quantities broadcast along rows
         y = y[:, None]
         if trials is not None:
             trials = np.asarray(trials, dtype=np.float64)[:, None]
+        if offset is not None:
+            offset = np.asarray(offset, dtype=np.float64)[:, None]
+    f = add_offset(f, offset)
     if lik.kind == "gaussian":
         s = lik.sigma
         ll = -math.log(s) - 0.5 * math.log(2 * math.pi) - 0.5 * ((y - f) / s) ** 2
