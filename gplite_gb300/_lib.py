@@ -95,6 +95,7 @@ SIGNATURES = {
     "gpgp_pred": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_pred_dev": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_loo": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "gpgp_mixed_selftest": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P]),
 }
 
 _lib = None

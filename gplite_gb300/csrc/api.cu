@@ -135,6 +135,9 @@ struct gpgp_model {
   DBuf fvar, cav_mean, cav_var;  // EP
   DBuf binv_diag;                // diag(B^-1), filled on demand
   bool have_binv_diag = false;
+  DBuf Linv;                     // W = L^-1, kept resident once computed (mixed precision)
+  bool have_Linv = false;
+  IBuf errflag;                  // bounded-wait timeouts of the tensor-core kernels
   bool has_trials = false, has_offset = false;
   double log_evidence = 0.0;
   int fitted = 0;
@@ -304,9 +307,17 @@ void make_B(cudaStream_t st, const double *K, int64_t n, const double *s, double
 // fnew = K alpha; returns 0 or the non-PD pivot
 // ---------------------------------------------------------------------------
 struct Work {
-  DBuf K, t1, t2, red, logdet_part, ll_part, tmpv;
+  DBuf K, t1, t2, u, rhs, red, logdet_part, ll_part, tmpv;
   IBuf status, flags;
 };
+
+// r = rhs - (u + s * Kalpha)
+__global__ void refine_residual_kernel(int64_t n, const double *__restrict__ rhs,
+                                       const double *__restrict__ u, const double *__restrict__ s,
+                                       const double *__restrict__ Kalpha, double *__restrict__ r) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = rhs[i] - (u[i] + s[i] * Kalpha[i]);
+}
 
 int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
                          double *fnew, double *logdetL) {
@@ -316,18 +327,36 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   GPGP_CUDA(cudaMemsetAsync(w.status.p, 0, sizeof(int), st));
   vec_rsqrt(st, n, m->V.p, m->s.p);
   make_B(st, w.K.p, n, m->s.p, m->L.p);
+  const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
   {
     Phase ph(ctx, GPGP_PHASE_POTRF);
-    potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
+    if (mixed)
+      potrf_mixed(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p, m->errflag.p);
+    else
+      potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
   }
   {
     Phase ph(ctx, GPGP_PHASE_SOLVE);
+    // u = B^-1 (s z) with B = L L^T; alpha = s u
     gauss_alpha_prep<<<g1(n), 256, 0, st>>>(n, m->s.p, zvec, w.t1.p);
     GPGP_CHECK_LAUNCH();
+    GPGP_CUDA(cudaMemcpyAsync(w.rhs.p, w.t1.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     trsv_lower(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, w.status.p);
-    trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, w.status.p);
-    vec_mul(st, n, m->s.p, w.t1.p, alpha);
+    trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, w.status.p);
+    vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+    if (mixed) {
+      // FP64 iterative refinement in B-space: r = s z - B u, B u = u + s (K alpha)
+      for (int it = 0; it < std::max(1, m->opts.refine_iters); ++it) {
+        refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
+        GPGP_CHECK_LAUNCH();
+        trsv_lower(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, w.status.p);
+        trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, w.status.p);
+        vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
+        vec_mul(st, n, m->s.p, w.u.p, alpha);
+        gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+      }
+    }
   }
   const int64_t nblk = (n + NB - 1) / NB;
   sum_vec(st, w.logdet_part.p, nblk, logdetL);
@@ -335,26 +364,46 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   GPGP_CUDA(cudaMemcpyAsync(&hstatus, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   GPGP_CUDA(cudaStreamSynchronize(st));
   m->have_binv_diag = false;
+  m->have_Linv = false;
   return hstatus;
 }
 
-// diag(B^-1) = column sums of squares of L^-1 (one triangular inverse).
+// W = L^-1, kept on the model (FP64 blocked solve or the sliced recursive inverse).
+void compute_linv(gpgp_model *m) {
+  if (m->have_Linv) return;
+  cudaStream_t st = m->ctx->stream;
+  const int64_t n = m->n;
+  if (m->Linv.n != (size_t)n * n) m->Linv.alloc(st, (size_t)n * n);
+  Phase ph(m->ctx, GPGP_PHASE_TRTRI);
+  if (m->opts.precision == GPGP_PREC_MIXED) {
+    trtri_mixed(st, m->L.p, n, n, m->Winv.p, m->Linv.p, n, m->errflag.p);
+  } else {
+    DBuf tmp;
+    tmp.alloc(st, (size_t)NB * n);
+    IBuf status;
+    status.alloc(st, 1);
+    GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+    trtri_lower(st, m->L.p, n, n, m->Winv.p, m->Linv.p, n, tmp.p, status.p);
+  }
+  m->have_Linv = true;
+}
+
+// diag(B^-1) = column sums of squares of L^-1.
 void compute_binv_diag(gpgp_model *m) {
   cudaStream_t st = m->ctx->stream;
   const int64_t n = m->n;
-  DBuf Wt, tmp;
-  Wt.alloc(st, (size_t)n * n);
-  tmp.alloc(st, (size_t)NB * n);
-  IBuf status;
-  status.alloc(st, 1);
-  GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
-  {
-    Phase ph(m->ctx, GPGP_PHASE_TRTRI);
-    trtri_lower(st, m->L.p, n, n, m->Winv.p, Wt.p, n, tmp.p, status.p);
-  }
+  compute_linv(m);
   m->binv_diag.alloc(st, n);
-  col_sumsq_lower(st, Wt.p, n, n, m->binv_diag.p);
+  col_sumsq_lower(st, m->Linv.p, n, n, m->binv_diag.p);
   m->have_binv_diag = true;
+}
+
+// Reads the tensor-core error flag; a set flag means a bounded wait ran out.
+bool tc_error(gpgp_model *m) {
+  int h = 0;
+  GPGP_CUDA(cudaMemcpyAsync(&h, m->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, m->ctx->stream));
+  GPGP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return h != 0;
 }
 
 gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
@@ -367,6 +416,8 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
   w.K.alloc(st, (size_t)n * n);
   w.t1.alloc(st, n);
   w.t2.alloc(st, n);
+  w.u.alloc(st, n);
+  w.rhs.alloc(st, n);
   w.red.alloc(st, 256);
   w.logdet_part.alloc(st, (n + NB - 1) / NB + 1);
   w.tmpv.alloc(st, n);
@@ -570,8 +621,8 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
     return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial likelihood");
   if (method->kind != GPGP_METHOD_FULL)
     return fail(ctx, GPGP_EUNSUPPORTED, "method_fitc is not available in this build");
-  if (opts->precision != GPGP_PREC_FP64)
-    return fail(ctx, GPGP_EUNSUPPORTED, "mixed precision is not available in this build");
+  if (opts->precision != GPGP_PREC_FP64 && opts->precision != GPGP_PREC_MIXED)
+    return fail(ctx, GPGP_EINVAL, "unknown precision");
   std::unique_ptr<gpgp_model> m(new gpgp_model());
   m->ctx = ctx;
   m->spec = *k;
@@ -586,6 +637,8 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   gpgp_status st = build_dev_kernel(k, d, &m->dk, &m->prep, &err);
   if (st != GPGP_OK) return fail(ctx, st, err);
   cudaStream_t s = ctx->stream;
+  m->errflag.alloc(s, 1);
+  GPGP_CUDA(cudaMemsetAsync(m->errflag.p, 0, sizeof(int), s));
   copy_in(s, m->x, x, (size_t)n * d, on_device);
   copy_in(s, m->y, y, n, on_device);
   if (trials) {
@@ -603,6 +656,7 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
     GPGP_CUDA(cudaStreamSynchronize(s));
     return st;
   }
+  if (tc_error(m.get())) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
   m->fitted = 1;
   GPGP_CUDA(cudaStreamSynchronize(s));
   *model = m.release();
@@ -882,12 +936,18 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       IBuf status;
       status.alloc(s, 1);
       GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+      const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
+      if (mixed) compute_linv(m);
       for (int64_t c0 = 0; c0 < mt; c0 += chunk) {
         const int64_t mc = std::min(chunk, mt - c0);
         cov_matrix(s, m->dk, gm, m->F.p, n, n, Ft.p + c0, mt, mc, R.p, n, COV_ROWSCALE, 0, 0, 0.0,
                    m->s.p);
-        trsm_lower(s, m->L.p, n, n, m->Winv.p, R.p, mc, n, tmp.p, status.p);
-        col_sumsq(s, R.p, n, mc, n, csum.p + c0);
+        if (mixed) {
+          trmv_sumsq_mixed(s, m->Linv.p, n, n, R.p, mc, n, csum.p + c0, m->errflag.p);
+        } else {
+          trsm_lower(s, m->L.p, n, n, m->Winv.p, R.p, mc, n, tmp.p, status.p);
+          col_sumsq(s, R.p, n, mc, n, csum.p + c0);
+        }
       }
       cov_diag(s, m->dk, gm, Ft.p, mt, Ft.p, mt, mt, kdiag.p);
       sub_from_kernel<<<g1(mt), 256, 0, s>>>(mt, kdiag.p, csum.p);
@@ -898,6 +958,7 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
     if (!on_device)
       GPGP_CUDA(cudaMemcpyAsync(mean, mout, mt * sizeof(double), cudaMemcpyDeviceToHost, s));
     GPGP_CUDA(cudaStreamSynchronize(s));
+    if (tc_error(m)) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
     return GPGP_OK;
   });
 }
@@ -965,23 +1026,17 @@ gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_
     GPGP_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const int64_t n = m->n;
-    DBuf Wt, Bi, tmp, part, g, dg, red;
-    IBuf status;
-    status.alloc(s, 1);
-    GPGP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
-    Wt.alloc(s, (size_t)n * n);
-    tmp.alloc(s, (size_t)NB * n);
-    {
-      Phase ph(ctx, GPGP_PHASE_TRTRI);
-      trtri_lower(s, m->L.p, n, n, m->Winv.p, Wt.p, n, tmp.p, status.p);
-    }
+    DBuf Bi, part, g, dg, red;
+    compute_linv(m);
     Bi.alloc(s, (size_t)n * n);
     {
       // B^-1 = W^T W (lower part), W = L^-1
       Phase ph(ctx, GPGP_PHASE_LAUUM);
-      gemm64(s, true, false, n, n, n, 1.0, Wt.p, n, Wt.p, n, 0.0, Bi.p, n, true, 1);
+      if (m->opts.precision == GPGP_PREC_MIXED)
+        lauum_mixed(s, m->Linv.p, n, n, Bi.p, n, m->errflag.p);
+      else
+        gemm64(s, true, false, n, n, n, 1.0, m->Linv.p, n, m->Linv.p, n, 0.0, Bi.p, n, true, 1);
     }
-    Wt.reset();
     // tr(C^-1) = sum_i s_i^2 Binv_ii
     dg.alloc(s, n);
     diag_scaled_kernel<<<g1(n), 256, 0, s>>>(n, Bi.p, m->s.p, dg.p);
@@ -1006,6 +1061,7 @@ gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_
     GPGP_CUDA(cudaMemcpyAsync(&h2[0], red.p + 200, sizeof(double), cudaMemcpyDeviceToHost, s));
     GPGP_CUDA(cudaMemcpyAsync(&h2[1], red.p + 64, sizeof(double), cudaMemcpyDeviceToHost, s));
     GPGP_CUDA(cudaStreamSynchronize(s));
+    if (tc_error(m)) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
     for (size_t i = 0; i < hg.size(); ++i) grad_terms[i] = 0.5 * hg[i];
     if (grad_lik_sigma) {
       const double s2 = m->lik.sigma * m->lik.sigma;

@@ -150,6 +150,39 @@ void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, cons
 void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out);
 
 // ---------------------------------------------------------------------------
+// mixed precision (mixed.cu / mixed_la.cu): BF16-sliced operands for tcgen05
+// ---------------------------------------------------------------------------
+struct OzSplit {
+  int *ex = nullptr;        // per-row power-of-two exponents (rows padded)
+  uint16_t *sl = nullptr;   // BF16 slices, pre-tiled for UMMA
+  int64_t rows = 0, K = 0, nrb = 0, nkb = 0;
+};
+int64_t oz_nrb(int64_t rows);
+size_t oz_split_bytes(int64_t rows, int64_t K);
+void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out);
+// rows x K operand: element (r, k) = P[r + k*ld] (trans 0) or P[k + r*ld] (trans 1)
+void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,
+              OzSplit *out);
+// C = alpha A B^T + beta C on K chunks [kc0, kc1) (64 wide); a_row0/b_row0 multiples of 64.
+// kmode: 0 all chunks; 1 start at max(row, col); 2 start at col; 3 stop after row.
+void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
+             int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
+             double *C, int64_t ldc, bool lower_only, int *err, const int *status = nullptr);
+void oz_set_desc_variant(int v);
+
+// Mixed-precision factorisation and inverses (same outputs as the FP64 versions).
+void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,
+                 double *logdet_part, int *status, int *err);
+void trtri_mixed(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                 double *W, int64_t ldw, int *err);
+// Binv (lower) = W^T W for lower-triangular W
+void lauum_mixed(cudaStream_t s, const double *W, int64_t n, int64_t ldw, double *Binv,
+                 int64_t ldb, int *err);
+// T = W R (W lower n x n, R n x m), then out[j] = sum_i T_ij^2
+void trmv_sumsq_mixed(cudaStream_t s, const double *W, int64_t n, int64_t ldw, const double *R,
+                      int64_t m, int64_t ldr, double *out, int *err);
+
+// ---------------------------------------------------------------------------
 // likelihood kernels
 // ---------------------------------------------------------------------------
 struct LikDev {

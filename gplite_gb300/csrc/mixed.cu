@@ -1,0 +1,498 @@
+// Mixed-precision dense kernels: FP64-accurate products on the tcgen05
+// tensor cores through exact BF16 slicing (an Ozaki-style split).
+//
+// Every operand row is scaled by a power of two so that its largest entry is
+// in [0.5, 1) and then cut into four 8-bit fixed-point slices
+//   x = 2^e * sum_t q_t 2^-8(t+1),  q_t integers in [-256, 256]
+// which BF16 holds exactly. A product of two slices is an integer below 2^16,
+// so a 64-long dot product of slice pairs (four pairs per level at most) stays
+// below 2^24 and the FP32 accumulators of tcgen05.mma hold it exactly. The 13
+// slice pairs with t + u <= 4 go into five level accumulators in TMEM; after
+// every 64-wide K chunk the levels are added into double-float (hi, lo) FP32
+// registers, and the result is written once in FP64:
+//   (A B^T)_ij = 2^(e_i + f_j - 16) sum_l 2^-8l P_l.
+// The truncation error is ~2^-33 of the row maxima, far below what the FP64
+// log-determinant and iterative refinement need for 1e-8 evidence accuracy.
+//
+// Data path: slices are stored pre-tiled in the canonical no-swizzle K-major
+// UMMA layout (8-row x 16-byte core matrices), so one cp.async.bulk per slice
+// tile moves them to shared memory; one elected thread issues the MMAs and a
+// tcgen05.commit arrives on an mbarrier; all eight warps drain TMEM with
+// tcgen05.ld. Every wait is bounded: on timeout the kernel records an error,
+// releases TMEM and returns.
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace gpgp {
+
+constexpr int OZ_S = 4;             // slices per operand
+constexpr int OZ_LEVELS = 5;        // levels kept (t + u <= 4): 13 products
+constexpr int OZ_TK = 64;           // K chunk
+constexpr int OZ_TR = 64;           // rows per slice tile
+constexpr int OZ_TILE = OZ_TR * OZ_TK;  // bf16 elements per slice tile (8 KB)
+constexpr int OZ_BM = 128, OZ_BN = 64;
+constexpr int OZ_A_STAGE = OZ_S * 2 * OZ_TILE * 2;  // bytes: 4 slices x 128 rows x 64 K x 2 B
+constexpr int OZ_B_STAGE = OZ_S * OZ_TILE * 2;      // bytes: 4 slices x 64 rows x 64 K x 2 B
+constexpr int OZ_STAGE = OZ_A_STAGE + OZ_B_STAGE;   // 96 KB
+constexpr int OZ_SMEM = 2 * OZ_STAGE + 1024;        // two stages + barriers
+constexpr uint32_t OZ_TMEM_COLS = 512;              // 5 levels x 64 columns (rounded to a power of 2)
+
+// Descriptor layout variant (selected by gpgp_mixed_selftest): 0 = LBO is the K
+// step (128 B), SBO the 8-row step (1024 B); 1 = the other way round.
+__device__ int g_oz_desc_variant = 0;
+static int h_oz_desc_variant = 0;
+
+// ---------------------------------------------------------------------------
+// split: FP64 rows -> 4 BF16 slices (canonical layout) + per-row exponents
+// ---------------------------------------------------------------------------
+// Element (r, k) of the logical rows x K operand is P[r + k*ld] (trans = 0)
+// or P[k + r*ld] (trans = 1). Tiles: [slice][kb][rb], 64 x 64 each; within a
+// tile, (r, k) lives at (r/8)*512 + (k/8)*64 + (r%8)*8 + (k%8) elements.
+__device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans, int64_t r,
+                                          int64_t k, int64_t rows, int64_t K) {
+  if (r >= rows || k >= K) return 0.0;
+  return trans ? P[k + r * ld] : P[r + k * ld];
+}
+
+__global__ void oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
+                                 int64_t K, int64_t rows_pad, int *__restrict__ ex) {
+  // one warp per row: coalesced when trans (row contiguous), strided otherwise
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= rows_pad) return;
+  double m = 0.0;
+  if (r < rows)
+    for (int64_t k = lane; k < K; k += 32) m = fmax(m, fabs(trans ? P[k + r * ld] : P[r + k * ld]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) {
+    int e = 0;
+    if (m > 0.0 && isfinite(m)) frexp(m, &e);
+    ex[r] = e;
+  }
+}
+
+__device__ __forceinline__ uint32_t bf16_bits_of_int(double q) {
+  // q is an integer with |q| <= 256: exact in FP32 and in BF16 (upper 16 bits)
+  return __float_as_uint((float)q) >> 16;
+}
+
+__global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
+                                int64_t K, int64_t nrb, int64_t nkb, const int *__restrict__ ex,
+                                uint16_t *__restrict__ sl) {
+  // thread per (row, 8-wide K group): writes 16 bytes per slice
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t rows_pad = nrb * OZ_TR;
+  const int64_t ngroups = nkb * (OZ_TK / 8);
+  if (tid >= rows_pad * ngroups) return;
+  const int64_t r = trans ? tid / ngroups : tid % rows_pad;
+  const int64_t g = trans ? tid % ngroups : tid / rows_pad;
+  const int64_t k0 = g * 8;
+  const int e = ex[r];
+  uint32_t packed[OZ_S][4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    double q[2][OZ_S];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      double x = ldexp(oz_elem(P, ld, trans, r, k0 + j + h, rows, K), -e);
+#pragma unroll
+      for (int t = 0; t < OZ_S; ++t) {
+        x = x * 256.0;
+        const double qt = rint(x);
+        x = x - qt;
+        q[h][t] = qt;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < OZ_S; ++t)
+      packed[t][j / 2] = bf16_bits_of_int(q[0][t]) | (bf16_bits_of_int(q[1][t]) << 16);
+  }
+  const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
+  const int64_t kb = k0 / OZ_TK, kk = k0 % OZ_TK;
+  const int64_t within = (rr / 8) * 512 + (kk / 8) * 64 + (rr % 8) * 8;
+#pragma unroll
+  for (int t = 0; t < OZ_S; ++t) {
+    const int64_t tile = ((int64_t)t * nkb + kb) * nrb + rb;
+    uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
+    *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) = v;
+  }
+}
+
+// 64-row tiles of a split operand: one more than the rows need, rounded up to
+// an even count, so that a 128-row A tile starting at any 64-row offset inside
+// the operand stays inside the buffer.
+int64_t oz_nrb(int64_t rows) {
+  const int64_t t = (rows + OZ_TR - 1) / OZ_TR + 1;
+  return (t + 1) / 2 * 2;
+}
+
+void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,
+              OzSplit *out) {
+  const int64_t nrb = oz_nrb(rows);
+  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
+  out->rows = rows;
+  out->K = K;
+  out->nrb = nrb;
+  out->nkb = nkb;
+  const int64_t rows_pad = nrb * OZ_TR;
+  {
+    const int64_t threads = rows_pad * 32;
+    oz_rowexp_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, ld, trans, rows, K, rows_pad,
+                                                                      out->ex);
+    GPGP_CHECK_LAUNCH();
+  }
+  {
+    const int64_t threads = rows_pad * nkb * (OZ_TK / 8);
+    oz_slice_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb,
+                                                                      out->ex, out->sl);
+    GPGP_CHECK_LAUNCH();
+  }
+}
+
+size_t oz_split_bytes(int64_t rows, int64_t K) {
+  const int64_t nrb = oz_nrb(rows);
+  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
+  return (size_t)nrb * OZ_TR * sizeof(int) + 256 + (size_t)OZ_S * nkb * nrb * OZ_TILE * 2;
+}
+
+void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out) {
+  const int64_t nrb = oz_nrb(rows);
+  (void)K;
+  char *p = (char *)mem;
+  out->ex = (int *)p;
+  size_t exb = ((size_t)nrb * OZ_TR * sizeof(int) + 255) / 256 * 256;
+  out->sl = (uint16_t *)(p + exb);
+}
+
+// ---------------------------------------------------------------------------
+// PTX helpers (tcgen05, mbarrier, bulk copy)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false after ~2^24 polls (about a second or more).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 24); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  // base offset 0, lbo mode 0, layout type 0 (no swizzle)
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// double-float accumulation of v into (hi, lo) with an error-free TwoSum
+__device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
+  const float s = __fadd_rn(hi, v);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
+// ---------------------------------------------------------------------------
+// the GEMM: C = alpha * A B^T + beta * C over the given K-chunk range
+// ---------------------------------------------------------------------------
+struct OzGemmArgs {
+  const uint16_t *a_sl;
+  const int *a_ex;
+  int64_t a_nrb, a_nkb, a_rb0;  // slice-tile geometry; first 64-row tile of this operand
+  const uint16_t *b_sl;
+  const int *b_ex;
+  int64_t b_nrb, b_nkb, b_rb0;
+  int64_t M, N;
+  int64_t kc0, kc1;  // K chunks [kc0, kc1) of both operands
+  int kmode;         // 0 all; 1 start at max(row,col)/64; 2 start at col/64; 3 end at row/64 + 2
+  double alpha, beta;
+  double *C;
+  int64_t ldc;
+  int lower_only;
+  int *err;
+  const int *status;  // optional: skip all work when a factorisation already failed
+};
+
+__global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // align the dynamic shared memory base to 1024 bytes
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int64_t row0 = (int64_t)blockIdx.x * OZ_BM;
+  const int64_t col0 = (int64_t)blockIdx.y * OZ_BN;
+  if (g.lower_only && col0 > row0 + OZ_BM - 1) return;
+
+  // K-chunk range of this tile
+  const int64_t grow0 = g.a_rb0 * OZ_TR + row0;  // absolute operand row of the tile
+  const int64_t gcol0 = g.b_rb0 * OZ_TR + col0;
+  int64_t kc0 = g.kc0, kc1 = g.kc1;
+  if (g.kmode == 1) {
+    const int64_t s0 = (grow0 > gcol0 ? grow0 : gcol0) / OZ_TK;
+    kc0 = kc0 > s0 ? kc0 : s0;
+  }
+  if (g.kmode == 2) {
+    const int64_t s0 = gcol0 / OZ_TK;
+    kc0 = kc0 > s0 ? kc0 : s0;
+  }
+  if (g.kmode == 3) {
+    const int64_t e0 = (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK;
+    kc1 = kc1 < e0 ? kc1 : e0;
+  }
+  if (g.status && *(volatile const int *)g.status != 0) return;
+  const int64_t nch = kc1 > kc0 ? kc1 - kc0 : 0;
+
+  uint64_t *bars = (uint64_t *)(smem + 2 * OZ_STAGE);
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_sh;
+  const uint32_t full0 = smem_u32(&bars[0]), full1 = smem_u32(&bars[1]), done = smem_u32(&bars[2]);
+  if (tid == 0) {
+    mbar_init(full0, 1);
+    mbar_init(full1, 1);
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_sh = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(OZ_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  // operand tile addresses for chunk c (global)
+  auto a_tile = [&](int s, int64_t kc) {
+    return g.a_sl + (((int64_t)s * g.a_nkb + kc) * g.a_nrb + g.a_rb0 + 2 * blockIdx.x) * OZ_TILE;
+  };
+  auto b_tile = [&](int s, int64_t kc) {
+    return g.b_sl + (((int64_t)s * g.b_nkb + kc) * g.b_nrb + g.b_rb0 + blockIdx.y) * OZ_TILE;
+  };
+  auto load_stage = [&](int st, int64_t kc) {
+    const uint32_t base = smem_u32(smem + st * OZ_STAGE);
+    const uint32_t bar = st ? full1 : full0;
+    mbar_expect_tx(bar, OZ_STAGE);
+    for (int s = 0; s < OZ_S; ++s) {
+      bulk_g2s(base + s * (2 * OZ_TILE * 2), a_tile(s, kc), 2 * OZ_TILE * 2, bar);
+      bulk_g2s(base + OZ_A_STAGE + s * (OZ_TILE * 2), b_tile(s, kc), OZ_TILE * 2, bar);
+    }
+  };
+
+  if (tid == 0) {
+    if (nch > 0) load_stage(0, kc0);
+    if (nch > 1) load_stage(1, kc0 + 1);
+  }
+
+  // instruction descriptor: D F32, A/B BF16, K-major both, N = 64, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+                         ((uint32_t)(OZ_BM >> 4) << 24);
+  const int variant = g_oz_desc_variant;
+  const uint32_t lbo = variant ? 1024u : 128u, sbo = variant ? 128u : 1024u;
+
+  // epilogue ownership: warp w reads TMEM lanes 32*(w%4).., columns 32*(w/4)..
+  const int quarter = warp & 3, half = warp >> 2;
+  const int64_t my_row = row0 + quarter * 32 + lane;
+  float hi[32], lo[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0.f;
+
+  bool ok = true;
+  for (int64_t c = 0; c < nch; ++c) {
+    const int st = (int)(c & 1);
+    const uint32_t parity = (uint32_t)((c >> 1) & 1);
+    if (tid == 0) {
+      if (!mbar_wait_bounded(st ? full1 : full0, parity)) {
+        atomicExch(g.err, 1);
+        abort_sh = 1;
+      } else {
+        tc_fence_after();
+        const uint32_t abase = smem_u32(smem + st * OZ_STAGE);
+        const uint32_t bbase = abase + OZ_A_STAGE;
+        int first[OZ_LEVELS] = {1, 1, 1, 1, 1};
+#pragma unroll
+        for (int t = 0; t < OZ_S; ++t) {
+#pragma unroll
+          for (int u = 0; u < OZ_S; ++u) {
+            const int lev = t + u;
+            if (lev >= OZ_LEVELS) continue;
+#pragma unroll
+            for (int kk = 0; kk < OZ_TK / 16; ++kk) {
+              const uint64_t ad = umma_desc(abase + t * (2 * OZ_TILE * 2) + kk * 2 * 128, lbo, sbo);
+              const uint64_t bd = umma_desc(bbase + u * (OZ_TILE * 2) + kk * 2 * 128, lbo, sbo);
+              umma_bf16(tmem + lev * OZ_BN, ad, bd, idesc, first[lev] ? 0u : 1u);
+              first[lev] = 0;
+            }
+          }
+        }
+        umma_commit(done);
+      }
+    }
+    __syncthreads();
+    if (abort_sh) {
+      ok = false;
+      break;
+    }
+    const bool waited = mbar_wait_bounded(done, (uint32_t)(c & 1));
+    if (__syncthreads_or(!waited)) {
+      if (tid == 0) atomicExch(g.err, 2);
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+    // stage st is free again: prefetch chunk c + 2
+    if (tid == 0 && c + 2 < nch) load_stage(st, kc0 + c + 2);
+#pragma unroll 1
+    for (int lev = 0; lev < OZ_LEVELS; ++lev) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + lev * OZ_BN + half * 32, r);
+      tmem_ld_wait();
+      const float sc = __uint_as_float((uint32_t)(127 - 8 * lev) << 23);  // 2^-8lev
+#pragma unroll
+      for (int j = 0; j < 32; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  __syncthreads();
+  if (!ok && tid == 0) {
+    // a wait ran out: give in-flight MMAs and bulk copies a bounded chance to land
+    // before the shared memory and TMEM are released
+    mbar_wait_bounded(done, 0);
+    mbar_wait_bounded(done, 1);
+    mbar_wait_bounded(full0, 0);
+    mbar_wait_bounded(full1, 0);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
+  }
+  if (!ok) return;
+  // FP64 epilogue: C = alpha * 2^(e_i + f_j - 16) (hi + lo) + beta * C
+  if (my_row < g.M) {
+    const int ea = g.a_ex[g.a_rb0 * OZ_TR + my_row];
+#pragma unroll 4
+    for (int j = 0; j < 32; ++j) {
+      const int64_t col = col0 + half * 32 + j;
+      if (col >= g.N) break;
+      if (g.lower_only && my_row < col) continue;
+      const int eb = g.b_ex[g.b_rb0 * OZ_TR + col];
+      const double v = ldexp((double)hi[j] + (double)lo[j], ea + eb - 16);
+      double *dst = g.C + my_row + col * g.ldc;
+      *dst = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * *dst);
+    }
+  }
+}
+
+void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
+             int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
+             double *C, int64_t ldc, bool lower_only, int *err, const int *status) {
+  if (M <= 0 || N <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM + 1024));
+    attr = true;
+  }
+  OzGemmArgs g;
+  g.a_sl = A.sl;
+  g.a_ex = A.ex;
+  g.a_nrb = A.nrb;
+  g.a_nkb = A.nkb;
+  g.a_rb0 = a_row0 / OZ_TR;
+  g.b_sl = B.sl;
+  g.b_ex = B.ex;
+  g.b_nrb = B.nrb;
+  g.b_nkb = B.nkb;
+  g.b_rb0 = b_row0 / OZ_TR;
+  g.M = M;
+  g.N = N;
+  g.kc0 = kc0;
+  g.kc1 = kc1;
+  g.kmode = kmode;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.C = C;
+  g.ldc = ldc;
+  g.lower_only = lower_only ? 1 : 0;
+  g.err = err;
+  g.status = status;
+  dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OZ_BN - 1) / OZ_BN));
+  oz_gemm_kernel<<<grid, 256, OZ_SMEM + 1024, s>>>(g);
+  GPGP_CHECK_LAUNCH();
+}
+
+void oz_set_desc_variant(int v) {
+  if (v == h_oz_desc_variant) return;
+  GPGP_CUDA(cudaMemcpyToSymbol(g_oz_desc_variant, &v, sizeof(int)));
+  h_oz_desc_variant = v;
+}
+
+}  // namespace gpgp

@@ -1,0 +1,277 @@
+// Mixed-precision blocked algorithms built on the sliced tensor-core GEMM
+// (mixed.cu): Cholesky, triangular inverse, B^-1 = L^-T L^-1 and the
+// predictive-variance product. Outputs have the same meaning and layout as the
+// FP64 routines of dense.cu; only the contractions change precision (products
+// of 32-bit fixed-point row slices, accumulated exactly, summed in FP64).
+//
+// Cholesky is two-level right-looking: 256-wide outer panels, each factored
+// with the 64-wide FP64 diagonal kernel of dense.cu, a sliced GEMM for the
+// panel solve L21 = A21 W11^T and sliced GEMMs for the updates inside the
+// panel; one sliced SYRK with K = 256 then updates the trailing matrix, so
+// every trailing element is rewritten in FP64 once per 256 columns.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gpgp {
+
+// potrf_diag_kernel lives in dense.cu
+__global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
+                                  double *__restrict__ Winv, double *__restrict__ logdet_part,
+                                  int *__restrict__ status, int64_t k0);
+
+namespace {
+
+// Stream-ordered scratch for split operands (freed when the scope ends).
+struct SplitBuf {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  OzSplit sp;
+  SplitBuf(cudaStream_t st, int64_t rows, int64_t K) : s(st) {
+    const size_t b = oz_split_bytes(rows, K);
+    if (cudaMallocAsync(&p, b, st) != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    oz_split_bind(p, rows, K, &sp);
+  }
+  ~SplitBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+constexpr int64_t NBO = 256;  // outer panel width of the mixed Cholesky
+
+}  // namespace
+
+void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,
+                 double *logdet_part, int *status, int *err) {
+  SplitBuf a(s, n, NBO);   // panel operand (rows below the current block)
+  SplitBuf w(s, NB, NB);   // inverse of the diagonal block
+  for (int64_t k0 = 0; k0 < n; k0 += NBO) {
+    const int64_t kbo = std::min<int64_t>(NBO, n - k0);
+    for (int64_t j0 = k0; j0 < k0 + kbo; j0 += NB) {
+      const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
+      const int64_t blk = j0 / NB;
+      double *Wb = Winv + blk * NB * NB;
+      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0);
+      GPGP_CHECK_LAUNCH();
+      const int64_t m = n - j0 - jb;
+      if (m <= 0) continue;
+      double *A21 = A + (j0 + jb) + j0 * lda;
+      // L21 = A21 W^T (W = L11^-1): sliced GEMM, result written over A21
+      oz_split(s, A21, lda, 0, m, jb, &a.sp);
+      oz_split(s, Wb, NB, 0, jb, jb, &w.sp);
+      oz_gemm(s, a.sp, 0, w.sp, 0, m, jb, 0, 1, 0, 1.0, 0.0, A21, lda, false, err, status);
+      // update of the remaining columns of this outer panel
+      const int64_t nc = k0 + kbo - (j0 + jb);
+      if (nc > 0) {
+        oz_split(s, A21, lda, 0, m, jb, &a.sp);
+        oz_gemm(s, a.sp, 0, a.sp, 0, m, nc, 0, 1, 0, -1.0, 1.0, A + (j0 + jb) + (j0 + jb) * lda, lda,
+                true, err, status);
+      }
+    }
+    const int64_t m2 = n - k0 - kbo;
+    if (m2 > 0) {
+      double *P = A + (k0 + kbo) + k0 * lda;
+      oz_split(s, P, lda, 0, m2, kbo, &a.sp);
+      oz_gemm(s, a.sp, 0, a.sp, 0, m2, m2, 0, (kbo + 63) / 64, 0, -1.0, 1.0,
+              A + (k0 + kbo) + (k0 + kbo) * lda, lda, true, err, status);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// recursive triangular inverse: W = L^-1, W21 = -W22 (L21 W11)
+// ---------------------------------------------------------------------------
+static void copy_diag_inverse(cudaStream_t s, const double *Winv, int64_t blk, int kb, double *W,
+                              int64_t ldw) {
+  GPGP_CUDA(cudaMemcpy2DAsync(W, ldw * sizeof(double), Winv + blk * NB * NB, NB * sizeof(double),
+                              kb * sizeof(double), kb, cudaMemcpyDeviceToDevice, s));
+}
+
+static void trtri_rec(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                      int64_t off, double *W, int64_t ldw, double *T, int *err) {
+  if (n <= NB) {
+    copy_diag_inverse(s, Winv, off / NB, (int)n, W, ldw);
+    return;
+  }
+  const int64_t n1 = ((n / 2) + NB - 1) / NB * NB;
+  const int64_t n2 = n - n1;
+  trtri_rec(s, L, n1, lda, Winv, off, W, ldw, T, err);
+  trtri_rec(s, L + n1 + n1 * lda, n2, lda, Winv, off + n1, W + n1 + n1 * ldw, ldw, T, err);
+  // T = L21 W11  (n2 x n1): A = L21 (rows n2, K n1), B rows j = columns of W11 (W11[k, j], k >= j)
+  {
+    SplitBuf a(s, n2, n1), b(s, n1, n1);
+    oz_split(s, L + n1, lda, 0, n2, n1, &a.sp);
+    oz_split(s, W, ldw, 1, n1, n1, &b.sp);
+    oz_gemm(s, a.sp, 0, b.sp, 0, n2, n1, 0, b.sp.nkb, 2, 1.0, 0.0, T, n2, false, err);
+  }
+  // W21 = -W22 T  (n2 x n1): A = W22 (rows n2, K n2, lower: k <= i), B rows j = columns of T
+  {
+    SplitBuf a(s, n2, n2), b(s, n1, n2);
+    oz_split(s, W + n1 + n1 * ldw, ldw, 0, n2, n2, &a.sp);
+    oz_split(s, T, n2, 1, n1, n2, &b.sp);
+    oz_gemm(s, a.sp, 0, b.sp, 0, n2, n1, 0, a.sp.nkb, 3, -1.0, 0.0, W + n1, ldw, false, err);
+  }
+}
+
+__global__ void zero_upper_kernel(double *W, int64_t n, int64_t ldw) {
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < j;
+         i += (int64_t)gridDim.x * blockDim.x)
+      W[i + j * ldw] = 0.0;
+}
+
+void trtri_mixed(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+                 double *W, int64_t ldw, int *err) {
+  if (n <= 0) return;
+  dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
+  zero_upper_kernel<<<g, 256, 0, s>>>(W, n, ldw);
+  GPGP_CHECK_LAUNCH();
+  double *T = nullptr;
+  const int64_t h = (n / 2 + NB) * (n / 2 + NB);
+  if (cudaMallocAsync((void **)&T, (size_t)h * sizeof(double), s) != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  try {
+    trtri_rec(s, L, n, lda, Winv, 0, W, ldw, T, err);
+  } catch (...) {
+    cudaFreeAsync(T, s);
+    throw;
+  }
+  GPGP_CUDA(cudaFreeAsync(T, s));
+}
+
+void lauum_mixed(cudaStream_t s, const double *W, int64_t n, int64_t ldw, double *Binv,
+                 int64_t ldb, int *err) {
+  // Binv_ij = sum_k W_ki W_kj (k >= max(i, j)); operand rows = columns of W
+  SplitBuf a(s, n, n);
+  oz_split(s, W, ldw, 1, n, n, &a.sp);
+  oz_gemm(s, a.sp, 0, a.sp, 0, n, n, 0, a.sp.nkb, 1, 1.0, 0.0, Binv, ldb, true, err);
+}
+
+void trmv_sumsq_mixed(cudaStream_t s, const double *W, int64_t n, int64_t ldw, const double *R,
+                      int64_t m, int64_t ldr, double *out, int *err) {
+  // T = W R (n x m): A = W (rows n, K n, k <= i), B rows j = columns of R
+  double *T = nullptr;
+  if (cudaMallocAsync((void **)&T, (size_t)n * m * sizeof(double), s) != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  {
+    SplitBuf a(s, n, n), b(s, m, n);
+    oz_split(s, W, ldw, 0, n, n, &a.sp);
+    oz_split(s, R, ldr, 1, m, n, &b.sp);
+    oz_gemm(s, a.sp, 0, b.sp, 0, n, m, 0, a.sp.nkb, 3, 1.0, 0.0, T, n, false, err);
+  }
+  col_sumsq(s, T, n, m, n, out);
+  GPGP_CUDA(cudaFreeAsync(T, s));
+}
+
+}  // namespace gpgp
+
+// ---------------------------------------------------------------------------
+// self-test entry point: sliced GEMM against the FP64 GEMM on random data
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void fill_random_kernel(double *a, int64_t n, uint64_t seed, double scale_spread) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    // entries of varying magnitude exercise the per-row scaling
+    const double mag = exp2(scale_spread * (double)((z >> 3) & 7) / 7.0 - scale_spread / 2);
+    a[i] = u * mag;
+  }
+}
+
+__global__ void max_abs_kernel(const double *a, const double *b, int64_t n, double *out) {
+  __shared__ double sd[256], sm[256];
+  double d = 0.0, m = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) {
+    d = fmax(d, fabs(a[i] - b[i]));
+    m = fmax(m, fabs(b[i]));
+  }
+  sd[threadIdx.x] = d;
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + st]);
+      sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + st]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sd[0];
+    out[1] = sm[0];
+  }
+}
+}  // namespace
+
+extern "C" gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K,
+                                           int32_t variant, double *max_rel_err) {
+  using namespace gpgp;
+  if (!ctx || M < 1 || N < 1 || K < 1 || !max_rel_err) return GPGP_EINVAL;
+  cudaStream_t s = (cudaStream_t)gpgp_stream(ctx);
+  try {
+    oz_set_desc_variant(variant);
+    double *A = nullptr, *B = nullptr, *C1 = nullptr, *C2 = nullptr, *red = nullptr;
+    int *err = nullptr;
+    GPGP_CUDA(cudaMallocAsync((void **)&A, M * K * sizeof(double), s));
+    GPGP_CUDA(cudaMallocAsync((void **)&B, N * K * sizeof(double), s));
+    GPGP_CUDA(cudaMallocAsync((void **)&C1, M * N * sizeof(double), s));
+    GPGP_CUDA(cudaMallocAsync((void **)&C2, M * N * sizeof(double), s));
+    GPGP_CUDA(cudaMallocAsync((void **)&red, 4 * sizeof(double), s));
+    GPGP_CUDA(cudaMallocAsync((void **)&err, sizeof(int), s));
+    GPGP_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    fill_random_kernel<<<256, 256, 0, s>>>(A, M * K, 12345, 8.0);
+    fill_random_kernel<<<256, 256, 0, s>>>(B, N * K, 777, 8.0);
+    fill_random_kernel<<<256, 256, 0, s>>>(C1, M * N, 99, 0.0);
+    GPGP_CUDA(cudaMemcpyAsync(C2, C1, M * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    {
+      void *pa = nullptr, *pb = nullptr;
+      GPGP_CUDA(cudaMallocAsync(&pa, oz_split_bytes(M, K), s));
+      GPGP_CUDA(cudaMallocAsync(&pb, oz_split_bytes(N, K), s));
+      OzSplit sa, sb;
+      oz_split_bind(pa, M, K, &sa);
+      oz_split_bind(pb, N, K, &sb);
+      oz_split(s, A, M, 0, M, K, &sa);
+      oz_split(s, B, N, 0, N, K, &sb);
+      // C1 = -A B^T + C1 (sliced) ; C2 = -A B^T + C2 (FP64)
+      oz_gemm(s, sa, 0, sb, 0, M, N, 0, sa.nkb, 0, -1.0, 1.0, C1, M, false, err);
+      gemm64(s, false, true, M, N, K, -1.0, A, M, B, N, 1.0, C2, M);
+      max_abs_kernel<<<1, 256, 0, s>>>(C1, C2, M * N, red);
+      cudaFreeAsync(pa, s);
+      cudaFreeAsync(pb, s);
+    }
+    double h[2];
+    int herr = 0;
+    GPGP_CUDA(cudaMemcpyAsync(h, red, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    cudaFreeAsync(A, s);
+    cudaFreeAsync(B, s);
+    cudaFreeAsync(C1, s);
+    cudaFreeAsync(C2, s);
+    cudaFreeAsync(red, s);
+    cudaFreeAsync(err, s);
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    *max_rel_err = h[0] / (h[1] > 0 ? h[1] : 1.0);
+    if (herr) return GPGP_ETIMEOUT;
+    return GPGP_OK;
+  } catch (const CudaError &) {
+    return GPGP_ECUDA;
+  } catch (const std::bad_alloc &) {
+    return GPGP_EOOM;
+  }
+}

@@ -252,6 +252,14 @@ gpgp_status gpgp_pred_dev(gpgp_model *model, const double *xt, int64_t m, uint32
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
 
+/* ---- self-test of the mixed-precision product: C = C - A B^T for random
+ *      M x K and N x K operands with entries spread over 2^8 in magnitude,
+ *      computed with the BF16-sliced tensor-core GEMM and with the FP64 GEMM;
+ *      returns max |difference| / max |C|. variant selects the shared-memory
+ *      descriptor convention (0 default) and stays selected afterwards. ---- */
+gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K, int32_t variant,
+                                double *max_rel_err);
+
 #ifdef __cplusplus
 }
 #endif
