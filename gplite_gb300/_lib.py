@@ -96,6 +96,8 @@ SIGNATURES = {
     "gpgp_pred_dev": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_loo": (C.c_int, [_P, C.c_int32, _P, _P]),
     "gpgp_mixed_selftest": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P]),
+    "gpgp_fit_gaussian_noalloc": (C.c_int, [_P, C.POINTER(Kernel), C.c_double, C.c_double, _P, C.c_int64,
+                                            C.c_int32, _P, _P, _P]),
 }
 
 _lib = None

@@ -252,6 +252,26 @@ gpgp_status gpgp_pred_dev(gpgp_model *model, const double *xt, int64_t m, uint32
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
 
+/* ---- allocation-free Gaussian fit (no counterpart in the reference) ---
+ * For callers that cannot allocate device memory while they need a fit: a
+ * serving process whose own pool already owns all of HBM, a latency-critical
+ * request path where an allocation stall or failure is not acceptable, or a
+ * host framework that forbids allocation while it drives the GPU. Runs the
+ * plain FP64 fit of gp_fit for lik_gaussian + method_full and writes alpha (n
+ * doubles, device memory) and the log evidence (one double, host memory);
+ * x (n-by-d column-major) and y are device memory owned by the caller.
+ * All scratch lives in one fixed device array of the library (about 4.8 MB,
+ * held by every GPU that loads the library until the process exits), so the
+ * call never allocates. Limits: n <= 512 and at most 64 feature columns,
+ * otherwise GPGP_EINVAL. The first call on a device looks up the array's
+ * device address (make it before any stream capture) and needs the
+ * context's device current. Calls share the array: calls whose GPU work
+ * overlaps race on it and must be serialised. Returns GPGP_ENOT_PD (and
+ * -Inf) when the factorisation fails. */
+gpgp_status gpgp_fit_gaussian_noalloc(gpgp_ctx *ctx, const gpgp_kernel *k, double sigma,
+                                      double jitter, const double *x, int64_t n, int32_t d,
+                                      const double *y, double *alpha, double *log_evidence);
+
 /* ---- self-test of the mixed-precision product: C = C - A B^T for random
  *      M x K and N x K operands with entries spread over 2^8 in magnitude,
  *      computed with the BF16-sliced tensor-core GEMM and with the FP64 GEMM;
