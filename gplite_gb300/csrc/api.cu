@@ -20,173 +20,15 @@
 #include <vector>
 
 #include "common.cuh"
+#include "model.cuh"
 
 using namespace gpgp;
 
-struct gpgp_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string last_error;
-  double *h_pinned = nullptr;  // host pinned scalars
-  // live profiling: (phase, start event, stop event) per recorded interval
-  bool prof = false;
-  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
-  double prof_ms[GPGP_NPHASE] = {0};
-  int64_t prof_calls[GPGP_NPHASE] = {0};
-};
-
-namespace {
-// Scoped phase timer: records a pair of events on the context stream when enabled.
-struct Phase {
-  gpgp_ctx *c;
-  int ph;
-  cudaEvent_t a = nullptr, b = nullptr;
-  Phase(gpgp_ctx *ctx, int phase) : c(ctx), ph(phase) {
-    if (!c->prof) return;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    cudaEventRecord(a, c->stream);
-  }
-  ~Phase() {
-    if (!c->prof || !a) return;
-    cudaEventRecord(b, c->stream);
-    c->prof_ev.push_back({ph, {a, b}});
-  }
-};
-
-void prof_collect(gpgp_ctx *c) {
-  for (auto &e : c->prof_ev) {
-    float ms = 0.f;
-    cudaEventSynchronize(e.second.second);
-    cudaEventElapsedTime(&ms, e.second.first, e.second.second);
-    c->prof_ms[e.first] += ms;
-    c->prof_calls[e.first] += 1;
-    cudaEventDestroy(e.second.first);
-    cudaEventDestroy(e.second.second);
-  }
-  c->prof_ev.clear();
-}
-}  // namespace
-
-namespace {
-
-// RAII device buffer on the context's stream-ordered pool.
-struct DBuf {
-  double *p = nullptr;
-  size_t n = 0;
-  cudaStream_t s = nullptr;
-  DBuf() = default;
-  DBuf(const DBuf &) = delete;
-  DBuf &operator=(const DBuf &) = delete;
-  ~DBuf() { reset(); }
-  void alloc(cudaStream_t st, size_t count) {
-    reset();
-    s = st;
-    n = count;
-    if (count == 0) return;
-    cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(double), st);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      (void)cudaGetLastError();
-      throw std::bad_alloc();
-    }
-  }
-  void reset() {
-    if (p) cudaFreeAsync(p, s);
-    p = nullptr;
-    n = 0;
-  }
-};
-
-struct IBuf {
-  int *p = nullptr;
-  cudaStream_t s = nullptr;
-  ~IBuf() {
-    if (p) cudaFreeAsync(p, s);
-  }
-  void alloc(cudaStream_t st, size_t count) {
-    s = st;
-    if (cudaMallocAsync((void **)&p, count * sizeof(int), st) != cudaSuccess) {
-      p = nullptr;
-      (void)cudaGetLastError();
-      throw std::bad_alloc();
-    }
-  }
-};
-
-}  // namespace
-
-struct gpgp_model {
-  gpgp_ctx *ctx = nullptr;
-  gpgp_kernel spec;
-  DevKernel dk;
-  std::vector<HostTermPrep> prep;
-  gpgp_lik lik;
-  LikDev lk;
-  gpgp_method method;
-  gpgp_approx approx;
-  gpgp_fit_opts opts;
-  int64_t n = 0;
-  int d = 0;
-  // inputs (owned copies)
-  DBuf x, y, trials, offset, F;
-  // full-method fit
-  DBuf L, Winv, s, alpha, fmean, z, V;
-  DBuf fvar, cav_mean, cav_var;  // EP
-  DBuf binv_diag;                // diag(B^-1), filled on demand
-  bool have_binv_diag = false;
-  DBuf Linv;                     // W = L^-1, kept resident once computed (mixed precision)
-  bool have_Linv = false;
-  IBuf errflag;                  // bounded-wait timeouts of the tensor-core kernels
-  bool has_trials = false, has_offset = false;
-  double log_evidence = 0.0;
-  int fitted = 0;
-};
-
-namespace {
-
+namespace gpgp {
 thread_local std::string tl_error;
-
-gpgp_status fail(gpgp_ctx *ctx, gpgp_status st, const std::string &msg) {
-  if (ctx) ctx->last_error = msg;
-  tl_error = msg;
-  return st;
 }
 
-template <class F>
-gpgp_status guarded(gpgp_ctx *ctx, F &&fn) {
-  try {
-    return fn();
-  } catch (const CudaError &e) {
-    std::string m = std::string("CUDA error ") + cudaGetErrorString(e.err) + " in " + e.what;
-    return fail(ctx, GPGP_ECUDA, m);
-  } catch (const std::bad_alloc &) {
-    return fail(ctx, GPGP_EOOM, "device or host allocation failed");
-  }
-}
-
-LikDev make_likdev(const gpgp_lik &l) {
-  LikDev d;
-  d.kind = l.kind;
-  d.link = l.link;
-  d.sigma = l.sigma;
-  d.phi = l.phi;
-  return d;
-}
-
-void copy_in(cudaStream_t s, DBuf &dst, const double *src, size_t count, bool src_on_device) {
-  dst.alloc(s, count);
-  if (count == 0) return;
-  GPGP_CUDA(cudaMemcpyAsync(dst.p, src, count * sizeof(double),
-                            src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-}
-
-double read_scalar(gpgp_ctx *ctx, const double *dptr) {
-  GPGP_CUDA(cudaMemcpyAsync(ctx->h_pinned, dptr, sizeof(double), cudaMemcpyDeviceToHost,
-                            ctx->stream));
-  GPGP_CUDA(cudaStreamSynchronize(ctx->stream));
-  return ctx->h_pinned[0];
-}
+namespace {
 
 // ---------------------------------------------------------------------------
 // small elementwise kernels used only by the orchestration
@@ -294,7 +136,6 @@ __global__ void sub_from_kernel(int64_t n, const double *__restrict__ a, double 
   if (i < n) b[i] = a[i] - b[i];
 }
 
-inline unsigned g1(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + 255) / 256); }
 
 void make_B(cudaStream_t st, const double *K, int64_t n, const double *s, double *B) {
   dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
@@ -341,8 +182,9 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     gauss_alpha_prep<<<g1(n), 256, 0, st>>>(n, m->s.p, zvec, w.t1.p);
     GPGP_CHECK_LAUNCH();
     GPGP_CUDA(cudaMemcpyAsync(w.rhs.p, w.t1.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    trsv_lower(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, w.status.p);
-    trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, w.status.p);
+    unsigned *bar = (unsigned *)w.flags.p + 2;
+    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
+    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, true, w.status.p, bar, m->errflag.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
     if (mixed) {
@@ -350,8 +192,8 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
       for (int it = 0; it < std::max(1, m->opts.refine_iters); ++it) {
         refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
         GPGP_CHECK_LAUNCH();
-        trsv_lower(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, w.status.p);
-        trsv_lower_t(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, w.status.p);
+        trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
+        trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
         vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
         vec_mul(st, n, m->s.p, w.u.p, alpha);
         gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
@@ -422,7 +264,7 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
   w.logdet_part.alloc(st, (n + NB - 1) / NB + 1);
   w.tmpv.alloc(st, n);
   w.status.alloc(st, 1);
-  w.flags.alloc(st, 1);
+  w.flags.alloc(st, 4);  // [0] site flags, [2..3] grid barrier of the solves
   m->L.alloc(st, (size_t)n * n);
   m->Winv.alloc(st, (size_t)((n + NB - 1) / NB) * NB * NB);
   m->s.alloc(st, n);
@@ -619,8 +461,8 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
     return fail(ctx, GPGP_EUNSUPPORTED, "lik_betabinom is not implemented on the device");
   if (lik->kind == GPGP_LIK_BINOMIAL && !trials)
     return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial likelihood");
-  if (method->kind != GPGP_METHOD_FULL)
-    return fail(ctx, GPGP_EUNSUPPORTED, "method_fitc is not available in this build");
+  if (method->kind != GPGP_METHOD_FULL && method->kind != GPGP_METHOD_FITC)
+    return fail(ctx, GPGP_EINVAL, "unknown method");
   if (opts->precision != GPGP_PREC_FP64 && opts->precision != GPGP_PREC_MIXED)
     return fail(ctx, GPGP_EINVAL, "unknown precision");
   std::unique_ptr<gpgp_model> m(new gpgp_model());
@@ -651,7 +493,10 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   }
   m->F.alloc(s, (size_t)n * std::max(1, m->dk.nfeat));
   prep_features(s, m->dk, m->prep, m->x.p, n, n, m->F.p, n);
-  st = fit_full(m.get(), result);
+  if (method->kind == GPGP_METHOD_FITC)
+    st = fit_fitc(m.get(), result, method->inducing, on_device);
+  else
+    st = fit_full(m.get(), result);
   if (st != GPGP_OK) {
     GPGP_CUDA(cudaStreamSynchronize(s));
     return st;
@@ -919,6 +764,23 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       dmean.alloc(s, mt);
       mout = dmean.p;
     }
+    if (m->fitc) {
+      DBuf dv;
+      if (var) dv.alloc(s, mt);
+      {
+        Phase ph(ctx, GPGP_PHASE_PRED_VAR);
+        gpgp_status st2 = pred_fitc(m, Ft.p, mt, gm, mout, var ? dv.p : nullptr);
+        if (st2 != GPGP_OK) return st2;
+      }
+      if (var)
+        GPGP_CUDA(cudaMemcpyAsync(var, dv.p, mt * sizeof(double),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+      if (!on_device)
+        GPGP_CUDA(cudaMemcpyAsync(mean, mout, mt * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaStreamSynchronize(s));
+      if (tc_error(m)) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
+      return GPGP_OK;
+    }
     // mean = Kt alpha (R/gp_pred.R:209), fused: Kt is never stored
     {
       Phase ph(ctx, GPGP_PHASE_PRED_MEAN);
@@ -988,6 +850,13 @@ gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *lo
       if (!m->cav_mean.p) return fail(ctx, GPGP_ENOT_FITTED, "EP fit has no cavity moments");
       mp = m->cav_mean.p;
       vp = m->cav_var.p;
+    } else if (m->fitc) {
+      lmean.alloc(s, n);
+      lvar.alloc(s, n);
+      gpgp_status st2 = loo_fitc_posteriors(m, lmean.p, lvar.p);
+      if (st2 != GPGP_OK) return st2;
+      mp = lmean.p;
+      vp = lvar.p;
     } else {
       if (!m->have_binv_diag) compute_binv_diag(m);
       lmean.alloc(s, n);

@@ -128,41 +128,60 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
+// Factor: right-looking over the 64 columns; warp 0 takes the pivot (one
+// square root and one reciprocal) and scales the column, then all threads
+// apply the rank-1 update. Inverse W = L^-1 by forward substitution over the
+// rows, all columns at once with four threads per column (partial dot
+// products combined by shuffles); a column only depends on itself, so rows
+// advance with warp synchronisation alone. log L_jj are summed in a fixed
+// tree order.
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                                          double *__restrict__ Winv,
                                                          double *__restrict__ logdet_part,
                                                          int *__restrict__ status, int64_t k0) {
   __shared__ double S[NB][NB + 1];
   __shared__ double Wsm[NB][NB + 1];
+  __shared__ double rdiag[NB];
+  __shared__ double lg[NB];
   __shared__ int failed;
   if (*(volatile int *)status != 0) return;
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   for (int idx = tid; idx < NB * NB; idx += 256) {
     int r = idx % NB, c = idx / NB;
     S[r][c] = (r < kb && c < kb && r >= c) ? A[r + c * lda] : 0.0;
-    Wsm[r][c] = 0.0;
   }
   if (tid == 0) failed = 0;
   __syncthreads();
   for (int j = 0; j < kb; ++j) {
-    if (tid == 0) {
-      double d = S[j][j];
-      if (!(d > 0.0) || !isfinite(d)) {
-        failed = 1;
-        atomicCAS(status, 0, (int)(k0 + j + 1));
+    if (warp == 0) {
+      const double dj = S[j][j];
+      const bool bad = !(dj > 0.0) || !isfinite(dj);
+      if (bad) {
+        if (lane == 0) {
+          failed = 1;
+          atomicCAS(status, 0, (int)(k0 + j + 1));
+        }
       } else {
-        S[j][j] = sqrt(d);
+        const double piv = sqrt(dj);
+        const double rp = 1.0 / piv;
+        for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
+        if (lane == 0) {
+          S[j][j] = piv;
+          rdiag[j] = rp;
+        }
       }
     }
     __syncthreads();
     if (failed) return;
-    const double piv = S[j][j];
-    for (int r = j + 1 + tid; r < kb; r += 256) S[r][j] = S[r][j] / piv;
-    __syncthreads();
     const int m = kb - j - 1;
-    for (int idx = tid; idx < m * m; idx += 256) {
-      int r = j + 1 + idx % m, c = j + 1 + idx / m;
-      if (r >= c) S[r][c] -= S[r][j] * S[c][j];
+    if (m > 0) {
+      // pairs (r, c), j < c <= r < kb, as a 16 x 16 thread grid stepping over the block
+      const int tr = tid & 15, tc = tid >> 4;
+      for (int c = j + 1 + tc; c < kb; c += 16) {
+        const double lc = S[c][j];
+        for (int r = c + ((tr - (c - (j + 1)) % 16 + 16) % 16); r < kb; r += 16) S[r][c] -= S[r][j] * lc;
+      }
     }
     __syncthreads();
   }
@@ -171,51 +190,66 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
     int r = idx % kb, c = idx / kb;
     if (r >= c) A[r + c * lda] = S[r][c];
   }
-  // inverse of the lower factor, one column per thread (forward substitution)
-  if (tid < kb) {
-    const int c = tid;
-    Wsm[c][c] = 1.0 / S[c][c];
-    for (int r = c + 1; r < kb; ++r) {
-      double sum = 0.0;
-      for (int k = c; k < r; ++k) sum = fma(S[r][k], Wsm[k][c], sum);
-      Wsm[r][c] = -sum / S[r][r];
+  // inverse: column c = tid / 4, part p = tid % 4
+  {
+    const int c = tid >> 2, p = tid & 3;
+    for (int r = 0; r < NB; ++r) {
+      double part = 0.0;
+      if (c < r && r < kb)
+        for (int k = c + p; k < r; k += 4) part = fma(S[r][k], Wsm[k][c], part);
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      if (p == 0) {
+        double w = 0.0;
+        if (r < kb && c < kb) w = (r == c) ? rdiag[r] : (c < r ? -part * rdiag[r] : 0.0);
+        Wsm[r][c] = w;
+      }
+      __syncwarp();
     }
   }
+  if (tid < NB) lg[tid] = tid < kb ? log(S[tid][tid]) : 0.0;
   __syncthreads();
   for (int idx = tid; idx < NB * NB; idx += 256) {
     int r = idx % NB, c = idx / NB;
     Winv[r + c * NB] = Wsm[r][c];
   }
-  if (tid == 0) {
-    double ls = 0.0;
-    for (int j = 0; j < kb; ++j) ls += log(S[j][j]);
-    *logdet_part = ls;
+  for (int st = NB / 2; st > 0; st >>= 1) {
+    if (tid < st) lg[tid] += lg[tid + st];
+    __syncthreads();
   }
+  if (tid == 0) *logdet_part = lg[0];
 }
 
-// panel: L21 = A21 * W^T for 64 rows per CTA (in place)
-__global__ void __launch_bounds__(256) potrf_panel_kernel(double *__restrict__ A21, int64_t m, int kb,
-                                                          int64_t lda, const double *__restrict__ W,
+// panel: L21 = A21 L11^-T by forward substitution, one row per thread (in place).
+// Substitution keeps the factorisation backward stable when a diagonal block is
+// ill-conditioned (FITC's K_z); the inverse W is used by the solves instead.
+__global__ void __launch_bounds__(128) potrf_panel_kernel(double *__restrict__ A21, int64_t m, int kb,
+                                                          int64_t lda, const double *__restrict__ L11,
                                                           const int *__restrict__ status) {
-  __shared__ double P[NB][NB + 1];
-  __shared__ double Ws[NB][NB + 1];
+  __shared__ double Ls[NB][NB + 1];
+  __shared__ double rd[NB];
   if (*(volatile const int *)status != 0) return;
-  const int64_t r0 = (int64_t)blockIdx.x * NB;
-  const int tid = threadIdx.x;
-  for (int idx = tid; idx < NB * NB; idx += 256) {
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     int r = idx % NB, c = idx / NB;
-    P[r][c] = (r0 + r < m && c < kb) ? A21[(r0 + r) + c * lda] : 0.0;
-    Ws[r][c] = W[r + c * NB];
+    Ls[r][c] = (r < kb && c < kb && r >= c) ? L11[r + c * lda] : 0.0;
   }
   __syncthreads();
-  for (int idx = tid; idx < NB * NB; idx += 256) {
-    int r = idx % NB, c = idx / NB;
-    if (r0 + r < m && c < kb) {
-      double sum = 0.0;
-      for (int k = 0; k <= c; ++k) sum = fma(P[r][k], Ws[c][k], sum);
-      A21[(r0 + r) + c * lda] = sum;
+  if (threadIdx.x < kb) rd[threadIdx.x] = 1.0 / Ls[threadIdx.x][threadIdx.x];
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  double x[NB];
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    if (c < kb) {
+      double s = A21[r + c * lda];
+      for (int k = 0; k < c; ++k) s = fma(-x[k], Ls[c][k], s);
+      x[c] = s * rd[c];
     }
   }
+#pragma unroll
+  for (int c = 0; c < NB; ++c)
+    if (c < kb) A21[r + c * lda] = x[c];
 }
 
 void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
@@ -229,7 +263,7 @@ void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, doub
     const int64_t m = n - k0 - kb;
     if (m > 0) {
       double *A21 = A + (k0 + kb) + k0 * lda;
-      potrf_panel_kernel<<<(unsigned)((m + NB - 1) / NB), 256, 0, s>>>(A21, m, kb, lda, W, status);
+      potrf_panel_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(A21, m, kb, lda, Akk, status);
       GPGP_CHECK_LAUNCH();
       double *A22 = A + (k0 + kb) + (k0 + kb) * lda;
       gemm64(s, false, true, m, m, kb, -1.0, A21, lda, A21, lda, 1.0, A22, lda, true, 0);
@@ -319,6 +353,174 @@ void trsv_lower_t(cudaStream_t s, const double *L, int64_t n, int64_t lda, const
     trsv_bwd_step<<<g, 256, 0, s>>>(L, lda, Winv + blk * NB * NB, k0, kb, b, x, status);
     GPGP_CHECK_LAUNCH();
   }
+}
+
+// ---------------------------------------------------------------------------
+// single-launch triangular solves: a cooperative grid walks the diagonal blocks
+// and meets at a bounded grid barrier after every block
+// ---------------------------------------------------------------------------
+// bar[0] = arrival count, bar[1] = generation; both zero at launch. Returns
+// false (and sets *err) when the wait runs out; every block then leaves.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *err) {
+  __shared__ int ok_sh;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok_sh = 1;
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned it = 0;
+      while (*gen == g) {
+        if (++it > (1u << 26)) {
+          atomicExch(err, 3);
+          ok_sh = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok_sh != 0;
+}
+
+__global__ void __launch_bounds__(256) trsv_coop_kernel(const double *__restrict__ L, int64_t n,
+                                                        int64_t lda, const double *__restrict__ Winv,
+                                                        double *b, double *x, int trans,
+                                                        const int *__restrict__ status,
+                                                        unsigned *bar, int *err) {
+  __shared__ double bk[NB];
+  __shared__ double xk[NB];
+  if (*(volatile const int *)status != 0) return;
+  const int tid = threadIdx.x;
+  const int64_t nblk = (n + NB - 1) / NB;
+  const unsigned G = gridDim.x;
+  for (int64_t step = 0; step < nblk; ++step) {
+    const int64_t blk = trans ? nblk - 1 - step : step;
+    const int64_t k0 = blk * NB;
+    const int kb = (int)((n - k0) < NB ? (n - k0) : NB);
+    const double *W = Winv + blk * NB * NB;
+    if (tid < NB) bk[tid] = tid < kb ? __ldcg(b + k0 + tid) : 0.0;
+    __syncthreads();
+    if (tid < NB) {
+      double s = 0.0;
+      if (!trans) {
+        for (int c = 0; c <= tid && c < kb; ++c) s = fma(W[tid + c * NB], bk[c], s);
+      } else {
+        for (int r = tid; r < kb; ++r) s = fma(W[r + tid * NB], bk[r], s);
+      }
+      xk[tid] = tid < kb ? s : 0.0;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid < kb) x[k0 + tid] = xk[tid];
+    if (!trans) {
+      // b[r] -= L[r, k0:k0+kb] xk for rows below the block
+      for (int64_t r = k0 + kb + (int64_t)blockIdx.x * 256 + tid; r < n; r += (int64_t)G * 256) {
+        double s = 0.0;
+        for (int c = 0; c < kb; ++c) s = fma(L[r + (k0 + c) * lda], xk[c], s);
+        b[r] = __ldcg(b + r) - s;
+      }
+    } else {
+      // b[c] -= sum_r L[r, c] xk[r] for columns left of the block, one warp per column
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int64_t c = (int64_t)blockIdx.x * 8 + warp; c < k0; c += (int64_t)G * 8) {
+        double s = 0.0;
+        for (int r = lane; r < kb; r += 32) s = fma(L[(k0 + r) + c * lda], xk[r], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) b[c] = __ldcg(b + c) - s;
+      }
+    }
+    if (!grid_barrier(bar, G, err)) return;
+  }
+}
+
+static int g_coop_blocks = 0;
+
+void trsv_coop(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+               double *b, double *x, bool trans, const int *status, unsigned *bar, int *err) {
+  if (n <= 0) return;
+  if (g_coop_blocks == 0) {
+    int dev = 0, sms = 0, per = 0;
+    GPGP_CUDA(cudaGetDevice(&dev));
+    GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GPGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop_kernel, 256, 0));
+    g_coop_blocks = sms * std::max(1, std::min(per, 2));
+  }
+  GPGP_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+  int tr = trans ? 1 : 0;
+  void *args[] = {(void *)&L, (void *)&n, (void *)&lda, (void *)&Winv, (void *)&b, (void *)&x,
+                  (void *)&tr, (void *)&status, (void *)&bar, (void *)&err};
+  GPGP_CUDA(cudaLaunchCooperativeKernel((const void *)trsv_coop_kernel, dim3(g_coop_blocks), dim3(256),
+                                        args, 0, s));
+  GPGP_LAUNCHED();
+}
+
+// ---------------------------------------------------------------------------
+// substitution solves for small factors (M x M lower L), as R's forwardsolve /
+// backsolve do: rows of a column-major n x M matrix, one thread per row
+// ---------------------------------------------------------------------------
+// mode 0: X = B L^-T (x L^T = b, forward); mode 1: X = B L^-1 (x L = b, backward).
+// X may alias B.
+__global__ void tri_rows_kernel(const double *__restrict__ L, int64_t M, int64_t ldl, const double *B,
+                                int64_t ldb, double *X, int64_t ldx, int64_t n, int mode) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (mode == 0) {
+    for (int64_t c = 0; c < M; ++c) {
+      double s = B[i + c * ldb];
+      for (int64_t k = 0; k < c; ++k) s = fma(-X[i + k * ldx], L[c + k * ldl], s);
+      X[i + c * ldx] = s / L[c + c * ldl];
+    }
+  } else {
+    for (int64_t c = M - 1; c >= 0; --c) {
+      double s = B[i + c * ldb];
+      for (int64_t k = c + 1; k < M; ++k) s = fma(-X[i + k * ldx], L[k + c * ldl], s);
+      X[i + c * ldx] = s / L[c + c * ldl];
+    }
+  }
+}
+
+void tri_rows(cudaStream_t s, const double *L, int64_t M, int64_t ldl, const double *B, int64_t ldb,
+              double *X, int64_t ldx, int64_t n, int mode) {
+  if (n <= 0 || M <= 0) return;
+  tri_rows_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(L, M, ldl, B, ldb, X, ldx, n, mode);
+  GPGP_CHECK_LAUNCH();
+}
+
+// one warp: x = L^-1 b (trans = 0) or x = L^-T b (trans = 1), x may alias b
+__global__ void tri_vec_kernel(const double *__restrict__ L, int64_t M, int64_t ldl, const double *b,
+                               double *x, int trans) {
+  const int lane = threadIdx.x & 31;
+  if (!trans) {
+    for (int64_t r = 0; r < M; ++r) {
+      double s = 0.0;
+      for (int64_t k = lane; k < r; k += 32) s = fma(L[r + k * ldl], x[k], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) x[r] = (b[r] - s) / L[r + r * ldl];
+      __syncwarp();
+    }
+  } else {
+    for (int64_t r = M - 1; r >= 0; --r) {
+      double s = 0.0;
+      for (int64_t k = r + 1 + lane; k < M; k += 32) s = fma(L[k + r * ldl], x[k], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) x[r] = (b[r] - s) / L[r + r * ldl];
+      __syncwarp();
+    }
+  }
+}
+
+void tri_vec(cudaStream_t s, const double *L, int64_t M, int64_t ldl, const double *b, double *x,
+             bool trans) {
+  if (M <= 0) return;
+  tri_vec_kernel<<<1, 32, 0, s>>>(L, M, ldl, b, x, trans ? 1 : 0);
+  GPGP_CHECK_LAUNCH();
 }
 
 // ---------------------------------------------------------------------------

@@ -5,10 +5,10 @@
 // in [0.5, 1) and then cut into four 8-bit fixed-point slices
 //   x = 2^e * sum_t q_t 2^-8(t+1),  q_t integers in [-256, 256]
 // which BF16 holds exactly. A product of two slices is an integer below 2^16,
-// so a 64-long dot product of slice pairs (four pairs per level at most) stays
-// below 2^24 and the FP32 accumulators of tcgen05.mma hold it exactly. The 13
-// slice pairs with t + u <= 4 go into five level accumulators in TMEM; after
-// every 64-wide K chunk the levels are added into double-float (hi, lo) FP32
+// so the level-0 and level-1 dot products of up to 256 terms stay below 2^24
+// and the FP32 accumulators of tcgen05.mma hold them exactly. The 13 slice
+// pairs with t + u <= 4 go into five level accumulators in TMEM; after every
+// 256-wide K group the levels are added into double-float (hi, lo) FP32
 // registers, and the result is written once in FP64:
 //   (A B^T)_ij = 2^(e_i + f_j - 16) sum_l 2^-8l P_l.
 // The truncation error is ~2^-33 of the row maxima, far below what the FP64
@@ -32,6 +32,10 @@ namespace gpgp {
 constexpr int OZ_S = 4;             // slices per operand
 constexpr int OZ_LEVELS = 5;        // levels kept (t + u <= 4): 13 products
 constexpr int OZ_TK = 64;           // K chunk
+// Chunks accumulated in TMEM before a flush: level-0 and level-1 sums stay below
+// 2^24 (exact in FP32) for 4 x 64 = 256 products; deeper levels may round, but
+// their rounding is below 2^-40 of the result.
+constexpr int OZ_GROUP = 4;
 constexpr int OZ_TR = 64;           // rows per slice tile
 constexpr int OZ_TILE = OZ_TR * OZ_TK;  // bf16 elements per slice tile (8 KB)
 constexpr int OZ_BM = 128, OZ_BN = 64;
@@ -58,26 +62,64 @@ __device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans
   return trans ? P[k + r * ld] : P[r + k * ld];
 }
 
+// Row exponents and slices are computed from the FP64 bit patterns with
+// integer instructions only (the FP64 pipe of this part is slow).
+
 __global__ void oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
                                  int64_t K, int64_t rows_pad, int *__restrict__ ex) {
-  // one warp per row: coalesced when trans (row contiguous), strided otherwise
+  // one warp per row: the largest |P| by an unsigned compare of the sign-cleared bits
   const int lane = threadIdx.x & 31;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= rows_pad) return;
-  double m = 0.0;
+  unsigned long long mx = 0ull;
   if (r < rows)
-    for (int64_t k = lane; k < K; k += 32) m = fmax(m, fabs(trans ? P[k + r * ld] : P[r + k * ld]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    for (int64_t k = lane; k < K; k += 32) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(trans ? P[k + r * ld] : P[r + k * ld]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
   if (lane == 0) {
-    int e = 0;
-    if (m > 0.0 && isfinite(m)) frexp(m, &e);
-    ex[r] = e;
+    // frexp exponent of the row maximum: max = 0.1m x 2^e; zero, subnormal or non-finite rows -> 0
+    const int E = (int)(mx >> 52);
+    ex[r] = (E == 0 || E == 2047) ? 0 : E - 1022;
   }
 }
 
-__device__ __forceinline__ uint32_t bf16_bits_of_int(double q) {
-  // q is an integer with |q| <= 256: exact in FP32 and in BF16 (upper 16 bits)
-  return __float_as_uint((float)q) >> 16;
+// bf16 bits of the integer s * q, |q| <= 256
+__device__ __forceinline__ uint32_t bf16_of_digit(int q) {
+  if (q == 0) return 0u;
+  const uint32_t sgn = q < 0 ? 0x8000u : 0u;
+  const uint32_t a = (uint32_t)(q < 0 ? -q : q);
+  const int p = 31 - __clz(a);
+  const uint32_t mant = p <= 7 ? ((a << (7 - p)) & 0x7Fu) : ((a >> (p - 7)) & 0x7Fu);
+  return sgn | ((uint32_t)(127 + p) << 7) | mant;
+}
+
+// 32-bit fixed-point |x| 2^32 (rounded to nearest) of x = P 2^-e, as balanced
+// base-256 digits d0..d3 (|d0| <= 256, |d1..d3| <= 128) carrying the sign of P
+__device__ __forceinline__ void oz_digits(double v, int e, int d[4]) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((b >> 52) & 0x7FF);
+  unsigned long long X = 0ull;
+  if (E != 0 && E != 2047) {
+    const unsigned long long mnt = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int rsh = 1043 + e - E;  // >= 21 because |v| < 2^e
+    if (rsh < 64) X = (mnt + (1ull << (rsh - 1))) >> rsh;
+  }
+  int u3 = (int)(X & 255ull), u2 = (int)((X >> 8) & 255ull), u1 = (int)((X >> 16) & 255ull);
+  int u0 = (int)(X >> 24);
+  if (u3 >= 128) { u3 -= 256; u2 += 1; }
+  if (u2 >= 128) { u2 -= 256; u1 += 1; }
+  if (u1 >= 128) { u1 -= 256; u0 += 1; }
+  const int s = (b >> 63) ? -1 : 1;
+  d[0] = s * u0;
+  d[1] = s * u1;
+  d[2] = s * u2;
+  d[3] = s * u3;
 }
 
 __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
@@ -95,21 +137,11 @@ __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int tr
   uint32_t packed[OZ_S][4];
 #pragma unroll
   for (int j = 0; j < 8; j += 2) {
-    double q[2][OZ_S];
+    int d0[4], d1[4];
+    oz_digits(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
+    oz_digits(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      double x = ldexp(oz_elem(P, ld, trans, r, k0 + j + h, rows, K), -e);
-#pragma unroll
-      for (int t = 0; t < OZ_S; ++t) {
-        x = x * 256.0;
-        const double qt = rint(x);
-        x = x - qt;
-        q[h][t] = qt;
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < OZ_S; ++t)
-      packed[t][j / 2] = bf16_bits_of_int(q[0][t]) | (bf16_bits_of_int(q[1][t]) << 16);
+    for (int t = 0; t < OZ_S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t]) | (bf16_of_digit(d1[t]) << 16);
   }
   const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
   const int64_t kb = k0 / OZ_TK, kk = k0 % OZ_TK;
@@ -248,6 +280,20 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// (double)f * 2^sh, exact, by moving the float's fields into a double: the
+// float exponent is rebiased and sh added; zero and out-of-range cases take ldexp
+__device__ __forceinline__ double f2d_scaled(float f, int sh) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t ef = (b >> 23) & 0xFFu;
+  if (ef == 0u || ef == 0xFFu) return ldexp((double)f, sh);
+  const int ed = (int)ef - 127 + 1023 + sh;
+  if (ed <= 0 || ed >= 2047) return ldexp((double)f, sh);
+  const unsigned long long db = ((unsigned long long)(b >> 31) << 63) |
+                                ((unsigned long long)ed << 52) |
+                                ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)db);
+}
+
 // double-float accumulation of v into (hi, lo) with an error-free TwoSum
 __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
   const float s = __fadd_rn(hi, v);
@@ -310,11 +356,17 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   uint64_t *bars = (uint64_t *)(smem + 2 * OZ_STAGE);
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
-  const uint32_t full0 = smem_u32(&bars[0]), full1 = smem_u32(&bars[1]), done = smem_u32(&bars[2]);
+  // full[s]: operands of the chunk in stage s landed; empty[s]: the MMAs that read
+  // stage s completed; flush: the MMAs of a flush group completed
+  const uint32_t full0 = smem_u32(&bars[0]), full1 = smem_u32(&bars[1]);
+  const uint32_t empty0 = smem_u32(&bars[2]), empty1 = smem_u32(&bars[3]);
+  const uint32_t flushb = smem_u32(&bars[4]);
   if (tid == 0) {
     mbar_init(full0, 1);
     mbar_init(full1, 1);
-    mbar_init(done, 1);
+    mbar_init(empty0, 1);
+    mbar_init(empty1, 1);
+    mbar_init(flushb, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_sh = 0;
   }
@@ -346,10 +398,7 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
     }
   };
 
-  if (tid == 0) {
-    if (nch > 0) load_stage(0, kc0);
-    if (nch > 1) load_stage(1, kc0 + 1);
-  }
+  if (tid == 0 && nch > 0) load_stage(0, kc0);
 
   // instruction descriptor: D F32, A/B BF16, K-major both, N = 64, M = 128
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
@@ -365,18 +414,20 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0.f;
 
   bool ok = true;
+  int nflush = 0;
   for (int64_t c = 0; c < nch; ++c) {
     const int st = (int)(c & 1);
-    const uint32_t parity = (uint32_t)((c >> 1) & 1);
+    const bool group_start = (c % OZ_GROUP) == 0;
+    const bool flush = ((c + 1) % OZ_GROUP) == 0 || c == nch - 1;
     if (tid == 0) {
-      if (!mbar_wait_bounded(st ? full1 : full0, parity)) {
-        atomicExch(g.err, 1);
-        abort_sh = 1;
-      } else {
+      bool good = mbar_wait_bounded(st ? full1 : full0, (uint32_t)((c >> 1) & 1));
+      if (good) {
         tc_fence_after();
         const uint32_t abase = smem_u32(smem + st * OZ_STAGE);
         const uint32_t bbase = abase + OZ_A_STAGE;
-        int first[OZ_LEVELS] = {1, 1, 1, 1, 1};
+        int first[OZ_LEVELS];
+#pragma unroll
+        for (int l = 0; l < OZ_LEVELS; ++l) first[l] = group_start ? 1 : 0;
 #pragma unroll
         for (int t = 0; t < OZ_S; ++t) {
 #pragma unroll
@@ -392,41 +443,60 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
             }
           }
         }
-        umma_commit(done);
+        umma_commit(st ? empty1 : empty0);
+        if (flush) umma_commit(flushb);
+        // refill the other stage with chunk c + 1 once the MMAs of chunk c - 1 are done
+        if (c + 1 < nch) {
+          if (c >= 1) good = mbar_wait_bounded(st ? empty0 : empty1, (uint32_t)(((c - 1) >> 1) & 1));
+          if (good) load_stage(st ^ 1, kc0 + c + 1);
+        }
+      }
+      if (!good) {
+        atomicExch(g.err, 1);
+        abort_sh = 1;
       }
     }
-    __syncthreads();
-    if (abort_sh) {
-      ok = false;
-      break;
-    }
-    const bool waited = mbar_wait_bounded(done, (uint32_t)(c & 1));
-    if (__syncthreads_or(!waited)) {
-      if (tid == 0) atomicExch(g.err, 2);
-      ok = false;
-      break;
-    }
-    tc_fence_after();
-    // stage st is free again: prefetch chunk c + 2
-    if (tid == 0 && c + 2 < nch) load_stage(st, kc0 + c + 2);
+    if (flush) {
+      __syncthreads();
+      if (abort_sh) {
+        ok = false;
+        break;
+      }
+      const bool waited = mbar_wait_bounded(flushb, (uint32_t)(nflush & 1));
+      if (__syncthreads_or(!waited)) {
+        if (tid == 0) atomicExch(g.err, 2);
+        ok = false;
+        break;
+      }
+      ++nflush;
+      tc_fence_after();
 #pragma unroll 1
-    for (int lev = 0; lev < OZ_LEVELS; ++lev) {
-      uint32_t r[32];
-      tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + lev * OZ_BN + half * 32, r);
-      tmem_ld_wait();
-      const float sc = __uint_as_float((uint32_t)(127 - 8 * lev) << 23);  // 2^-8lev
+      for (int lev = 0; lev < OZ_LEVELS; ++lev) {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + lev * OZ_BN + half * 32, r);
+        tmem_ld_wait();
+        const float sc = __uint_as_float((uint32_t)(127 - 8 * lev) << 23);  // 2^-8lev
 #pragma unroll
-      for (int j = 0; j < 32; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+        for (int j = 0; j < 32; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+      }
+      tc_fence_before();
+      __syncthreads();
+    } else if (c % 8 == 7) {
+      // keep abort visible between flushes without a barrier per chunk
+      __syncthreads();
+      if (abort_sh) {
+        ok = false;
+        break;
+      }
     }
-    tc_fence_before();
-    __syncthreads();
   }
   __syncthreads();
   if (!ok && tid == 0) {
     // a wait ran out: give in-flight MMAs and bulk copies a bounded chance to land
     // before the shared memory and TMEM are released
-    mbar_wait_bounded(done, 0);
-    mbar_wait_bounded(done, 1);
+    mbar_wait_bounded(flushb, (uint32_t)(nflush & 1));
+    mbar_wait_bounded(empty0, 0);
+    mbar_wait_bounded(empty1, 0);
     mbar_wait_bounded(full0, 0);
     mbar_wait_bounded(full1, 0);
   }
@@ -436,18 +506,25 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
   }
   if (!ok) return;
-  // FP64 epilogue: C = alpha * 2^(e_i + f_j - 16) (hi + lo) + beta * C
+  // FP64 epilogue: C = alpha * 2^(e_i + f_j - 16) (hi + lo) + beta * C, with the
+  // float -> double conversion and the power of two done on the bit patterns
   if (my_row < g.M) {
     const int ea = g.a_ex[g.a_rb0 * OZ_TR + my_row];
-#pragma unroll 4
+    const bool unit = (g.alpha == 1.0 || g.alpha == -1.0) && (g.beta == 0.0 || g.beta == 1.0);
+#pragma unroll
     for (int j = 0; j < 32; ++j) {
       const int64_t col = col0 + half * 32 + j;
-      if (col >= g.N) break;
-      if (g.lower_only && my_row < col) continue;
-      const int eb = g.b_ex[g.b_rb0 * OZ_TR + col];
-      const double v = ldexp((double)hi[j] + (double)lo[j], ea + eb - 16);
-      double *dst = g.C + my_row + col * g.ldc;
-      *dst = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * *dst);
+      if (col < g.N && !(g.lower_only && my_row < col)) {
+        const int sh = ea + g.b_ex[g.b_rb0 * OZ_TR + col] - 16;
+        double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
+        double *dst = g.C + my_row + col * g.ldc;
+        if (unit) {
+          if (g.alpha < 0.0) v = -v;
+          *dst = (g.beta == 0.0) ? v : *dst + v;
+        } else {
+          *dst = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * *dst);
+        }
+      }
     }
   }
 }

@@ -1,0 +1,206 @@
+// Context and model objects shared by the orchestration files (api.cu, fitc.cu).
+#pragma once
+#include <math.h>
+
+#include <memory>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "common.cuh"
+
+struct gpgp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  double *h_pinned = nullptr;  // host pinned scalars
+  // live profiling: (phase, start event, stop event) per recorded interval
+  bool prof = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
+  double prof_ms[GPGP_NPHASE] = {0};
+  int64_t prof_calls[GPGP_NPHASE] = {0};
+};
+
+namespace gpgp {
+
+// Scoped phase timer: records a pair of events on the context stream when enabled.
+struct Phase {
+  gpgp_ctx *c;
+  int ph;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Phase(gpgp_ctx *ctx, int phase) : c(ctx), ph(phase) {
+    if (!c->prof) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, c->stream);
+  }
+  ~Phase() {
+    if (!c->prof || !a) return;
+    cudaEventRecord(b, c->stream);
+    c->prof_ev.push_back({ph, {a, b}});
+  }
+};
+
+inline void prof_collect(gpgp_ctx *c) {
+  for (auto &e : c->prof_ev) {
+    float ms = 0.f;
+    cudaEventSynchronize(e.second.second);
+    cudaEventElapsedTime(&ms, e.second.first, e.second.second);
+    c->prof_ms[e.first] += ms;
+    c->prof_calls[e.first] += 1;
+    cudaEventDestroy(e.second.first);
+    cudaEventDestroy(e.second.second);
+  }
+  c->prof_ev.clear();
+}
+
+// RAII device buffer on the context's stream-ordered pool.
+struct DBuf {
+  double *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { reset(); }
+  void alloc(cudaStream_t st, size_t count) {
+    reset();
+    s = st;
+    n = count;
+    if (count == 0) return;
+    cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(double), st);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+  }
+  void reset() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct IBuf {
+  int *p = nullptr;
+  cudaStream_t s = nullptr;
+  IBuf() = default;
+  IBuf(const IBuf &) = delete;
+  IBuf &operator=(const IBuf &) = delete;
+  ~IBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  void alloc(cudaStream_t st, size_t count) {
+    if (p) cudaFreeAsync(p, s);
+    s = st;
+    if (cudaMallocAsync((void **)&p, count * sizeof(int), st) != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+  }
+};
+
+// Resident quantities of a FITC fit (R/gp_fit.R:101-123, R/linear_algebra.R:3-43).
+struct FitcState {
+  int64_t M = 0;
+  DBuf z, Fz;           // inducing inputs (M x d) and their features
+  DBuf Kz, Lz, Wz_blk;  // K(z,z) + jitter I, its factor, diagonal-block inverses
+  DBuf Kxz;             // K(x, z), n x M
+  DBuf X;               // Kxz Lz^-T = t(forwardsolve(Kz_chol, t(Kxz))), n x M
+  DBuf D, Kdiag;        // FITC diagonal (with jitter) and diag K(x, x)
+  DBuf S, iDU;          // S = D + V, inv_D_U = Kxz / S (n x M)
+  DBuf Cm, Lm, Wm_blk;  // K_z + U^T S^-1 U and its factor
+  double logdet = 0.0;  // log det of the lemma's matrix (R/linear_algebra.R:30-34)
+  // prediction caches (independent of the test points), filled on first use:
+  // Sig1 holds sol = A1 S^-1 A1^T - P C_m^-1 P^T, P = A1 inv_D_U
+  DBuf Sig1, P;
+  bool have_pred_cache = false;
+};
+
+}  // namespace gpgp
+
+struct gpgp_model {
+  gpgp_ctx *ctx = nullptr;
+  gpgp_kernel spec;
+  gpgp::DevKernel dk;
+  std::vector<gpgp::HostTermPrep> prep;
+  gpgp_lik lik;
+  gpgp::LikDev lk;
+  gpgp_method method;
+  gpgp_approx approx;
+  gpgp_fit_opts opts;
+  int64_t n = 0;
+  int d = 0;
+  // inputs (owned copies)
+  gpgp::DBuf x, y, trials, offset, F;
+  // full-method fit
+  gpgp::DBuf L, Winv, s, alpha, fmean, z, V;
+  gpgp::DBuf fvar, cav_mean, cav_var;  // EP
+  gpgp::DBuf binv_diag;                // diag(B^-1), filled on demand
+  bool have_binv_diag = false;
+  gpgp::DBuf Linv;                     // W = L^-1, kept resident once computed
+  bool have_Linv = false;
+  gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
+  std::unique_ptr<gpgp::FitcState> fitc;
+  bool has_trials = false, has_offset = false;
+  double log_evidence = 0.0;
+  int fitted = 0;
+};
+
+namespace gpgp {
+
+extern thread_local std::string tl_error;
+
+inline gpgp_status fail(gpgp_ctx *ctx, gpgp_status st, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  tl_error = msg;
+  return st;
+}
+
+template <class F>
+gpgp_status guarded(gpgp_ctx *ctx, F &&fn) {
+  try {
+    return fn();
+  } catch (const CudaError &e) {
+    std::string m = std::string("CUDA error ") + cudaGetErrorString(e.err) + " in " + e.what;
+    return fail(ctx, GPGP_ECUDA, m);
+  } catch (const std::bad_alloc &) {
+    return fail(ctx, GPGP_EOOM, "device or host allocation failed");
+  }
+}
+
+inline LikDev make_likdev(const gpgp_lik &l) {
+  LikDev d;
+  d.kind = l.kind;
+  d.link = l.link;
+  d.sigma = l.sigma;
+  d.phi = l.phi;
+  return d;
+}
+
+inline void copy_in(cudaStream_t s, DBuf &dst, const double *src, size_t count, bool src_on_device) {
+  dst.alloc(s, count);
+  if (count == 0) return;
+  GPGP_CUDA(cudaMemcpyAsync(dst.p, src, count * sizeof(double),
+                            src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+}
+
+inline double read_scalar(gpgp_ctx *ctx, const double *dptr) {
+  GPGP_CUDA(cudaMemcpyAsync(ctx->h_pinned, dptr, sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  GPGP_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ctx->h_pinned[0];
+}
+
+inline unsigned g1(int64_t n) { return (unsigned)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
+
+// FITC orchestration (fitc.cu)
+gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing, bool on_device);
+gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double *mean,
+                      double *var);
+gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar);
+
+}  // namespace gpgp

@@ -238,3 +238,67 @@ def test_energy_gradient_matches_finite_differences():
                 R.gp_fit(og, x, y)
                 fd[i] += sgn * R.gp_energy(og) / (2 * h)
         assert close(g, fd, 1e-5, 1e-6), (cfs, g, fd)
+
+
+FITC_LIKS = [("gaussian", "laplace"), ("poisson", "laplace"), ("bernoulli", "laplace"),
+             ("bernoulli", "ep"), ("poisson", "ep")]
+
+
+def relmax(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("lik,approx", FITC_LIKS)
+def test_fitc_matches_oracle(lik, approx):
+    """method_fitc with given inducing points (R/gp_fit.R:101-188): evidence, posterior mean,
+    prediction and LOO against the restatement (test_sparse.R / test_loo.R shapes).
+
+    Vectors are compared in the max norm relative to their largest entry (1e-9): FITC's
+    solves with K_z (condition ~3e4 here) and the lemma's cancellation z/S - iDU C^-1 iDU^T z
+    make single entries sensitive at ~1e-8 to one-ulp input changes (measured on the oracle
+    itself), so per-entry 1e-10 would test rounding noise, not the algorithm."""
+    rng = np.random.default_rng(7)
+    n, M = 300, 24
+    x = rng.uniform(-3, 3, (n, 2))
+    xt = rng.uniform(-3, 3, (41, 2))
+    z = rng.uniform(-3, 3, (M, 2))
+    f = np.sin(x[:, 0]) + 0.5 * x[:, 1]
+    if lik == "gaussian":
+        y = f + 0.2 * rng.standard_normal(n)
+        lk = G.lik_gaussian(sigma=0.2)
+    elif lik == "poisson":
+        y = rng.poisson(np.exp(f)).astype(float)
+        lk = G.lik_poisson()
+    else:
+        y = (rng.uniform(size=n) < 1 / (1 + np.exp(-2 * f))).astype(float)
+        lk = G.lik_bernoulli()
+    ap = G.approx_laplace() if approx == "laplace" else G.approx_ep()
+    gp = G.gp_init([G.cf_sexp(lscale=1.2, magn=1.0), G.cf_const(0.5)], lk, method=G.method_fitc(inducing=z),
+                   approx=ap)
+    og = oracle_gp(gp)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        gp = G.gp_fit(gp, x, y)
+        og = R.gp_fit(og, x, y)
+    assert gp.fit["iters"] == og.fit["iters"]
+    assert rel_err(gp.fit["log_evidence"], og.fit["log_evidence"]) < 1e-10
+    assert relmax(G.model_field(gp, "fmean"), og.fit["fmean"]) < 1e-9
+    p, po = G.gp_pred(gp, xt, var=True), R.gp_pred(og, xt, var=True)
+    assert relmax(p["mean"], po["mean"]) < 1e-9
+    assert relmax(p["var"], po["var"]) < 1e-9
+    loo, lo = G.gp_loo(gp, x, y), R.gp_loo(og, x, y)
+    assert relmax(loo["loos"], lo["loos"]) < 1e-9
+
+
+def test_fitc_method_full_agreement_at_full_inducing():
+    """With every training input as an inducing point FITC's D vanishes (up to jitter) and
+    its evidence approaches method_full's: a size-independent property of the lemma path."""
+    rng = np.random.default_rng(11)
+    n = 120
+    x = rng.uniform(-2, 2, (n, 1))
+    y = np.sin(2 * x[:, 0]) + 0.1 * rng.standard_normal(n)
+    g1 = G.gp_fit(G.gp_init(G.cf_sexp(lscale=0.8), G.lik_gaussian(sigma=0.3)), x, y)
+    g2 = G.gp_fit(G.gp_init(G.cf_sexp(lscale=0.8), G.lik_gaussian(sigma=0.3), method=G.method_fitc(inducing=x)),
+                  x, y)
+    assert abs(g1.fit["log_evidence"] - g2.fit["log_evidence"]) < 1e-3 * abs(g1.fit["log_evidence"])
