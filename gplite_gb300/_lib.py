@@ -64,6 +64,12 @@ class FitResult(C.Structure):
                 ("info", C.c_int64), ("quad_ok", C.c_int32), ("converged", C.c_int32)]
 
 
+class BatchProblem(C.Structure):
+    _fields_ = [("n", C.c_int32), ("d", C.c_int32), ("m", C.c_int32), ("kind", C.c_int32),
+                ("lscale", C.c_double), ("magn", C.c_double), ("sigma", C.c_double),
+                ("x", C.c_void_p), ("y", C.c_void_p), ("xt", C.c_void_p)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 
@@ -95,6 +101,12 @@ SIGNATURES = {
     "gpgp_pred": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_pred_dev": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_loo": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "gpgp_batch_create": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.POINTER(_P)]),
+    "gpgp_batch_upload": (C.c_int, [_P, _P]),
+    "gpgp_batch_run": (C.c_int, [_P]),
+    "gpgp_batch_results": (C.c_int, [_P, _P, _P, _P, _P]),
+    "gpgp_batch_info": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "gpgp_batch_destroy": (C.c_int, [_P]),
     "gpgp_mixed_selftest": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P]),
     "gpgp_fit_gaussian_noalloc": (C.c_int, [_P, C.POINTER(Kernel), C.c_double, C.c_double, _P, C.c_int64,
                                             C.c_int32, _P, _P, _P]),

@@ -119,6 +119,15 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
             const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
             int64_t ldc, bool lower_only = false, int tri_mode = 0);
 
+// Batched FP64 GEMM: problem z uses A + z sA, B + z sB, C + z sC.
+void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+                    const double *A, int64_t lda, int64_t sA, const double *B, int64_t ldb, int64_t sB,
+                    double beta, double *C, int64_t ldc, int64_t sC, int64_t batch,
+                    bool lower_only = false, int tri_mode = 0);
+// Batched Cholesky of `batch` problems of equal size (see potrf).
+void potrf_batched(cudaStream_t s, double *A, int64_t n, int64_t lda, int64_t sA, double *Winv,
+                   int64_t sW, double *logdet_part, int64_t sL, int *status, int64_t batch);
+
 // Blocked right-looking Cholesky of the lower triangle of A (n x n, lda), in
 // place. Winv receives the inverses of the NB x NB diagonal factors
 // (nblocks * NB * NB); logdet_part the per-block sums of log L_jj; status[0]
@@ -167,10 +176,12 @@ struct OzSplit {
   int *ex = nullptr;        // per-row power-of-two exponents (rows padded)
   uint16_t *sl = nullptr;   // BF16 slices, pre-tiled for UMMA
   int64_t rows = 0, K = 0, nrb = 0, nkb = 0;
+  int64_t bstride_ex = 0, bstride_sl = 0;  // batched operands: per-problem strides
+  int S = 4;  // slices (8S-bit fixed point); both operands of a product use the same S
 };
 int64_t oz_nrb(int64_t rows);
-size_t oz_split_bytes(int64_t rows, int64_t K);
-void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out);
+size_t oz_split_bytes(int64_t rows, int64_t K, int S = 4);
+void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out, int S = 4);
 // rows x K operand: element (r, k) = P[r + k*ld] (trans 0) or P[k + r*ld] (trans 1)
 void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,
               OzSplit *out);
@@ -179,7 +190,14 @@ void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t ro
 void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
              int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
              double *C, int64_t ldc, bool lower_only, int *err, const int *status = nullptr);
-void oz_set_desc_variant(int v);
+// Batched versions: problem z uses P + z sP and the split's batch strides (set
+// bstride_ex / bstride_sl before splitting); C + z sC; status + z status_bs.
+void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, int trans, int64_t rows,
+                      int64_t K, OzSplit *out, int64_t batch);
+void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
+                     int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha,
+                     double beta, double *C, int64_t ldc, int64_t sC, bool lower_only, int *err,
+                     const int *status, int64_t status_bs, int64_t batch);
 
 // Mixed-precision factorisation and inverses (same outputs as the FP64 versions).
 void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,

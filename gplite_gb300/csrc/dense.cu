@@ -29,8 +29,12 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
                                                      const double *__restrict__ A, int64_t lda,
                                                      const double *__restrict__ B, int64_t ldb,
                                                      double beta, double *__restrict__ C,
-                                                     int64_t ldc, int lower_only, int tri_mode) {
+                                                     int64_t ldc, int lower_only, int tri_mode,
+                                                     int64_t sA, int64_t sB, int64_t sC) {
   const int64_t bm = blockIdx.x, bn = blockIdx.y;
+  A += blockIdx.z * sA;  // batched: problem blockIdx.z
+  B += blockIdx.z * sB;
+  C += blockIdx.z * sC;
   const int64_t row0 = bm * GBM, col0 = bn * GBN;
   if (lower_only && col0 > row0 + GBM - 1) return;
   __shared__ double As[GBK][GBM + 1];
@@ -108,21 +112,29 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
   }
 }
 
+void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+                    const double *A, int64_t lda, int64_t sA, const double *B, int64_t ldb, int64_t sB,
+                    double beta, double *C, int64_t ldc, int64_t sC, int64_t batch, bool lower_only,
+                    int tri_mode) {
+  if (M <= 0 || N <= 0 || batch <= 0) return;
+  dim3 grid((unsigned)((M + GBM - 1) / GBM), (unsigned)((N + GBN - 1) / GBN), (unsigned)batch);
+  int lo = lower_only ? 1 : 0;
+  if (!ta && !tb)
+    gemm64_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
+  else if (!ta && tb)
+    gemm64_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
+  else if (ta && !tb)
+    gemm64_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
+  else
+    gemm64_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
+  GPGP_CHECK_LAUNCH();
+}
+
 void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
             const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
             int64_t ldc, bool lower_only, int tri_mode) {
-  if (M <= 0 || N <= 0) return;
-  dim3 grid((unsigned)((M + GBM - 1) / GBM), (unsigned)((N + GBN - 1) / GBN));
-  int lo = lower_only ? 1 : 0;
-  if (!ta && !tb)
-    gemm64_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
-  else if (!ta && tb)
-    gemm64_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
-  else if (ta && !tb)
-    gemm64_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
-  else
-    gemm64_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode);
-  GPGP_CHECK_LAUNCH();
+  gemm64_batched(s, ta, tb, M, N, K, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, lower_only,
+                 tri_mode);
 }
 
 // ---------------------------------------------------------------------------
@@ -138,7 +150,13 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                                          double *__restrict__ Winv,
                                                          double *__restrict__ logdet_part,
-                                                         int *__restrict__ status, int64_t k0) {
+                                                         int *__restrict__ status, int64_t k0,
+                                                         int64_t sA, int64_t sW, int64_t sL) {
+  // batched: problem blockIdx.x (strides sA, sW, sL; status has one word per problem)
+  A += blockIdx.x * sA;
+  Winv += blockIdx.x * sW;
+  logdet_part += blockIdx.x * sL;
+  status += blockIdx.x;
   __shared__ double S[NB][NB + 1];
   __shared__ double Wsm[NB][NB + 1];
   __shared__ double rdiag[NB];
@@ -225,7 +243,11 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
 // ill-conditioned (FITC's K_z); the inverse W is used by the solves instead.
 __global__ void __launch_bounds__(128) potrf_panel_kernel(double *__restrict__ A21, int64_t m, int kb,
                                                           int64_t lda, const double *__restrict__ L11,
-                                                          const int *__restrict__ status) {
+                                                          const int *__restrict__ status, int64_t sA) {
+  // batched: problem blockIdx.y (A21 and L11 offset by sA, one status word per problem)
+  A21 += blockIdx.y * sA;
+  L11 += blockIdx.y * sA;
+  status += blockIdx.y;
   __shared__ double Ls[NB][NB + 1];
   __shared__ double rd[NB];
   if (*(volatile const int *)status != 0) return;
@@ -258,15 +280,38 @@ void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, doub
     const int kb = (int)std::min<int64_t>(NB, n - k0);
     double *Akk = A + k0 + k0 * lda;
     double *W = Winv + blk * NB * NB;
-    potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0);
+    potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0, 0, 0, 0);
     GPGP_CHECK_LAUNCH();
     const int64_t m = n - k0 - kb;
     if (m > 0) {
       double *A21 = A + (k0 + kb) + k0 * lda;
-      potrf_panel_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(A21, m, kb, lda, Akk, status);
+      potrf_panel_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(A21, m, kb, lda, Akk, status, 0);
       GPGP_CHECK_LAUNCH();
       double *A22 = A + (k0 + kb) + (k0 + kb) * lda;
       gemm64(s, false, true, m, m, kb, -1.0, A21, lda, A21, lda, 1.0, A22, lda, true, 0);
+    }
+  }
+}
+
+// Batched: `batch` problems of the same size n, matrices sA apart, inverses sW
+// apart, logdet partials sL apart, one status word each.
+void potrf_batched(cudaStream_t s, double *A, int64_t n, int64_t lda, int64_t sA, double *Winv,
+                   int64_t sW, double *logdet_part, int64_t sL, int *status, int64_t batch) {
+  for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
+    const int kb = (int)std::min<int64_t>(NB, n - k0);
+    double *Akk = A + k0 + k0 * lda;
+    potrf_diag_kernel<<<(unsigned)batch, 256, 0, s>>>(Akk, kb, lda, Winv + blk * NB * NB, logdet_part + blk,
+                                                      status, k0, sA, sW, sL);
+    GPGP_CHECK_LAUNCH();
+    const int64_t m = n - k0 - kb;
+    if (m > 0) {
+      double *A21 = A + (k0 + kb) + k0 * lda;
+      dim3 pg((unsigned)((m + 127) / 128), (unsigned)batch);
+      potrf_panel_kernel<<<pg, 128, 0, s>>>(A21, m, kb, lda, Akk, status, sA);
+      GPGP_CHECK_LAUNCH();
+      double *A22 = A + (k0 + kb) + (k0 + kb) * lda;
+      gemm64_batched(s, false, true, m, m, kb, -1.0, A21, lda, sA, A21, lda, sA, 1.0, A22, lda, sA, batch,
+                     true, 0);
     }
   }
 }

@@ -29,8 +29,6 @@
 
 namespace gpgp {
 
-constexpr int OZ_S = 4;             // slices per operand
-constexpr int OZ_LEVELS = 5;        // levels kept (t + u <= 4): 13 products
 constexpr int OZ_TK = 64;           // K chunk
 // Chunks accumulated in TMEM before a flush: level-0 and level-1 sums stay below
 // 2^24 (exact in FP32) for 4 x 64 = 256 products; deeper levels may round, but
@@ -38,17 +36,25 @@ constexpr int OZ_TK = 64;           // K chunk
 constexpr int OZ_GROUP = 4;
 constexpr int OZ_TR = 64;           // rows per slice tile
 constexpr int OZ_TILE = OZ_TR * OZ_TK;  // bf16 elements per slice tile (8 KB)
-constexpr int OZ_BM = 128, OZ_BN = 64;
-constexpr int OZ_A_STAGE = OZ_S * 2 * OZ_TILE * 2;  // bytes: 4 slices x 128 rows x 64 K x 2 B
-constexpr int OZ_B_STAGE = OZ_S * OZ_TILE * 2;      // bytes: 4 slices x 64 rows x 64 K x 2 B
-constexpr int OZ_STAGE = OZ_A_STAGE + OZ_B_STAGE;   // 96 KB
-constexpr int OZ_SMEM = 2 * OZ_STAGE + 1024;        // two stages + barriers
-constexpr uint32_t OZ_TMEM_COLS = 512;              // 5 levels x 64 columns (rounded to a power of 2)
+constexpr int OZ_BM = 128;
 
-// Descriptor layout variant (selected by gpgp_mixed_selftest): 0 = LBO is the K
-// step (128 B), SBO the 8-row step (1024 B); 1 = the other way round.
-__device__ int g_oz_desc_variant = 0;
-static int h_oz_desc_variant = 0;
+// S slices per operand (8S-bit fixed point): levels t + u <= S are kept
+// (S = 4: 13 products, truncation 2^-33; S = 5: 19 products, 2^-41). The
+// tile is 128 x 64 for S = 4 and 128 x 32 for S = 5 so that two pipeline
+// stages of operands fit in shared memory.
+template <int S>
+struct OzCfg {
+  static constexpr int LEVELS = S + 1;
+  static constexpr int BN = S == 4 ? 64 : 32;
+  static constexpr int A_STAGE = S * 2 * OZ_TILE * 2;  // S slices x 128 rows x 64 K x 2 B
+  static constexpr int B_TILE = BN * OZ_TK * 2;        // one slice of BN rows
+  static constexpr int B_STAGE = S * B_TILE;
+  static constexpr int STAGE = A_STAGE + B_STAGE;
+  static constexpr int SMEM = 2 * STAGE + 1024;
+  static constexpr uint32_t TMEM_COLS = LEVELS * BN <= 256 ? 256u : 512u;
+  static constexpr int CPT = BN / 2;  // accumulator columns per epilogue thread
+};
+
 
 // ---------------------------------------------------------------------------
 // split: FP64 rows -> 4 BF16 slices (canonical layout) + per-row exponents
@@ -66,7 +72,10 @@ __device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans
 // integer instructions only (the FP64 pipe of this part is slow).
 
 __global__ void oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
-                                 int64_t K, int64_t rows_pad, int *__restrict__ ex) {
+                                 int64_t K, int64_t rows_pad, int *__restrict__ ex, int64_t sP,
+                                 int64_t sE) {
+  P += blockIdx.y * sP;  // batched: problem blockIdx.y
+  ex += blockIdx.y * sE;
   // one warp per row: the largest |P| by an unsigned compare of the sign-cleared bits
   const int lane = threadIdx.x & 31;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -99,32 +108,40 @@ __device__ __forceinline__ uint32_t bf16_of_digit(int q) {
   return sgn | ((uint32_t)(127 + p) << 7) | mant;
 }
 
-// 32-bit fixed-point |x| 2^32 (rounded to nearest) of x = P 2^-e, as balanced
-// base-256 digits d0..d3 (|d0| <= 256, |d1..d3| <= 128) carrying the sign of P
-__device__ __forceinline__ void oz_digits(double v, int e, int d[4]) {
+// 8S-bit fixed point |x| 2^8S (rounded to nearest) of x = P 2^-e, as balanced
+// base-256 digits d0..d(S-1) (|d0| <= 256, the others <= 128) carrying the sign of P
+template <int S>
+__device__ __forceinline__ void oz_digits(double v, int e, int d[S]) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const int E = (int)((b >> 52) & 0x7FF);
   unsigned long long X = 0ull;
   if (E != 0 && E != 2047) {
     const unsigned long long mnt = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int rsh = 1043 + e - E;  // >= 21 because |v| < 2^e
+    const int rsh = 1075 + e - E - 8 * S;  // >= 13 because |v| < 2^e
     if (rsh < 64) X = (mnt + (1ull << (rsh - 1))) >> rsh;
   }
-  int u3 = (int)(X & 255ull), u2 = (int)((X >> 8) & 255ull), u1 = (int)((X >> 16) & 255ull);
-  int u0 = (int)(X >> 24);
-  if (u3 >= 128) { u3 -= 256; u2 += 1; }
-  if (u2 >= 128) { u2 -= 256; u1 += 1; }
-  if (u1 >= 128) { u1 -= 256; u0 += 1; }
-  const int s = (b >> 63) ? -1 : 1;
-  d[0] = s * u0;
-  d[1] = s * u1;
-  d[2] = s * u2;
-  d[3] = s * u3;
+  int u[S];
+#pragma unroll
+  for (int t = 0; t < S; ++t) u[t] = (int)((X >> (8 * (S - 1 - t))) & 255ull);
+  u[0] = (int)(X >> (8 * (S - 1)));
+#pragma unroll
+  for (int t = S - 1; t >= 1; --t)
+    if (u[t] >= 128) {
+      u[t] -= 256;
+      u[t - 1] += 1;
+    }
+  const int sg = (b >> 63) ? -1 : 1;
+#pragma unroll
+  for (int t = 0; t < S; ++t) d[t] = sg * u[t];
 }
 
+template <int S>
 __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
                                 int64_t K, int64_t nrb, int64_t nkb, const int *__restrict__ ex,
-                                uint16_t *__restrict__ sl) {
+                                uint16_t *__restrict__ sl, int64_t sP, int64_t sE, int64_t sS) {
+  P += blockIdx.y * sP;  // batched: problem blockIdx.y
+  ex += blockIdx.y * sE;
+  sl += blockIdx.y * sS;
   // thread per (row, 8-wide K group): writes 16 bytes per slice
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t rows_pad = nrb * OZ_TR;
@@ -134,20 +151,20 @@ __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int tr
   const int64_t g = trans ? tid % ngroups : tid / rows_pad;
   const int64_t k0 = g * 8;
   const int e = ex[r];
-  uint32_t packed[OZ_S][4];
+  uint32_t packed[S][4];
 #pragma unroll
   for (int j = 0; j < 8; j += 2) {
-    int d0[4], d1[4];
-    oz_digits(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
-    oz_digits(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
+    int d0[S], d1[S];
+    oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
+    oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
 #pragma unroll
-    for (int t = 0; t < OZ_S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t]) | (bf16_of_digit(d1[t]) << 16);
+    for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t]) | (bf16_of_digit(d1[t]) << 16);
   }
   const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
   const int64_t kb = k0 / OZ_TK, kk = k0 % OZ_TK;
   const int64_t within = (rr / 8) * 512 + (kk / 8) * 64 + (rr % 8) * 8;
 #pragma unroll
-  for (int t = 0; t < OZ_S; ++t) {
+  for (int t = 0; t < S; ++t) {
     const int64_t tile = ((int64_t)t * nkb + kb) * nrb + rb;
     uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
     *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) = v;
@@ -162,8 +179,8 @@ int64_t oz_nrb(int64_t rows) {
   return (t + 1) / 2 * 2;
 }
 
-void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,
-              OzSplit *out) {
+void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, int trans, int64_t rows,
+                      int64_t K, OzSplit *out, int64_t batch) {
   const int64_t nrb = oz_nrb(rows);
   const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
   out->rows = rows;
@@ -171,29 +188,39 @@ void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t ro
   out->nrb = nrb;
   out->nkb = nkb;
   const int64_t rows_pad = nrb * OZ_TR;
+  const int64_t sE = out->bstride_ex, sS = out->bstride_sl;
   {
     const int64_t threads = rows_pad * 32;
-    oz_rowexp_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, ld, trans, rows, K, rows_pad,
-                                                                      out->ex);
+    dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);
+    oz_rowexp_kernel<<<g, 256, 0, s>>>(P, ld, trans, rows, K, rows_pad, out->ex, sP, sE);
     GPGP_CHECK_LAUNCH();
   }
   {
     const int64_t threads = rows_pad * nkb * (OZ_TK / 8);
-    oz_slice_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb,
-                                                                      out->ex, out->sl);
+    dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);
+    if (out->S == 5)
+      oz_slice_kernel<5><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
+    else
+      oz_slice_kernel<4><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
     GPGP_CHECK_LAUNCH();
   }
 }
 
-size_t oz_split_bytes(int64_t rows, int64_t K) {
-  const int64_t nrb = oz_nrb(rows);
-  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
-  return (size_t)nrb * OZ_TR * sizeof(int) + 256 + (size_t)OZ_S * nkb * nrb * OZ_TILE * 2;
+void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,
+              OzSplit *out) {
+  oz_split_batched(s, P, ld, 0, trans, rows, K, out, 1);
 }
 
-void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out) {
+size_t oz_split_bytes(int64_t rows, int64_t K, int S) {
+  const int64_t nrb = oz_nrb(rows);
+  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
+  return (size_t)nrb * OZ_TR * sizeof(int) + 256 + (size_t)S * nkb * nrb * OZ_TILE * 2;
+}
+
+void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out, int S) {
   const int64_t nrb = oz_nrb(rows);
   (void)K;
+  out->S = S;
   char *p = (char *)mem;
   out->ex = (int *)p;
   size_t exb = ((size_t)nrb * OZ_TR * sizeof(int) + 255) / 256 * 256;
@@ -276,6 +303,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+template <int NC>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[NC]) {
+  if constexpr (NC == 32) tmem_ld32(taddr, r);
+  else tmem_ld16(taddr, r);
+}
+
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -322,17 +364,28 @@ struct OzGemmArgs {
   int lower_only;
   int *err;
   const int *status;  // optional: skip all work when a factorisation already failed
+  int64_t a_bs_sl, a_bs_ex, b_bs_sl, b_bs_ex, c_bs;  // batch strides (problem blockIdx.z)
+  int64_t status_bs;
 };
 
+template <int S>
 __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
+  using Cfg = OzCfg<S>;
+  constexpr int BN = Cfg::BN, CPT = Cfg::CPT;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // align the dynamic shared memory base to 1024 bytes
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int64_t row0 = (int64_t)blockIdx.x * OZ_BM;
-  const int64_t col0 = (int64_t)blockIdx.y * OZ_BN;
+  const int64_t col0 = (int64_t)blockIdx.y * BN;
   if (g.lower_only && col0 > row0 + OZ_BM - 1) return;
+  const int64_t zb = blockIdx.z;
+  const uint16_t *a_sl = g.a_sl + zb * g.a_bs_sl;
+  const int *a_ex = g.a_ex + zb * g.a_bs_ex;
+  const uint16_t *b_sl = g.b_sl + zb * g.b_bs_sl;
+  const int *b_ex = g.b_ex + zb * g.b_bs_ex;
+  double *Cz = g.C + zb * g.c_bs;
 
   // K-chunk range of this tile
   const int64_t grow0 = g.a_rb0 * OZ_TR + row0;  // absolute operand row of the tile
@@ -350,10 +403,10 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
     const int64_t e0 = (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK;
     kc1 = kc1 < e0 ? kc1 : e0;
   }
-  if (g.status && *(volatile const int *)g.status != 0) return;
+  if (g.status && *(volatile const int *)(g.status + blockIdx.z * g.status_bs) != 0) return;
   const int64_t nch = kc1 > kc0 ? kc1 - kc0 : 0;
 
-  uint64_t *bars = (uint64_t *)(smem + 2 * OZ_STAGE);
+  uint64_t *bars = (uint64_t *)(smem + 2 * Cfg::STAGE);
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
   // full[s]: operands of the chunk in stage s landed; empty[s]: the MMAs that read
@@ -373,7 +426,7 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_sh)),
-                 "r"(OZ_TMEM_COLS));
+                 "r"(Cfg::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -383,35 +436,38 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
 
   // operand tile addresses for chunk c (global)
   auto a_tile = [&](int s, int64_t kc) {
-    return g.a_sl + (((int64_t)s * g.a_nkb + kc) * g.a_nrb + g.a_rb0 + 2 * blockIdx.x) * OZ_TILE;
+    return a_sl + (((int64_t)s * g.a_nkb + kc) * g.a_nrb + g.a_rb0 + 2 * blockIdx.x) * OZ_TILE;
   };
+  // a BN-row part of a 64-row slice tile is contiguous (rows are the outer index)
   auto b_tile = [&](int s, int64_t kc) {
-    return g.b_sl + (((int64_t)s * g.b_nkb + kc) * g.b_nrb + g.b_rb0 + blockIdx.y) * OZ_TILE;
+    return b_sl + (((int64_t)s * g.b_nkb + kc) * g.b_nrb + g.b_rb0 + col0 / OZ_TR) * OZ_TILE +
+           (col0 % OZ_TR) * OZ_TK;
   };
   auto load_stage = [&](int st, int64_t kc) {
-    const uint32_t base = smem_u32(smem + st * OZ_STAGE);
+    const uint32_t base = smem_u32(smem + st * Cfg::STAGE);
     const uint32_t bar = st ? full1 : full0;
-    mbar_expect_tx(bar, OZ_STAGE);
-    for (int s = 0; s < OZ_S; ++s) {
+    mbar_expect_tx(bar, Cfg::STAGE);
+    for (int s = 0; s < S; ++s) {
       bulk_g2s(base + s * (2 * OZ_TILE * 2), a_tile(s, kc), 2 * OZ_TILE * 2, bar);
-      bulk_g2s(base + OZ_A_STAGE + s * (OZ_TILE * 2), b_tile(s, kc), OZ_TILE * 2, bar);
+      bulk_g2s(base + Cfg::A_STAGE + s * Cfg::B_TILE, b_tile(s, kc), Cfg::B_TILE, bar);
     }
   };
 
   if (tid == 0 && nch > 0) load_stage(0, kc0);
 
-  // instruction descriptor: D F32, A/B BF16, K-major both, N = 64, M = 128
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+  // instruction descriptor: D F32, A/B BF16, K-major both, N = BN, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                          ((uint32_t)(OZ_BM >> 4) << 24);
-  const int variant = g_oz_desc_variant;
-  const uint32_t lbo = variant ? 1024u : 128u, sbo = variant ? 128u : 1024u;
+  // no-swizzle K-major operands: 8 x 16-byte core matrices, the leading byte
+  // offset steps K (128 B), the stride byte offset steps 8 rows (1024 B)
+  const uint32_t lbo = 128u, sbo = 1024u;
 
-  // epilogue ownership: warp w reads TMEM lanes 32*(w%4).., columns 32*(w/4)..
+  // epilogue ownership: warp w reads TMEM lanes 32*(w%4).., columns CPT*(w/4)..
   const int quarter = warp & 3, half = warp >> 2;
   const int64_t my_row = row0 + quarter * 32 + lane;
-  float hi[32], lo[32];
+  float hi[CPT], lo[CPT];
 #pragma unroll
-  for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0.f;
+  for (int c = 0; c < CPT; ++c) hi[c] = lo[c] = 0.f;
 
   bool ok = true;
   int nflush = 0;
@@ -423,22 +479,22 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
       bool good = mbar_wait_bounded(st ? full1 : full0, (uint32_t)((c >> 1) & 1));
       if (good) {
         tc_fence_after();
-        const uint32_t abase = smem_u32(smem + st * OZ_STAGE);
-        const uint32_t bbase = abase + OZ_A_STAGE;
-        int first[OZ_LEVELS];
+        const uint32_t abase = smem_u32(smem + st * Cfg::STAGE);
+        const uint32_t bbase = abase + Cfg::A_STAGE;
+        int first[Cfg::LEVELS];
 #pragma unroll
-        for (int l = 0; l < OZ_LEVELS; ++l) first[l] = group_start ? 1 : 0;
+        for (int l = 0; l < Cfg::LEVELS; ++l) first[l] = group_start ? 1 : 0;
 #pragma unroll
-        for (int t = 0; t < OZ_S; ++t) {
+        for (int t = 0; t < S; ++t) {
 #pragma unroll
-          for (int u = 0; u < OZ_S; ++u) {
+          for (int u = 0; u < S; ++u) {
             const int lev = t + u;
-            if (lev >= OZ_LEVELS) continue;
+            if (lev >= Cfg::LEVELS) continue;
 #pragma unroll
             for (int kk = 0; kk < OZ_TK / 16; ++kk) {
               const uint64_t ad = umma_desc(abase + t * (2 * OZ_TILE * 2) + kk * 2 * 128, lbo, sbo);
-              const uint64_t bd = umma_desc(bbase + u * (OZ_TILE * 2) + kk * 2 * 128, lbo, sbo);
-              umma_bf16(tmem + lev * OZ_BN, ad, bd, idesc, first[lev] ? 0u : 1u);
+              const uint64_t bd = umma_desc(bbase + u * Cfg::B_TILE + kk * 2 * 128, lbo, sbo);
+              umma_bf16(tmem + lev * BN, ad, bd, idesc, first[lev] ? 0u : 1u);
               first[lev] = 0;
             }
           }
@@ -471,13 +527,13 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
       ++nflush;
       tc_fence_after();
 #pragma unroll 1
-      for (int lev = 0; lev < OZ_LEVELS; ++lev) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + lev * OZ_BN + half * 32, r);
+      for (int lev = 0; lev < Cfg::LEVELS; ++lev) {
+        uint32_t r[CPT];
+        tmem_ld<CPT>(tmem + ((uint32_t)(quarter * 32) << 16) + lev * BN + half * CPT, r);
         tmem_ld_wait();
         const float sc = __uint_as_float((uint32_t)(127 - 8 * lev) << 23);  // 2^-8lev
 #pragma unroll
-        for (int j = 0; j < 32; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+        for (int j = 0; j < CPT; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
       }
       tc_fence_before();
       __syncthreads();
@@ -503,21 +559,21 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::TMEM_COLS));
   }
   if (!ok) return;
   // FP64 epilogue: C = alpha * 2^(e_i + f_j - 16) (hi + lo) + beta * C, with the
   // float -> double conversion and the power of two done on the bit patterns
   if (my_row < g.M) {
-    const int ea = g.a_ex[g.a_rb0 * OZ_TR + my_row];
+    const int ea = a_ex[g.a_rb0 * OZ_TR + my_row];
     const bool unit = (g.alpha == 1.0 || g.alpha == -1.0) && (g.beta == 0.0 || g.beta == 1.0);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int64_t col = col0 + half * 32 + j;
+    for (int j = 0; j < CPT; ++j) {
+      const int64_t col = col0 + half * CPT + j;
       if (col < g.N && !(g.lower_only && my_row < col)) {
-        const int sh = ea + g.b_ex[g.b_rb0 * OZ_TR + col] - 16;
+        const int sh = ea + b_ex[g.b_rb0 * OZ_TR + col] - 16;
         double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
-        double *dst = g.C + my_row + col * g.ldc;
+        double *dst = Cz + my_row + col * g.ldc;
         if (unit) {
           if (g.alpha < 0.0) v = -v;
           *dst = (g.beta == 0.0) ? v : *dst + v;
@@ -529,13 +585,18 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   }
 }
 
-void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
-             int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
-             double *C, int64_t ldc, bool lower_only, int *err, const int *status) {
-  if (M <= 0 || N <= 0) return;
+void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
+                     int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha,
+                     double beta, double *C, int64_t ldc, int64_t sC, bool lower_only, int *err,
+                     const int *status, int64_t status_bs, int64_t batch) {
+  if (M <= 0 || N <= 0 || batch <= 0) return;
+  if (A.S != B.S) throw CudaError{cudaErrorInvalidValue, "oz_gemm: operands split to different slice counts", __LINE__};
   static bool attr = false;
   if (!attr) {
-    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM + 1024));
+    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OzCfg<4>::SMEM + 1024));
+    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OzCfg<5>::SMEM + 1024));
     attr = true;
   }
   OzGemmArgs g;
@@ -561,15 +622,30 @@ void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B,
   g.lower_only = lower_only ? 1 : 0;
   g.err = err;
   g.status = status;
-  dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OZ_BN - 1) / OZ_BN));
-  oz_gemm_kernel<<<grid, 256, OZ_SMEM + 1024, s>>>(g);
+  g.a_bs_sl = A.bstride_sl;
+  g.a_bs_ex = A.bstride_ex;
+  g.b_bs_sl = B.bstride_sl;
+  g.b_bs_ex = B.bstride_ex;
+  g.c_bs = sC;
+  g.status_bs = status_bs;
+  if (A.S == 5) {
+    dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OzCfg<5>::BN - 1) / OzCfg<5>::BN),
+              (unsigned)batch);
+    oz_gemm_kernel<5><<<grid, 256, OzCfg<5>::SMEM + 1024, s>>>(g);
+  } else {
+    dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OzCfg<4>::BN - 1) / OzCfg<4>::BN),
+              (unsigned)batch);
+    oz_gemm_kernel<4><<<grid, 256, OzCfg<4>::SMEM + 1024, s>>>(g);
+  }
   GPGP_CHECK_LAUNCH();
 }
 
-void oz_set_desc_variant(int v) {
-  if (v == h_oz_desc_variant) return;
-  GPGP_CUDA(cudaMemcpyToSymbol(g_oz_desc_variant, &v, sizeof(int)));
-  h_oz_desc_variant = v;
+void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
+             int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
+             double *C, int64_t ldc, bool lower_only, int *err, const int *status) {
+  oz_gemm_batched(s, A, a_row0, B, b_row0, M, N, kc0, kc1, kmode, alpha, beta, C, ldc, 0, lower_only,
+                  err, status, 0, 1);
 }
+
 
 }  // namespace gpgp

@@ -21,7 +21,8 @@ namespace gpgp {
 // potrf_diag_kernel lives in dense.cu
 __global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                   double *__restrict__ Winv, double *__restrict__ logdet_part,
-                                  int *__restrict__ status, int64_t k0);
+                                  int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
+                                  int64_t sL);
 
 namespace {
 
@@ -58,7 +59,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
       const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
       const int64_t blk = j0 / NB;
       double *Wb = Winv + blk * NB * NB;
-      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0);
+      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
       GPGP_CHECK_LAUNCH();
       const int64_t m = n - j0 - jb;
       if (m <= 0) continue;
@@ -219,12 +220,12 @@ __global__ void max_abs_kernel(const double *a, const double *b, int64_t n, doub
 }  // namespace
 
 extern "C" gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K,
-                                           int32_t variant, double *max_rel_err) {
+                                           int32_t slices, double *max_rel_err) {
   using namespace gpgp;
-  if (!ctx || M < 1 || N < 1 || K < 1 || !max_rel_err) return GPGP_EINVAL;
+  if (!ctx || M < 1 || N < 1 || K < 1 || !max_rel_err || (slices != 4 && slices != 5))
+    return GPGP_EINVAL;
   cudaStream_t s = (cudaStream_t)gpgp_stream(ctx);
   try {
-    oz_set_desc_variant(variant);
     double *A = nullptr, *B = nullptr, *C1 = nullptr, *C2 = nullptr, *red = nullptr;
     int *err = nullptr;
     GPGP_CUDA(cudaMallocAsync((void **)&A, M * K * sizeof(double), s));
@@ -240,11 +241,11 @@ extern "C" gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, 
     GPGP_CUDA(cudaMemcpyAsync(C2, C1, M * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     {
       void *pa = nullptr, *pb = nullptr;
-      GPGP_CUDA(cudaMallocAsync(&pa, oz_split_bytes(M, K), s));
-      GPGP_CUDA(cudaMallocAsync(&pb, oz_split_bytes(N, K), s));
+      GPGP_CUDA(cudaMallocAsync(&pa, oz_split_bytes(M, K, slices), s));
+      GPGP_CUDA(cudaMallocAsync(&pb, oz_split_bytes(N, K, slices), s));
       OzSplit sa, sb;
-      oz_split_bind(pa, M, K, &sa);
-      oz_split_bind(pb, N, K, &sb);
+      oz_split_bind(pa, M, K, &sa, slices);
+      oz_split_bind(pb, N, K, &sb, slices);
       oz_split(s, A, M, 0, M, K, &sa);
       oz_split(s, B, N, 0, N, K, &sb);
       // C1 = -A B^T + C1 (sliced) ; C2 = -A B^T + C2 (FP64)

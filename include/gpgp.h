@@ -252,6 +252,35 @@ gpgp_status gpgp_pred_dev(gpgp_model *model, const double *xt, int64_t m, uint32
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
 
+/* ---- batched small GPs: many independent regressions of uneven size --
+ * Each problem is gp_fit (lik_gaussian, method_full, one covariance term of
+ * kind sexp / matern32 / matern52 over all d inputs), gp_loo (approx_laplace,
+ * Gauss-Hermite of order quad_order) and gp_pred with var = TRUE at its m test
+ * points. Host buffers, column-major; n <= 4096, d <= 8. A plan uploads the
+ * inputs, autotunes each size bucket (mixed precision: FP64 pipe or sliced
+ * tensor cores, whichever is faster) and captures the whole pipeline in one
+ * CUDA graph; gpgp_batch_run replays it; gpgp_batch_upload replaces the inputs
+ * of a plan with new data of the same shapes. Results are packed in problem
+ * order: log_evidence[nprob], mean/var[sum m_i], loos[sum n_i]. A problem whose
+ * factor is not positive definite gets log_evidence = -Inf. */
+typedef struct gpgp_batch_problem {
+  int32_t n, d, m;
+  int32_t kind;                /* GPGP_CF_SEXP, GPGP_CF_MATERN32 or GPGP_CF_MATERN52 */
+  double lscale, magn, sigma;  /* cf lscale, cf magn, lik_gaussian sigma */
+  const double *x, *y, *xt;
+} gpgp_batch_problem;
+typedef struct gpgp_batch gpgp_batch;
+gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, int32_t nprob,
+                              int32_t precision, int32_t quad_order, double jitter,
+                              gpgp_batch **out);
+gpgp_status gpgp_batch_upload(gpgp_batch *b, const gpgp_batch_problem *probs);
+gpgp_status gpgp_batch_run(gpgp_batch *b);
+gpgp_status gpgp_batch_results(gpgp_batch *b, double *log_evidence, double *mean, double *var,
+                               double *loos);
+gpgp_status gpgp_batch_info(gpgp_batch *b, int32_t *nbuckets, int32_t *bucket_n,
+                            int32_t *bucket_count, int32_t *bucket_variant, double *tune_ms);
+gpgp_status gpgp_batch_destroy(gpgp_batch *b);
+
 /* ---- allocation-free Gaussian fit (no counterpart in the reference) ---
  * For callers that cannot allocate device memory while they need a fit: a
  * serving process whose own pool already owns all of HBM, a latency-critical
@@ -275,9 +304,9 @@ gpgp_status gpgp_fit_gaussian_noalloc(gpgp_ctx *ctx, const gpgp_kernel *k, doubl
 /* ---- self-test of the mixed-precision product: C = C - A B^T for random
  *      M x K and N x K operands with entries spread over 2^8 in magnitude,
  *      computed with the BF16-sliced tensor-core GEMM and with the FP64 GEMM;
- *      returns max |difference| / max |C|. variant selects the shared-memory
- *      descriptor convention (0 default) and stays selected afterwards. ---- */
-gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K, int32_t variant,
+ *      returns max |difference| / max |C|. slices is 4 (32-bit fixed point,
+ *      the factorisation path) or 5 (40-bit, the batched path). ---- */
+gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K, int32_t slices,
                                 double *max_rel_err);
 
 #ifdef __cplusplus

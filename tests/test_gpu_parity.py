@@ -257,7 +257,10 @@ def test_fitc_matches_oracle(lik, approx):
     Vectors are compared in the max norm relative to their largest entry (1e-9): FITC's
     solves with K_z (condition ~3e4 here) and the lemma's cancellation z/S - iDU C^-1 iDU^T z
     make single entries sensitive at ~1e-8 to one-ulp input changes (measured on the oracle
-    itself), so per-entry 1e-10 would test rounding noise, not the algorithm."""
+    itself), so per-entry 1e-10 would test rounding noise, not the algorithm. The LOO
+    densities add one more cancellation (1/post_var - 1/V): one-ulp relative changes of x
+    and z move the oracle's own max-norm LOO by 1.7e-9 .. 1.9e-8 (four seeds), so they are
+    held to 5e-8."""
     rng = np.random.default_rng(7)
     n, M = 300, 24
     x = rng.uniform(-3, 3, (n, 2))
@@ -288,7 +291,7 @@ def test_fitc_matches_oracle(lik, approx):
     assert relmax(p["mean"], po["mean"]) < 1e-9
     assert relmax(p["var"], po["var"]) < 1e-9
     loo, lo = G.gp_loo(gp, x, y), R.gp_loo(og, x, y)
-    assert relmax(loo["loos"], lo["loos"]) < 1e-9
+    assert relmax(loo["loos"], lo["loos"]) < 5e-8
 
 
 def test_fitc_method_full_agreement_at_full_inducing():
