@@ -70,6 +70,32 @@ class BatchProblem(C.Structure):
                 ("x", C.c_void_p), ("y", C.c_void_p), ("xt", C.c_void_p)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("workers", C.c_int32), ("hbm_budget", C.c_int64),
+                ("precision", C.c_int32), ("batch_max_n", C.c_int32), ("batch_max", C.c_int32),
+                ("jitter", C.c_double)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kernel", C.c_void_p), ("lik", C.c_void_p), ("method", C.c_void_p), ("approx", C.c_void_p),
+                ("x", C.c_void_p), ("n", C.c_int64), ("d", C.c_int32), ("y", C.c_void_p),
+                ("trials", C.c_void_p), ("offset", C.c_void_p), ("xt", C.c_void_p), ("m", C.c_int64),
+                ("keep", C.c_int32), ("model", C.c_int64), ("mean", C.c_void_p), ("var", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("lane", C.c_int32), ("log_evidence", C.c_double),
+                ("model", C.c_int64), ("queue_ms", C.c_double), ("run_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "completed", "failed", "pending", "inflight", "batches",
+                                         "batched_requests", "bytes_inflight", "bytes_resident", "bytes_peak",
+                                         "budget")] + [("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                                                       ("max_ms", C.c_double)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 
@@ -107,6 +133,12 @@ SIGNATURES = {
     "gpgp_batch_results": (C.c_int, [_P, _P, _P, _P, _P]),
     "gpgp_batch_info": (C.c_int, [_P, _P, _P, _P, _P, _P]),
     "gpgp_batch_destroy": (C.c_int, [_P]),
+    "gpgp_server_create": (C.c_int, [C.POINTER(ServerOpts), C.POINTER(_P)]),
+    "gpgp_server_submit": (C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "gpgp_server_poll": (C.c_int, [_P, C.c_int64, C.c_int32, C.POINTER(RequestResult)]),
+    "gpgp_server_release": (C.c_int, [_P, C.c_int64]),
+    "gpgp_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "gpgp_server_destroy": (C.c_int, [_P]),
     "gpgp_mixed_selftest": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P]),
     "gpgp_fit_gaussian_noalloc": (C.c_int, [_P, C.POINTER(Kernel), C.c_double, C.c_double, _P, C.c_int64,
                                             C.c_int32, _P, _P, _P]),

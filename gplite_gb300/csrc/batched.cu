@@ -505,7 +505,125 @@ void upload(gpgp_batch *b, const gpgp_batch_problem *probs) {
   }
 }
 
+std::string check_problems(const gpgp_batch_problem *probs, int32_t nprob) {
+  for (int32_t i = 0; i < nprob; ++i) {
+    const gpgp_batch_problem &p = probs[i];
+    if (p.n < 1 || p.n > 4096 || p.d < 1 || p.d > 8 || p.m < 0 || !p.x || !p.y || (p.m > 0 && !p.xt) ||
+        !(p.sigma > 0) || !(p.lscale > 0) ||
+        (p.kind != GPGP_CF_SEXP && p.kind != GPGP_CF_MATERN32 && p.kind != GPGP_CF_MATERN52))
+      return "batched problem " + std::to_string(i) + " is invalid";
+  }
+  return std::string();
+}
+
+// buckets, device buffers and the first upload of a plan
+void build_plan(gpgp_batch *b, gpgp_ctx *ctx, const gpgp_batch_problem *probs, int32_t nprob,
+                int32_t precision, int32_t quad_order, double jitter) {
+  GPGP_CUDA(cudaSetDevice(ctx->device));
+  b->ctx = ctx;
+  b->precision = precision;
+  b->quad_order = quad_order;
+  b->jitter = jitter;
+  b->nprob = nprob;
+  b->shape.assign(probs, probs + nprob);
+  cudaStream_t st = ctx->stream;
+  std::map<int64_t, std::vector<int>> groups;
+  for (int32_t i = 0; i < nprob; ++i) groups[(probs[i].n + NB - 1) / NB * NB].push_back(i);
+  b->bucket_of.assign(nprob, 0);
+  b->slot_of.assign(nprob, 0);
+  for (auto &g : groups) {
+    std::unique_ptr<Bucket> k(new Bucket());
+    k->nb = g.first;
+    k->count = (int64_t)g.second.size();
+    k->probs = g.second;
+    int64_t mb = 1, dm = 1;
+    for (int i : g.second) {
+      mb = std::max<int64_t>(mb, probs[i].m);
+      dm = std::max<int64_t>(dm, probs[i].d);
+    }
+    k->mb = (mb + NB - 1) / NB * NB;
+    k->dm = dm;
+    const int64_t P = k->count, nb = k->nb, mbb = k->mb;
+    k->prm.alloc(st, P * PRM);
+    k->X.alloc(st, P * nb * dm);
+    k->Y.alloc(st, P * nb);
+    k->Xt.alloc(st, P * mbb * dm);
+    k->Bm.alloc(st, P * nb * nb);
+    k->Winv.alloc(st, P * nb * NB);
+    k->ldp.alloc(st, P * (nb / NB));
+    k->W.alloc(st, P * nb * nb);
+    k->R.alloc(st, P * nb * mbb);
+    k->T.alloc(st, P * nb * mbb);
+    k->tmp.alloc(st, std::max<int64_t>(P * NB * nb, 3 * P * nb));
+    k->alpha.alloc(st, P * nb);
+    k->fhat.alloc(st, P * nb);
+    k->lml.alloc(st, P);
+    k->mean.alloc(st, P * mbb);
+    k->var.alloc(st, P * mbb);
+    k->loos.alloc(st, P * nb);
+    k->binv.alloc(st, P * nb);
+    k->status.alloc(st, P);
+    if (precision == GPGP_PREC_MIXED) {
+      // per-problem sliced operands: at most nb rows x nb K (A), max(nb, mb) rows x nb K (B)
+      const size_t ba = split_stride_bytes(nb, nb), bb = split_stride_bytes(std::max(nb, mbb), nb);
+      if (cudaMallocAsync(&k->sa, ba * P, st) != cudaSuccess || cudaMallocAsync(&k->sb, bb * P, st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw std::bad_alloc();
+      }
+      oz_split_bind(k->sa, nb, nb, &k->SA, kSlices);
+      oz_split_bind(k->sb, std::max(nb, mbb), nb, &k->SB, kSlices);
+      k->Bc.alloc(st, P * nb * nb);
+      // batch strides in elements of each array (ex ints, slices uint16)
+      k->SA.bstride_ex = (int64_t)(ba / sizeof(int));
+      k->SA.bstride_sl = (int64_t)(ba / sizeof(uint16_t));
+      k->SB.bstride_ex = (int64_t)(bb / sizeof(int));
+      k->SB.bstride_sl = (int64_t)(bb / sizeof(uint16_t));
+    }
+    k->variant = precision == GPGP_PREC_MIXED ? 1 : 0;
+    for (int64_t s = 0; s < P; ++s) {
+      b->bucket_of[g.second[s]] = (int)b->buckets.size();
+      b->slot_of[g.second[s]] = (int)s;
+    }
+    b->buckets.push_back(std::move(k));
+  }
+  std::vector<double> hx, hw;
+  gauss_hermite(quad_order, &hx, &hw);
+  copy_in(st, b->ghx, hx.data(), quad_order, false);
+  copy_in(st, b->ghw, hw.data(), quad_order, false);
+  b->err.alloc(st, 1);
+  GPGP_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(int), st));
+  upload(b, probs);
+}
+
 }  // namespace
+
+// One-shot batched solve for the request server: plan, upload, run the pipeline
+// once without autotuning or graph capture (the tensor-core variant for mixed
+// precision, the FP64 pipe otherwise, so a problem's result does not depend on
+// its batch-mates) and read the evidence, predictive means and variances back.
+gpgp_status gpgp::batch_solve_once(gpgp_ctx *ctx, const gpgp_batch_problem *probs, int32_t nprob,
+                                   int32_t precision, double jitter, double *lml, double *mean,
+                                   double *var) {
+  if (std::string why = check_problems(probs, nprob); !why.empty()) return fail(ctx, GPGP_EINVAL, why);
+  gpgp_status st = guarded(ctx, [&]() -> gpgp_status {
+    gpgp_batch b;
+    build_plan(&b, ctx, probs, nprob, precision, 11, jitter);
+    run_all(&b);
+    return gpgp_batch_results(&b, lml, mean, var, nullptr);
+  });
+  return st;
+}
+
+// Device bytes of a one-shot batch holding one problem of this size (the
+// allocations of build_plan, rounded up per problem).
+size_t gpgp::batch_bytes_estimate(int64_t n, int64_t m, int32_t d, int32_t precision) {
+  const int64_t nb = (n + NB - 1) / NB * NB, mb = std::max<int64_t>(NB, (m + NB - 1) / NB * NB);
+  size_t b = 8 * (size_t)(PRM + nb * d + nb + mb * d + 2 * nb * nb + nb * NB + nb / NB + 2 * nb * mb +
+                          std::max<int64_t>(NB * nb, 3 * nb) + 4 * nb + 1 + 2 * mb) + 4;
+  if (precision == GPGP_PREC_MIXED)
+    b += 8 * (size_t)nb * nb + split_stride_bytes(nb, nb) + split_stride_bytes(std::max(nb, mb), nb);
+  return b;
+}
 
 extern "C" {
 
@@ -514,88 +632,11 @@ gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, in
   if (!ctx || !probs || nprob < 1 || !out || quad_order < 1 || quad_order > 64)
     return fail(ctx, GPGP_EINVAL, "invalid argument");
   *out = nullptr;
-  for (int32_t i = 0; i < nprob; ++i) {
-    const gpgp_batch_problem &p = probs[i];
-    if (p.n < 1 || p.n > 4096 || p.d < 1 || p.d > 8 || p.m < 0 || !p.x || !p.y || (p.m > 0 && !p.xt) ||
-        !(p.sigma > 0) || !(p.lscale > 0) ||
-        (p.kind != GPGP_CF_SEXP && p.kind != GPGP_CF_MATERN32 && p.kind != GPGP_CF_MATERN52))
-      return fail(ctx, GPGP_EINVAL, "batched problem " + std::to_string(i) + " is invalid");
-  }
+  if (std::string why = check_problems(probs, nprob); !why.empty()) return fail(ctx, GPGP_EINVAL, why);
   return guarded(ctx, [&]() -> gpgp_status {
-    GPGP_CUDA(cudaSetDevice(ctx->device));
     std::unique_ptr<gpgp_batch> b(new gpgp_batch());
-    b->ctx = ctx;
-    b->precision = precision;
-    b->quad_order = quad_order;
-    b->jitter = jitter;
-    b->nprob = nprob;
-    b->shape.assign(probs, probs + nprob);
+    build_plan(b.get(), ctx, probs, nprob, precision, quad_order, jitter);
     cudaStream_t st = ctx->stream;
-    std::map<int64_t, std::vector<int>> groups;
-    for (int32_t i = 0; i < nprob; ++i) groups[(probs[i].n + NB - 1) / NB * NB].push_back(i);
-    b->bucket_of.assign(nprob, 0);
-    b->slot_of.assign(nprob, 0);
-    for (auto &g : groups) {
-      std::unique_ptr<Bucket> k(new Bucket());
-      k->nb = g.first;
-      k->count = (int64_t)g.second.size();
-      k->probs = g.second;
-      int64_t mb = 1, dm = 1;
-      for (int i : g.second) {
-        mb = std::max<int64_t>(mb, probs[i].m);
-        dm = std::max<int64_t>(dm, probs[i].d);
-      }
-      k->mb = (mb + NB - 1) / NB * NB;
-      k->dm = dm;
-      const int64_t P = k->count, nb = k->nb, mbb = k->mb;
-      k->prm.alloc(st, P * PRM);
-      k->X.alloc(st, P * nb * dm);
-      k->Y.alloc(st, P * nb);
-      k->Xt.alloc(st, P * mbb * dm);
-      k->Bm.alloc(st, P * nb * nb);
-      k->Winv.alloc(st, P * nb * NB);
-      k->ldp.alloc(st, P * (nb / NB));
-      k->W.alloc(st, P * nb * nb);
-      k->R.alloc(st, P * nb * mbb);
-      k->T.alloc(st, P * nb * mbb);
-      k->tmp.alloc(st, std::max<int64_t>(P * NB * nb, 3 * P * nb));
-      k->alpha.alloc(st, P * nb);
-      k->fhat.alloc(st, P * nb);
-      k->lml.alloc(st, P);
-      k->mean.alloc(st, P * mbb);
-      k->var.alloc(st, P * mbb);
-      k->loos.alloc(st, P * nb);
-      k->binv.alloc(st, P * nb);
-      k->status.alloc(st, P);
-      if (precision == GPGP_PREC_MIXED) {
-        // per-problem sliced operands: at most nb rows x nb K (A), max(nb, mb) rows x nb K (B)
-        const size_t ba = split_stride_bytes(nb, nb), bb = split_stride_bytes(std::max(nb, mbb), nb);
-        if (cudaMallocAsync(&k->sa, ba * P, st) != cudaSuccess || cudaMallocAsync(&k->sb, bb * P, st) != cudaSuccess) {
-          (void)cudaGetLastError();
-          throw std::bad_alloc();
-        }
-        oz_split_bind(k->sa, nb, nb, &k->SA, kSlices);
-        oz_split_bind(k->sb, std::max(nb, mbb), nb, &k->SB, kSlices);
-        k->Bc.alloc(st, P * nb * nb);
-        // batch strides in elements of each array (ex ints, slices uint16)
-        k->SA.bstride_ex = (int64_t)(ba / sizeof(int));
-        k->SA.bstride_sl = (int64_t)(ba / sizeof(uint16_t));
-        k->SB.bstride_ex = (int64_t)(bb / sizeof(int));
-        k->SB.bstride_sl = (int64_t)(bb / sizeof(uint16_t));
-      }
-      for (int64_t s = 0; s < P; ++s) {
-        b->bucket_of[g.second[s]] = (int)b->buckets.size();
-        b->slot_of[g.second[s]] = (int)s;
-      }
-      b->buckets.push_back(std::move(k));
-    }
-    std::vector<double> hx, hw;
-    gauss_hermite(quad_order, &hx, &hw);
-    copy_in(st, b->ghx, hx.data(), quad_order, false);
-    copy_in(st, b->ghw, hw.data(), quad_order, false);
-    b->err.alloc(st, 1);
-    GPGP_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(int), st));
-    upload(b.get(), probs);
     // autotune: the FP64 pipe or the sliced tensor-core GEMM, per bucket (mixed precision only)
     cudaEvent_t e0, e1;
     GPGP_CUDA(cudaEventCreate(&e0));
@@ -624,20 +665,20 @@ gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, in
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // capture the whole pipeline once (captured launches are not launches: the
-    // counter is restored and the graph's kernel nodes are counted per replay)
-    const int64_t launches_before = g_launches;
+    // capture the whole pipeline once; the graph's kernel nodes are counted per replay
     GPGP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    tl_capturing = true;
     try {
       run_all(b.get());
     } catch (...) {
+      tl_capturing = false;
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(st, &g);
       if (g) cudaGraphDestroy(g);
       throw;
     }
+    tl_capturing = false;
     GPGP_CUDA(cudaStreamEndCapture(st, &b->graph));
-    g_launches = launches_before;
     size_t nnodes = 0;
     GPGP_CUDA(cudaGraphGetNodes(b->graph, nullptr, &nnodes));
     std::vector<cudaGraphNode_t> nodes(nnodes);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -25,9 +27,15 @@ struct CudaError {
     if (e__ != cudaSuccess) throw ::gpgp::CudaError{e__, #call, __LINE__}; \
   } while (0)
 
-// Number of kernel launches issued through the library (all contexts).
-extern int64_t g_launches;
-#define GPGP_LAUNCHED() (++::gpgp::g_launches)
+// Number of kernel launches issued through the library (all contexts and
+// threads). Launches recorded into a graph under capture are not counted; a
+// graph replay adds its kernel nodes.
+extern std::atomic<int64_t> g_launches;
+extern thread_local bool tl_capturing;
+#define GPGP_LAUNCHED()                                                                 \
+  do {                                                                                 \
+    if (!::gpgp::tl_capturing) ::gpgp::g_launches.fetch_add(1, std::memory_order_relaxed); \
+  } while (0)
 #define GPGP_CHECK_LAUNCH()              \
   do {                                   \
     GPGP_LAUNCHED();                     \

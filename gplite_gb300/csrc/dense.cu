@@ -485,18 +485,16 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const double *__restrict
   }
 }
 
-static int g_coop_blocks = 0;
-
 void trsv_coop(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
                double *b, double *x, bool trans, const int *status, unsigned *bar, int *err) {
   if (n <= 0) return;
-  if (g_coop_blocks == 0) {
+  static const int g_coop_blocks = [] {
     int dev = 0, sms = 0, per = 0;
     GPGP_CUDA(cudaGetDevice(&dev));
     GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     GPGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop_kernel, 256, 0));
-    g_coop_blocks = sms * std::max(1, std::min(per, 2));
-  }
+    return sms * std::max(1, std::min(per, 2));
+  }();
   GPGP_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
   int tr = trans ? 1 : 0;
   void *args[] = {(void *)&L, (void *)&n, (void *)&lda, (void *)&Winv, (void *)&b, (void *)&x,
@@ -698,11 +696,6 @@ __global__ void gemv_reduce_kernel(int64_t M, int nchunk, const double *__restri
   y[r] = (beta == 0.0) ? alpha * s : alpha * s + beta * y[r];
 }
 
-// scratch for the row-major partials lives right after y's owner provides; we
-// allocate a small cached buffer per process for it.
-static double *g_gemv_part = nullptr;
-static size_t g_gemv_part_n = 0;
-
 void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, const double *A,
             int64_t lda, const double *x, double beta, double *y) {
   if (trans) {
@@ -713,18 +706,16 @@ void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, cons
   }
   if (M == 0) return;
   const int nchunk = (int)std::max<int64_t>(1, (N + GV_COLS - 1) / GV_COLS);
-  size_t need = (size_t)M * nchunk;
-  if (need > g_gemv_part_n) {
-    if (g_gemv_part) GPGP_CUDA(cudaFreeAsync(g_gemv_part, s));
-    GPGP_CUDA(cudaMallocAsync((void **)&g_gemv_part, need * sizeof(double), s));
-    g_gemv_part_n = need;
-  }
+  // partial sums of the column chunks: stream-ordered scratch of this call
+  double *part = nullptr;
+  GPGP_CUDA(cudaMallocAsync((void **)&part, (size_t)M * nchunk * sizeof(double), s));
   dim3 grid((unsigned)((M + GV_ROWS - 1) / GV_ROWS), (unsigned)nchunk);
-  gemv_n_kernel<<<grid, GV_ROWS, 0, s>>>(M, N, A, lda, x, g_gemv_part);
+  gemv_n_kernel<<<grid, GV_ROWS, 0, s>>>(M, N, A, lda, x, part);
   GPGP_CHECK_LAUNCH();
-  gemv_reduce_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(M, nchunk, g_gemv_part, alpha,
+  gemv_reduce_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(M, nchunk, part, alpha,
                                                                   beta, y);
   GPGP_CHECK_LAUNCH();
+  GPGP_CUDA(cudaFreeAsync(part, s));
 }
 
 // ---------------------------------------------------------------------------

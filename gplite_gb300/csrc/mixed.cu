@@ -591,14 +591,14 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
                      const int *status, int64_t status_bs, int64_t batch) {
   if (M <= 0 || N <= 0 || batch <= 0) return;
   if (A.S != B.S) throw CudaError{cudaErrorInvalidValue, "oz_gemm: operands split to different slice counts", __LINE__};
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    OzCfg<4>::SMEM + 1024));
     GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    OzCfg<5>::SMEM + 1024));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   OzGemmArgs g;
   g.a_sl = A.sl;
   g.a_ex = A.ex;

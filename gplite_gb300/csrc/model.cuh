@@ -203,4 +203,10 @@ gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, 
                       double *var);
 gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar);
 
+// Batched pipeline for the request server (batched.cu): one plan, one run, no
+// autotune or graph; lml[nprob], mean/var[sum m] packed in problem order.
+gpgp_status batch_solve_once(gpgp_ctx *ctx, const gpgp_batch_problem *probs, int32_t nprob,
+                             int32_t precision, double jitter, double *lml, double *mean, double *var);
+size_t batch_bytes_estimate(int64_t n, int64_t m, int32_t d, int32_t precision);
+
 }  // namespace gpgp

@@ -281,6 +281,72 @@ gpgp_status gpgp_batch_info(gpgp_batch *b, int32_t *nbuckets, int32_t *bucket_n,
                             int32_t *bucket_count, int32_t *bucket_variant, double *tune_ms);
 gpgp_status gpgp_batch_destroy(gpgp_batch *b);
 
+/* ---- request server: continuous batching of fit + predict requests -----
+ * Serves gp_fit (+ gp_pred with var) and gp_pred-on-a-resident-model requests
+ * that arrive one by one (the reference has no counterpart: it is one R call
+ * per fit). gpgp_server_submit copies the request's inputs and returns at
+ * once. Requests are admitted in arrival order while their device memory
+ * estimate fits the HBM budget (a later, smaller request may pass one that
+ * does not fit, until that one has waited 100 ms); a request larger than the
+ * whole budget fails with GPGP_EOOM. Admitted Gaussian full-method requests
+ * with one sexp / matern32 / matern52 term over all inputs and n <= batch_max_n
+ * join the batch lane: whatever has gathered while the previous batch ran is
+ * solved as the next batch (the batched pipeline, one launch sequence for all);
+ * the others (Laplace / EP likelihoods, FITC, compound kernels, large n) run on
+ * a pool of worker streams through gpgp_fit / gpgp_pred, overlapping on the
+ * device. keep = 1 leaves the fitted model resident (its memory stays counted
+ * against the budget) and returns its id for predict requests (model >= 0),
+ * until gpgp_server_release. Outputs: mean / var (m doubles each, caller-owned
+ * host memory that must stay valid until the request completes; var may be
+ * NULL). A request's results do not depend on what else is in flight. */
+typedef struct gpgp_server gpgp_server;
+typedef struct gpgp_server_opts {
+  int32_t device;
+  int32_t workers;       /* worker streams for non-batched requests (default 4) */
+  int64_t hbm_budget;    /* bytes for in-flight work and resident models (0: 80% of free) */
+  int32_t precision;     /* GPGP_PREC_FP64 or GPGP_PREC_MIXED, for every request */
+  int32_t batch_max_n;   /* largest n sent to the batch lane (default 1024, at most 4096) */
+  int32_t batch_max;     /* most requests in one batch (default 4096) */
+  double jitter;         /* added to K for every fit (default 1e-6 when <= 0) */
+} gpgp_server_opts;
+typedef struct gpgp_request {
+  const gpgp_kernel *kernel;
+  const gpgp_lik *lik;
+  const gpgp_method *method;   /* NULL: method_full */
+  const gpgp_approx *approx;   /* NULL: approx_laplace defaults */
+  const double *x;             /* n-by-d column-major */
+  int64_t n;
+  int32_t d;
+  const double *y, *trials, *offset; /* trials / offset may be NULL */
+  const double *xt;            /* m-by-d column-major */
+  int64_t m;
+  int32_t keep;                /* keep the fitted model resident */
+  int64_t model;               /* >= 0: predict with this resident model (fit fields unused) */
+  double *mean, *var;          /* outputs, m doubles each (var may be NULL) */
+} gpgp_request;
+typedef struct gpgp_request_result {
+  int32_t status;              /* gpgp_status of the request */
+  int32_t lane;                /* 0 batch lane, 1 worker stream */
+  double log_evidence;         /* fit requests */
+  int64_t model;               /* id of the resident model (keep = 1), else -1 */
+  double queue_ms, run_ms, total_ms; /* admission wait, service, submit -> done */
+} gpgp_request_result;
+typedef struct gpgp_server_stats {
+  int64_t submitted, completed, failed, pending, inflight;
+  int64_t batches, batched_requests;
+  int64_t bytes_inflight, bytes_resident, bytes_peak, budget;
+  double p50_ms, p99_ms, max_ms; /* total latency of the completed requests */
+} gpgp_server_stats;
+gpgp_status gpgp_server_create(const gpgp_server_opts *opts, gpgp_server **out);
+gpgp_status gpgp_server_submit(gpgp_server *s, const gpgp_request *req, int64_t *id);
+/* GPGP_OK with *res filled once the request is done (the id is then retired),
+ * GPGP_EBUSY while it is not after waiting up to wait_ms (< 0: until done). */
+gpgp_status gpgp_server_poll(gpgp_server *s, int64_t id, int32_t wait_ms, gpgp_request_result *res);
+gpgp_status gpgp_server_release(gpgp_server *s, int64_t model);
+gpgp_status gpgp_server_stats_get(gpgp_server *s, gpgp_server_stats *out);
+/* waits for every submitted request, then stops the lanes */
+gpgp_status gpgp_server_destroy(gpgp_server *s);
+
 /* ---- allocation-free Gaussian fit (no counterpart in the reference) ---
  * For callers that cannot allocate device memory while they need a fit: a
  * serving process whose own pool already owns all of HBM, a latency-critical

@@ -47,9 +47,11 @@ def test_struct_sizes_match_c(lib):
 #include <stddef.h>
 #include "gpgp.h"
 int main(void){
- printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(gpgp_cf_term), sizeof(gpgp_kernel), sizeof(gpgp_lik),
-  sizeof(gpgp_method), sizeof(gpgp_approx), sizeof(gpgp_fit_opts), sizeof(gpgp_fit_result),
-  offsetof(gpgp_cf_term, lscale));
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(gpgp_cf_term),
+  sizeof(gpgp_kernel), sizeof(gpgp_lik), sizeof(gpgp_method), sizeof(gpgp_approx), sizeof(gpgp_fit_opts),
+  sizeof(gpgp_fit_result), offsetof(gpgp_cf_term, lscale), sizeof(gpgp_batch_problem),
+  sizeof(gpgp_server_opts), sizeof(gpgp_request), offsetof(gpgp_request, model), sizeof(gpgp_request_result),
+  sizeof(gpgp_server_stats), offsetof(gpgp_server_stats, p50_ms));
  return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -59,7 +61,9 @@ int main(void){
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), p, "-o", exe], check=True)
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     got = [C.sizeof(L.CfTerm), C.sizeof(L.Kernel), C.sizeof(L.Lik), C.sizeof(L.Method),
-           C.sizeof(L.Approx), C.sizeof(L.FitOpts), C.sizeof(L.FitResult), L.CfTerm.lscale.offset]
+           C.sizeof(L.Approx), C.sizeof(L.FitOpts), C.sizeof(L.FitResult), L.CfTerm.lscale.offset,
+           C.sizeof(L.BatchProblem), C.sizeof(L.ServerOpts), C.sizeof(L.Request), L.Request.model.offset,
+           C.sizeof(L.RequestResult), C.sizeof(L.ServerStats), L.ServerStats.p50_ms.offset]
     assert [int(v) for v in out] == got
 
 
