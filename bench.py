@@ -255,7 +255,7 @@ def run_gpu(args):
     # x column-major on the device: the memory of a row-major (d, n) array
     xd = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
     yd = torch.from_numpy(y).cuda()
-    prec = L.PRECISION[args.precision]
+    prec = L.PRECISION["mixed" if args.precision == "both" else args.precision]
 
     def specs(theta):
         ls, mg, cm, sg = np.exp(theta)
@@ -314,66 +314,88 @@ def run_gpu(args):
         return float(t.item())
 
     stream = torch.cuda.ExternalStream(lib.gpgp_stream(ctx.h))
-    # warm-up
-    for k in range(args.warmup):
-        step_dev(k)
-    barrier()
-    # timed: device-resident inputs
-    lib.gpgp_profile_enable(ctx.h, 1)
-    launches0 = L.launch_count()
-    clk = ClockSampler(local)
-    clk.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    ev0.record(stream)
-    t0 = time.perf_counter()
-    lmls = []
-    for k in range(args.steps):
-        lmls.append(step_dev(args.warmup + k))
-    ev1.record(stream)
-    barrier()
-    wall = time.perf_counter() - t0
-    clocks = clk.stop()
-    dev_s = ev0.elapsed_time(ev1) / 1e3
-    launches = L.launch_count() - launches0
-    ms = np.zeros(8)
-    calls = np.zeros(8, dtype=np.int64)
-    lib.gpgp_profile_read(ctx.h, L.ptr(ms), calls.ctypes.data_as(C.c_void_p))
-    lib.gpgp_profile_enable(ctx.h, 0)
-    t_step = max_over_ranks(dev_s) / args.steps
-    value = world / t_step
 
-    # e2e through the host-buffer C ABI call (copies inside the timed region)
-    barrier()
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        step_host(args.warmup + k)
-    barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0) / args.steps
+    def measure(p):
+        """Warm-up, then K timed steps (device inputs, per-step CUDA events on the
+        library's stream), the phase and per-kernel timers, then K e2e steps."""
+        nonlocal prec
+        prec = L.PRECISION[p]
+        for k in range(args.warmup):
+            step_dev(k)
+        barrier()
+        lib.gpgp_profile_enable(ctx.h, 1)
+        launches0 = L.launch_count()
+        clk = ClockSampler(local)
+        clk.start()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        barrier()
+        evs[0].record(stream)
+        t0 = time.perf_counter()
+        lmls = []
+        for k in range(args.steps):
+            lmls.append(step_dev(args.warmup + k))
+            evs[k + 1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        clocks = clk.stop()
+        step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+        launches = L.launch_count() - launches0
+        ms = np.zeros(8)
+        calls = np.zeros(8, dtype=np.int64)
+        lib.gpgp_profile_read(ctx.h, L.ptr(ms), calls.ctypes.data_as(C.c_void_p))
+        kp = {}
+        for kid, name in ((0, "oz_gemm"), (1, "gemm64")):
+            nl, kms, kfl = C.c_int64(), C.c_double(), C.c_double()
+            lib.gpgp_kernel_profile_read(ctx.h, kid, C.byref(nl), C.byref(kms), C.byref(kfl))
+            kp[name] = dict(launches=nl.value, ms=kms.value, flops=kfl.value)
+        lib.gpgp_profile_enable(ctx.h, 0)
+        t_step = max_over_ranks(sum(step_ms) / 1e3) / args.steps
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step_host(args.warmup + k)
+        barrier()
+        e2e_s = max_over_ranks(time.perf_counter() - t0) / args.steps
+        phases = {nm: {"ms_total": float(ms[i]), "calls": int(calls[i])} for i, nm in enumerate(L.PHASES)}
+        return dict(t_step=t_step, step_ms=step_ms, lmls=lmls, launches=launches, phases=phases, kernels=kp,
+                    clocks=clocks, wall=wall, e2e_s=e2e_s, potrf_ms=float(ms[1]), potrf_calls=int(calls[1]))
+
+    precs = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+    res = {p: measure(p) for p in precs}
+    head = res[precs[0]]
+    value = world / head["t_step"]
     h2d = xf.nbytes + yh.nbytes
     d2h = 8 * (1 + gt.size + 1)
 
     out = None
     if rank == 0:
-        phases = {nm: {"ms_total": float(ms[i]), "calls": int(calls[i])} for i, nm in enumerate(L.PHASES)}
         peaks = measured_peaks()
-        if args.precision == "fp64":
-            fp64 = fp64_peak_gflops(torch)
-            t_potrf = ms[1] / max(calls[1], 1) / 1e3
-            achieved = (n ** 3 / 3) / t_potrf / 1e12
-            roof = {"bound": "fp64", "kernel": "blocked potrf (gemm64_kernel trailing updates)",
-                    "achieved": achieved, "peak": fp64 / 1e3, "unit": "TFLOP/s",
-                    "frac": achieved / (fp64 / 1e3),
-                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 is not in "
-                                   "MEASURED_PEAKS.json)",
+
+        def roofline(p):
+            r = res[p]
+            if p == "fp64":
+                fp64 = fp64_peak_gflops(torch) / 1e3
+                k = r["kernels"]["gemm64"]
+                ach = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+                return {"bound": "fp64", "kernel": "gemm64_kernel (FP64 trailing updates of potrf, "
+                                                   "trtri/lauum products)",
+                        "achieved": ach, "peak": fp64, "unit": "TFLOP/s", "frac": ach / fp64 if ach else None,
+                        "launches": k["launches"], "avg_launch_ms": k["ms"] / max(k["launches"], 1),
+                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 is not in "
+                                       "MEASURED_PEAKS.json)",
+                        "potrf_fp64_tflops": (n ** 3 / 3) / (r["potrf_ms"] / max(r["potrf_calls"], 1) / 1e3) / 1e12,
+                        "traffic": None}
+            k = r["kernels"]["oz_gemm"]
+            bf = peaks.get("bf16_tflops_sustained", 1700.0)
+            ach = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+            return {"bound": "tensor", "kernel": "oz_gemm_kernel<4> (BF16-sliced tcgen05 trailing updates)",
+                    "achieved": ach, "peak": bf, "unit": "TFLOP/s", "frac": ach / bf if ach else None,
+                    "launches": k["launches"], "avg_launch_ms": k["ms"] / max(k["launches"], 1),
+                    "peak_source": "of measured: MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed "
+                                   "inside a long step)",
+                    "potrf_fp64_equiv_tflops": (n ** 3 / 3) / (r["potrf_ms"] / max(r["potrf_calls"], 1) / 1e3) / 1e12,
                     "traffic": None}
-        else:
-            bf = peaks.get("bf16_tflops", 1900.0)
-            t_potrf = ms[1] / max(calls[1], 1) / 1e3
-            achieved = (n ** 3 / 3) / t_potrf / 1e12
-            roof = {"bound": "tensor", "kernel": "blocked potrf, mixed", "achieved": achieved, "peak": bf,
-                    "unit": "TFLOP/s", "frac": achieved / bf, "peak_source": "MEASURED_PEAKS.json bf16_tflops",
-                    "traffic": None}
+
         cpu = None
         if not args.no_cpu and world == 1:
             xs, ys = make_data(args.cpu_n, seed=2)
@@ -384,27 +406,37 @@ def run_gpu(args):
             cpu = {"value": 1.0 / (tc * sc), "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
                    "sample": "one oracle fit + numpy gradient at n=%d (R unavailable), time scaled by "
                              "(16384/%d)^3" % (args.cpu_n, args.cpu_n)}
+        sm = sorted(head["step_ms"])
         out = {
             "metric": "GP solves/s (energy+gradient, n=16384 full GP)", "value": value, "unit": "solves/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["t_step"] * 1e3,
+            "p50_ms": float(np.percentile(sm, 50)), "p99_ms": float(np.percentile(sm, 99)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64 (bf16-split tensor updates)",
+            "dtype": "f64" if precs[0] == "fp64" else "f64 (bf16-split tensor updates)",
             "data": "synthetic (numpy seeded; GP draw from matern52+const)",
             "config": {"workload": "full GP regression energy+gradient, n=%d d=8 matern52+const, "
-                                   "lik_gaussian sigma 0.05, fixed 20-step theta sequence" % n,
-                       "n": n, "d": D, "precision": args.precision,
+                                   "lik_gaussian sigma 0.05, fixed theta sequence" % n,
+                       "n": n, "d": D, "precision": precs[0],
                        "l2": "inputs larger than L2 (K and its factor are %.1f GB each)" % (n * n * 8 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+            "e2e": {"value": world / head["e2e_s"], "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": roof,
+            "roofline": roofline(precs[0]),
             "cpu_baseline": cpu,
-            "clocks": clocks,
-            "gpu_launches": int(launches),
-            "wall_s_timed": wall,
-            "phases_ms": phases,
-            "log_evidence_last": lmls[-1],
+            "clocks": head["clocks"],
+            "gpu_launches": int(head["launches"]),
+            "wall_s_timed": head["wall"],
+            "phases_ms": head["phases"],
+            "log_evidence_last": head["lmls"][-1],
         }
+        if "fp64" in res and precs[0] != "fp64":
+            f = res["fp64"]
+            rel = [abs(a - b) / abs(b) for a, b in zip(head["lmls"], f["lmls"])]
+            out["fp64_plain"] = {"value": world / f["t_step"], "ms_per_step": f["t_step"] * 1e3,
+                                 "e2e": world / f["e2e_s"], "roofline": roofline("fp64"),
+                                 "phases_ms": f["phases"], "clocks": f["clocks"]}
+            out["mixed_over_fp64"] = f["t_step"] / head["t_step"]
+            out["lml_rel_err_mixed_vs_fp64"] = max(rel)
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.barrier()
@@ -540,23 +572,198 @@ def run_batched(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# served stream: open-loop Poisson arrivals of fit+predict requests
+# ---------------------------------------------------------------------------
+
+def rff_draw(x, ls, rng, nfeat=64):
+    """A draw from an approximately sexp(ls, magn 1) GP: random Fourier features
+    (cos features with N(0, 1/ls^2) frequencies), O(n * nfeat) instead of a
+    Cholesky of K at every n up to 65536."""
+    w = rng.standard_normal((x.shape[1], nfeat)) / ls
+    b = rng.uniform(0, 2 * np.pi, nfeat)
+    return np.sqrt(2.0 / nfeat) * (np.cos(x @ w + b) @ rng.standard_normal(nfeat))
+
+
+def make_stream(rate=2000.0, window=2.0, seed=5, m=256, pool=48):
+    """Arrivals: Poisson(rate) over `window` s. Each request: n = round(exp(U[ln 32, ln 8192])),
+    d = 2, cf_sexp; 80% lik_gaussian, 20% lik_poisson (approx_laplace) with counts from
+    exp(GP draw); plus 5% method_fitc requests at n = 65536 with 256 random inducing points;
+    m = 256 prediction points. Inputs are prefixes of a seeded pool of full-size datasets
+    (x ~ U[-2,2]^2, an RFF draw of the latent), so the stream is cheap to build."""
+    rng = np.random.default_rng(seed)
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > window:
+            break
+        arrivals.append(t)
+    pools = []
+    for i in range(pool):
+        x = rng.uniform(-2, 2, (8192, 2))
+        ls = float(np.exp(rng.uniform(np.log(0.3), np.log(1.5))))
+        f = rff_draw(x, ls, rng)
+        pools.append((x, f, ls))
+    fitc_pool = []
+    for i in range(4):
+        x = rng.uniform(-2, 2, (65536, 2))
+        f = rff_draw(x, 0.7, rng)
+        fitc_pool.append((x, f))
+    xt = rng.uniform(-2, 2, (m, 2))
+    reqs = []
+    for t in arrivals:
+        u = rng.uniform()
+        if rng.uniform() < 0.05:
+            x, f = fitc_pool[rng.integers(len(fitc_pool))]
+            y = f + 0.1 * rng.standard_normal(len(f))
+            z = x[rng.choice(len(f), 256, replace=False)]
+            reqs.append(dict(t=t, kind="fitc", x=x, y=y, z=z, ls=0.7, sigma=0.1, xt=xt))
+            continue
+        n = int(round(np.exp(rng.uniform(np.log(32), np.log(8192)))))
+        x, f, ls = pools[rng.integers(len(pools))]
+        x, f = x[:n], f[:n]
+        if u < 0.8:
+            sig = float(rng.uniform(0.05, 0.3))
+            reqs.append(dict(t=t, kind="gaussian", x=x, y=f + sig * rng.standard_normal(n), ls=ls, sigma=sig, xt=xt))
+        else:
+            reqs.append(dict(t=t, kind="poisson", x=x, y=rng.poisson(np.exp(f)).astype(float), ls=ls, xt=xt))
+    return reqs
+
+
+def _gp_of(G, r):
+    cf = G.cf_sexp(lscale=r["ls"], magn=1.0)
+    if r["kind"] == "gaussian":
+        return G.gp_init(cf, G.lik_gaussian(sigma=r["sigma"]))
+    if r["kind"] == "poisson":
+        return G.gp_init(cf, G.lik_poisson())
+    return G.gp_init(cf, G.lik_gaussian(sigma=r["sigma"]), method=G.method_fitc(inducing=r["z"]))
+
+
+def replay(reqs, precision, workers, open_loop=True):
+    """Submit at the arrival times (open loop) from one thread, collect from another."""
+    import gplite_gb300 as G
+    from gplite_gb300.server import GPServer
+    gps = [_gp_of(G, r) for r in reqs]
+    out = [None] * len(reqs)
+    with GPServer(precision=precision, workers=workers) as s:
+        tickets = [None] * len(reqs)
+        ready = threading.Semaphore(0)
+
+        def collect():
+            for i in range(len(reqs)):
+                ready.acquire()
+                out[i] = s.poll(tickets[i], wait_ms=-1)
+        th = threading.Thread(target=collect)
+        th.start()
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            if open_loop:
+                dt = r["t"] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+            tickets[i] = s.submit(gps[i], r["x"], r["y"], r["xt"])
+            ready.release()
+        th.join()
+        wall = time.perf_counter() - t0
+        st = s.stats()
+    return out, wall, st
+
+
+def run_served(args):
+    import torch
+    from gplite_gb300 import _lib as L
+    reqs = make_stream(window=args.window)
+    warm = make_stream(window=0.05, seed=50)
+    flops = 0.0
+    for r in reqs:
+        n = len(r["y"])
+        if r["kind"] == "fitc":
+            flops += 2 * n * 256 ** 2 + 2 * 256 ** 3 / 3 + 2 * 256 * 256 * n
+        else:
+            it = 1 if r["kind"] == "gaussian" else 6
+            flops += it * n ** 3 / 3 + 256 * n * n
+    res = {}
+    clocks = ClockSampler()
+    for prec in ("mixed", "fp64"):
+        replay(warm, prec, args.workers)
+        torch.cuda.synchronize()
+        l0 = L.launch_count()
+        if prec == "mixed":
+            clocks.start()
+        out, wall, st = replay(reqs, prec, args.workers)
+        if prec == "mixed":
+            clk = clocks.stop()
+        lat = np.array([o["total_ms"] for o in out])
+        res[prec] = dict(out=out, wall=wall, stats=st, launches=L.launch_count() - l0,
+                         solves=len(reqs) / wall, p50=float(np.percentile(lat, 50)),
+                         p99=float(np.percentile(lat, 99)),
+                         failed=int(sum(o["status"] not in (0, 1) for o in out)))
+    # the plain FP64 path: the same requests one at a time through gp_fit + gp_pred
+    import gplite_gb300 as G
+    sample = reqs[::max(1, len(reqs) // 400)]
+    t0 = time.perf_counter()
+    done = 0
+    for r in sample:
+        gp = G.gp_fit(_gp_of(G, r), r["x"], r["y"], precision="fp64")
+        G.gp_pred(gp, r["xt"], var=True)
+        done += 1
+        if time.perf_counter() - t0 > args.plain_budget:
+            break
+    plain = done / (time.perf_counter() - t0)
+    ns = np.array([len(r["y"]) for r in reqs], dtype=np.float64)
+    a = np.array([o["log_evidence"] for o in res["mixed"]["out"]])
+    b = np.array([o["log_evidence"] for o in res["fp64"]["out"]])
+    ok = np.isfinite(a) & np.isfinite(b)
+    rel = np.abs(a[ok] - b[ok]) / np.maximum(np.abs(b[ok]), ns[ok])
+    m = res["mixed"]
+    line = {
+        "metric": "GP solves/s + p99 ms (served stream: Poisson 2000 req/s fit+predict 256)",
+        "value": m["solves"], "unit": "requests/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": m["wall"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (bf16-split tensor updates)", "data": "synthetic (seeded Poisson trace, RFF GP draws)",
+        "config": {"workload": "served stream: Poisson arrivals 2000 req/s for %.1f s, n log-uniform [32,8192], "
+                               "d=2, sexp, 80%% gaussian / 20%% poisson-laplace, +5%% fitc n=65536 M=256, m=256"
+                               % args.window, "requests": len(reqs), "workers": args.workers},
+        "p50_ms": m["p50"], "p99_ms": m["p99"],
+        "fp64_server": {"requests_per_s": res["fp64"]["solves"], "p50_ms": res["fp64"]["p50"],
+                        "p99_ms": res["fp64"]["p99"]},
+        "plain_fp64_requests_per_s": plain,
+        "plain_fp64_sample": "%d requests, every %dth of the stream" % (done, max(1, len(reqs) // 400)),
+        "mixed_over_plain_fp64": m["solves"] / plain,
+        "mixed_over_fp64_server": m["solves"] / res["fp64"]["solves"],
+        "offered_tflops": flops / args.window / 1e12, "served_fp64_equiv_tflops": flops / m["wall"] / 1e12,
+        "lml_rel_err_mixed_vs_fp64": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                      "norm": "max(|LML|, n)"},
+        "failed": m["failed"], "batches": m["stats"]["batches"],
+        "batched_requests": m["stats"]["batched_requests"], "bytes_peak": m["stats"]["bytes_peak"],
+        "clocks": clk, "gpu_launches": int(m["launches"]),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
     ap.add_argument("--n", type=int, default=N_FULL)
     ap.add_argument("--cpu-n", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batched"])
+    ap.add_argument("--workload", default="full", choices=["full", "batched", "served"])
+    ap.add_argument("--window", type=float, default=2.0)
+    ap.add_argument("--workers", type=int, default=6)
+    ap.add_argument("--plain-budget", type=float, default=40.0)
     ap.add_argument("--batch-count", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_gpu(args)
 
 

@@ -110,6 +110,7 @@ SIGNATURES = {
     "gpgp_stream": (_P, [_P]),
     "gpgp_profile_enable": (C.c_int, [_P, C.c_int32]),
     "gpgp_profile_read": (C.c_int, [_P, _P, _P]),
+    "gpgp_kernel_profile_read": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "gpgp_cf_sexp": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_int32, _P]),
     "gpgp_cf_matern32": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_int32, _P]),
     "gpgp_cf_matern52": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_int32, _P]),

@@ -161,14 +161,14 @@ __global__ void refine_residual_kernel(int64_t n, const double *__restrict__ rhs
 }
 
 int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
-                         double *fnew, double *logdetL) {
+                         double *fnew, double *logdetL, bool force_fp64 = false) {
   gpgp_ctx *ctx = m->ctx;
   cudaStream_t st = ctx->stream;
   const int64_t n = m->n;
   GPGP_CUDA(cudaMemsetAsync(w.status.p, 0, sizeof(int), st));
   vec_rsqrt(st, n, m->V.p, m->s.p);
   make_B(st, w.K.p, n, m->s.p, m->L.p);
-  const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
+  const bool mixed = !force_fp64 && m->opts.precision == GPGP_PREC_MIXED;
   {
     Phase ph(ctx, GPGP_PHASE_POTRF);
     if (mixed)
@@ -207,6 +207,15 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   GPGP_CUDA(cudaStreamSynchronize(st));
   m->have_binv_diag = false;
   m->have_Linv = false;
+  if (hstatus != 0 && mixed) {
+    // The sliced trailing updates carry an error of ~2^-33 of the largest entries
+    // of B; when B's entries are large (big Laplace weights W) and a pivot is
+    // small, that can break the factorisation of a matrix that is positive
+    // definite in FP64. Redo this factorisation on the FP64 pipe, whose
+    // verdict is the reference's.
+    ++m->fp64_fallbacks;
+    return factor_and_solve(m, w, zvec, alpha, fnew, logdetL, true);
+  }
   return hstatus;
 }
 
@@ -587,7 +596,21 @@ gpgp_status gpgp_profile_enable(gpgp_ctx *ctx, int32_t on) {
       ctx->prof_ms[i] = 0.0;
       ctx->prof_calls[i] = 0;
     }
+    ctx->kt.reset();
     ctx->prof = on != 0;
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_kernel_profile_read(gpgp_ctx *ctx, int32_t kernel, int64_t *launches, double *ms,
+                                     double *flops) {
+  if (!ctx || kernel < 0 || kernel >= GPGP_NKPROF) return GPGP_EINVAL;
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    ctx->kt.collect();
+    if (launches) *launches = ctx->kt.launches[kernel];
+    if (ms) *ms = ctx->kt.ms[kernel];
+    if (flops) *flops = ctx->kt.flops[kernel];
     return GPGP_OK;
   });
 }

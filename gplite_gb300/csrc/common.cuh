@@ -36,6 +36,26 @@ extern thread_local bool tl_capturing;
   do {                                                                                 \
     if (!::gpgp::tl_capturing) ::gpgp::g_launches.fetch_add(1, std::memory_order_relaxed); \
   } while (0)
+// Per-kernel timers (gpgp_kernel_profile_read): the API entry points bind the
+// context's timer to the calling thread while profiling is on; KTScope
+// brackets one launch with events and adds its executed arithmetic.
+struct KernelTimer {
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+  double ms[GPGP_NKPROF] = {0};
+  double flops[GPGP_NKPROF] = {0};
+  int64_t launches[GPGP_NKPROF] = {0};
+  void collect();
+  void reset();
+};
+extern thread_local KernelTimer *tl_kt;
+struct KTScope {
+  cudaStream_t s;
+  int k;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KTScope(int kernel, cudaStream_t st, double flops);
+  ~KTScope();
+};
+
 #define GPGP_CHECK_LAUNCH()              \
   do {                                   \
     GPGP_LAUNCHED();                     \

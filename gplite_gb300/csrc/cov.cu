@@ -15,6 +15,46 @@ namespace gpgp {
 
 std::atomic<int64_t> g_launches{0};
 thread_local bool tl_capturing = false;
+thread_local KernelTimer *tl_kt = nullptr;
+
+KTScope::KTScope(int kernel, cudaStream_t st, double flops) : s(st), k(kernel) {
+  if (!tl_kt || tl_capturing) return;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    (void)cudaGetLastError();
+    a = b = nullptr;
+    return;
+  }
+  cudaEventRecord(a, s);
+  tl_kt->flops[k] += flops;
+  tl_kt->launches[k] += 1;
+}
+
+KTScope::~KTScope() {
+  if (!a) return;
+  cudaEventRecord(b, s);
+  tl_kt->ev.push_back({k, {a, b}});
+}
+
+void KernelTimer::collect() {
+  for (auto &e : ev) {
+    float t = 0.f;
+    cudaEventSynchronize(e.second.second);
+    cudaEventElapsedTime(&t, e.second.first, e.second.second);
+    ms[e.first] += t;
+    cudaEventDestroy(e.second.first);
+    cudaEventDestroy(e.second.second);
+  }
+  ev.clear();
+}
+
+void KernelTimer::reset() {
+  collect();
+  for (int i = 0; i < GPGP_NKPROF; ++i) {
+    ms[i] = 0;
+    flops[i] = 0;
+    launches[i] = 0;
+  }
+}
 
 static const double kPi = 3.14159265358979323846;
 

@@ -30,11 +30,14 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
                                                      const double *__restrict__ B, int64_t ldb,
                                                      double beta, double *__restrict__ C,
                                                      int64_t ldc, int lower_only, int tri_mode,
-                                                     int64_t sA, int64_t sB, int64_t sC) {
+                                                     int64_t sA, int64_t sB, int64_t sC, int64_t kchunk) {
   const int64_t bm = blockIdx.x, bn = blockIdx.y;
-  A += blockIdx.z * sA;  // batched: problem blockIdx.z
+  // blockIdx.z: the problem of a batch (strides sA, sB, sC), or with kchunk > 0 the
+  // K range [z kchunk, (z + 1) kchunk) of one product whose partial goes to C + z sC
+  A += blockIdx.z * sA;
   B += blockIdx.z * sB;
   C += blockIdx.z * sC;
+  int64_t kend = K;
   const int64_t row0 = bm * GBM, col0 = bn * GBN;
   if (lower_only && col0 > row0 + GBM - 1) return;
   __shared__ double As[GBK][GBM + 1];
@@ -48,7 +51,12 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
     for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
   int64_t kstart = 0;
   if (tri_mode == 1) kstart = (row0 / GBK) * GBK;  // W^T W with W lower: k >= row
-  for (int64_t k0 = kstart; k0 < K; k0 += GBK) {
+  if (kchunk > 0) {
+    const int64_t kb = (int64_t)blockIdx.z * kchunk;
+    kstart = kstart > kb ? kstart : kb;
+    kend = kb + kchunk < K ? kb + kchunk : K;
+  }
+  for (int64_t k0 = kstart; k0 < kend; k0 += GBK) {
     // load A tile: op(A) is M x K
 #pragma unroll
     for (int e = 0; e < (GBM * GBK) / 256; ++e) {
@@ -63,7 +71,7 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
       }
       int64_t gr = row0 + r, gk = k0 + kk;
       double v = 0.0;
-      if (gr < M && gk < K) v = TA ? A[gk + gr * lda] : A[gr + gk * lda];
+      if (gr < M && gk < kend) v = TA ? A[gk + gr * lda] : A[gr + gk * lda];
       As[kk][r] = v;
     }
     // load B tile: op(B) is K x N
@@ -80,7 +88,7 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
       }
       int64_t gc = col0 + c, gk = k0 + kk;
       double v = 0.0;
-      if (gc < N && gk < K) v = TB ? B[gc + gk * ldb] : B[gk + gc * ldb];
+      if (gc < N && gk < kend) v = TB ? B[gc + gk * ldb] : B[gk + gc * ldb];
       Bs[kk][c] = v;
     }
     __syncthreads();
@@ -112,6 +120,57 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int64_t M, int64_t N, int64
   }
 }
 
+// C = alpha sum_z P_z + beta C over the split-K partials (fixed order)
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int nz, const double *__restrict__ P,
+                                     double alpha, double beta, double *__restrict__ C, int64_t ldc,
+                                     int lower_only) {
+  const int64_t MN = M * N;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < MN;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx % M, c = idx / M;
+    if (lower_only && r < c) continue;
+    double s = 0.0;
+    for (int z = 0; z < nz; ++z) s += P[idx + z * MN];
+    double *dst = C + r + c * ldc;
+    *dst = (beta == 0.0) ? alpha * s : alpha * s + beta * *dst;
+  }
+}
+
+template <bool TA, bool TB>
+static void launch_gemm64(cudaStream_t s, dim3 grid, int64_t M, int64_t N, int64_t K, double alpha,
+                          const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                          int64_t ldc, int lo, int tri_mode, int64_t sA, int64_t sB, int64_t sC, int64_t kchunk) {
+  double fl = 0.0;
+  if (tl_kt) {  // executed FP64 arithmetic of the tiles this launch runs
+    for (int64_t bm = 0; bm < (int64_t)grid.x; ++bm)
+      for (int64_t bn = 0; bn < (int64_t)grid.y; ++bn) {
+        const int64_t row0 = bm * GBM, col0 = bn * GBN;
+        if (lo && col0 > row0 + GBM - 1) continue;
+        const int64_t ks = tri_mode == 1 ? (row0 / GBK) * GBK : 0;
+        fl += 2.0 * GBM * GBN * (double)std::max<int64_t>(0, K - ks);
+      }
+    if (kchunk == 0) fl *= (double)grid.z;
+  }
+  KTScope kts(GPGP_KPROF_GEMM64, s, fl);
+  gemm64_kernel<TA, TB><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA,
+                                             sB, sC, kchunk);
+  GPGP_CHECK_LAUNCH();
+}
+
+static void gemm64_dispatch(cudaStream_t s, bool ta, bool tb, dim3 grid, int64_t M, int64_t N, int64_t K,
+                            double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
+                            double beta, double *C, int64_t ldc, int lo, int tri_mode, int64_t sA, int64_t sB,
+                            int64_t sC, int64_t kchunk) {
+  if (!ta && !tb)
+    launch_gemm64<false, false>(s, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, kchunk);
+  else if (!ta && tb)
+    launch_gemm64<false, true>(s, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, kchunk);
+  else if (ta && !tb)
+    launch_gemm64<true, false>(s, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, kchunk);
+  else
+    launch_gemm64<true, true>(s, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, kchunk);
+}
+
 void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
                     const double *A, int64_t lda, int64_t sA, const double *B, int64_t ldb, int64_t sB,
                     double beta, double *C, int64_t ldc, int64_t sC, int64_t batch, bool lower_only,
@@ -119,15 +178,26 @@ void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int6
   if (M <= 0 || N <= 0 || batch <= 0) return;
   dim3 grid((unsigned)((M + GBM - 1) / GBM), (unsigned)((N + GBN - 1) / GBN), (unsigned)batch);
   int lo = lower_only ? 1 : 0;
-  if (!ta && !tb)
-    gemm64_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
-  else if (!ta && tb)
-    gemm64_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
-  else if (ta && !tb)
-    gemm64_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
-  else
-    gemm64_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC);
-  GPGP_CHECK_LAUNCH();
+  const int64_t tiles = (int64_t)grid.x * grid.y;
+  // few output tiles and a long K (Gram matrices of tall n x M factors): split K
+  // over the third grid axis so that every SM gets work, then reduce the
+  // partials in a fixed order
+  if (batch == 1 && tiles < 152 && K >= 4096) {
+    int64_t nz = std::min<int64_t>((2 * 152 + tiles - 1) / tiles, K / 1024);
+    const int64_t kchunk = ((K + nz - 1) / nz + GBK - 1) / GBK * GBK;
+    nz = (K + kchunk - 1) / kchunk;
+    double *P = nullptr;
+    GPGP_CUDA(cudaMallocAsync((void **)&P, (size_t)nz * M * N * sizeof(double), s));
+    dim3 g2(grid.x, grid.y, (unsigned)nz);
+    gemm64_dispatch(s, ta, tb, g2, M, N, K, 1.0, A, lda, B, ldb, 0.0, P, M, 0, tri_mode, 0, 0, M * N, kchunk);
+    const int64_t MN = M * N;
+    splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((MN + 255) / 256, 4096), 256, 0, s>>>(
+        M, N, (int)nz, P, alpha, beta, C, ldc, lo);
+    GPGP_CHECK_LAUNCH();
+    GPGP_CUDA(cudaFreeAsync(P, s));
+    return;
+  }
+  gemm64_dispatch(s, ta, tb, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, 0);
 }
 
 void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,

@@ -230,29 +230,12 @@ void rows_times_cminv(gpgp_model *m, const double *B, double *X, int64_t n) {
   tri_rows(st, f.Lm.p, f.M, f.M, X, n, X, n, n, 1);
 }
 
-// U^T B for U = Kxz, B both n x M: FP64 GEMM or the sliced tensor-core GEMM
+// U^T B for U = Kxz, B both n x M, on the FP64 pipe in both precisions: the
+// lemma's C_m inherits K_z's conditioning (~1e4 and more), so BF16-sliced
+// products move its log-determinant by ~1e-5 relative at n = 65536, and the
+// Gram (2 n M^2 flops, split over K) is a small part of a FITC fit anyway.
 void gram_tn(gpgp_model *m, const double *A, const double *B, int64_t n, int64_t M, double *C) {
-  cudaStream_t st = m->ctx->stream;
-  if (m->opts.precision == GPGP_PREC_MIXED && n >= 1024) {
-    // operand rows are the columns of A and B (trans = 1 on a column-major n x M matrix)
-    const size_t ba = oz_split_bytes(M, n);
-    void *pa = nullptr, *pb = nullptr;
-    if (cudaMallocAsync(&pa, ba, st) != cudaSuccess || cudaMallocAsync(&pb, ba, st) != cudaSuccess) {
-      (void)cudaGetLastError();
-      if (pa) cudaFreeAsync(pa, st);
-      throw std::bad_alloc();
-    }
-    OzSplit sa, sb;
-    oz_split_bind(pa, M, n, &sa);
-    oz_split_bind(pb, M, n, &sb);
-    oz_split(st, A, n, 1, M, n, &sa);
-    oz_split(st, B, n, 1, M, n, &sb);
-    oz_gemm(st, sa, 0, sb, 0, M, M, 0, sa.nkb, 0, 1.0, 0.0, C, M, false, m->errflag.p);
-    cudaFreeAsync(pa, st);
-    cudaFreeAsync(pb, st);
-  } else {
-    gemm64(st, true, false, M, M, n, 1.0, A, n, B, n, 0.0, C, M);
-  }
+  gemm64(m->ctx->stream, true, false, M, M, n, 1.0, A, n, B, n, 0.0, C, M);
 }
 
 // The lemma for the current S (R/linear_algebra.R:3-43): iDU = Kxz / S, C_m and its

@@ -628,14 +628,34 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   g.b_bs_ex = B.bstride_ex;
   g.c_bs = sC;
   g.status_bs = status_bs;
-  if (A.S == 5) {
-    dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OzCfg<5>::BN - 1) / OzCfg<5>::BN),
-              (unsigned)batch);
-    oz_gemm_kernel<5><<<grid, 256, OzCfg<5>::SMEM + 1024, s>>>(g);
-  } else {
-    dim3 grid((unsigned)((M + OZ_BM - 1) / OZ_BM), (unsigned)((N + OzCfg<4>::BN - 1) / OzCfg<4>::BN),
-              (unsigned)batch);
-    oz_gemm_kernel<4><<<grid, 256, OzCfg<4>::SMEM + 1024, s>>>(g);
+  {
+    // executed MMA arithmetic of the tiles this launch runs (the kernel's own tile
+    // skipping and K ranges), for the per-kernel timer
+    const int BN = A.S == 5 ? OzCfg<5>::BN : OzCfg<4>::BN;
+    const int prods = A.S == 5 ? 19 : 13;
+    const int64_t gx = (M + OZ_BM - 1) / OZ_BM, gy = (N + BN - 1) / BN;
+    double fl = 0.0;
+    if (tl_kt) {
+      for (int64_t bx = 0; bx < gx; ++bx)
+        for (int64_t by = 0; by < gy; ++by) {
+          const int64_t row0 = bx * OZ_BM, col0 = by * BN;
+          if (lower_only && col0 > row0 + OZ_BM - 1) continue;
+          const int64_t grow0 = g.a_rb0 * OZ_TR + row0, gcol0 = g.b_rb0 * OZ_TR + col0;
+          int64_t k0 = kc0, k1 = kc1;
+          if (kmode == 1) k0 = std::max(k0, std::max(grow0, gcol0) / OZ_TK);
+          if (kmode == 2) k0 = std::max(k0, gcol0 / OZ_TK);
+          if (kmode == 3) k1 = std::min(k1, (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK);
+          if (k1 > k0) fl += 2.0 * OZ_BM * BN * OZ_TK * (double)(k1 - k0) * prods;
+        }
+    }
+    KTScope kts(GPGP_KPROF_OZ_GEMM, s, fl * (double)batch);
+    if (A.S == 5) {
+      dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch);
+      oz_gemm_kernel<5><<<grid, 256, OzCfg<5>::SMEM + 1024, s>>>(g);
+    } else {
+      dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch);
+      oz_gemm_kernel<4><<<grid, 256, OzCfg<4>::SMEM + 1024, s>>>(g);
+    }
   }
   GPGP_CHECK_LAUNCH();
 }

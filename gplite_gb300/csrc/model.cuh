@@ -20,6 +20,7 @@ struct gpgp_ctx {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
   double prof_ms[GPGP_NPHASE] = {0};
   int64_t prof_calls[GPGP_NPHASE] = {0};
+  gpgp::KernelTimer kt;
 };
 
 namespace gpgp {
@@ -148,6 +149,7 @@ struct gpgp_model {
   bool has_trials = false, has_offset = false;
   double log_evidence = 0.0;
   int fitted = 0;
+  int64_t fp64_fallbacks = 0;  // mixed factorisations redone in FP64 after a breakdown
 };
 
 namespace gpgp {
@@ -160,8 +162,16 @@ inline gpgp_status fail(gpgp_ctx *ctx, gpgp_status st, const std::string &msg) {
   return st;
 }
 
+// binds the context's kernel timer to this thread for one API call
+struct KTBind {
+  KernelTimer *prev;
+  explicit KTBind(gpgp_ctx *ctx) : prev(tl_kt) { tl_kt = (ctx && ctx->prof) ? &ctx->kt : nullptr; }
+  ~KTBind() { tl_kt = prev; }
+};
+
 template <class F>
 gpgp_status guarded(gpgp_ctx *ctx, F &&fn) {
+  KTBind bind(ctx);
   try {
     return fn();
   } catch (const CudaError &e) {

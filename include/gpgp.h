@@ -184,6 +184,20 @@ typedef enum gpgp_phase {
 } gpgp_phase;
 gpgp_status gpgp_profile_enable(gpgp_ctx *ctx, int32_t on);
 gpgp_status gpgp_profile_read(gpgp_ctx *ctx, double *ms, int64_t *calls);
+/* Per-kernel timing of the dense contractions (instrumentation, no
+ * counterpart in the reference): while profiling is on, each launch of these
+ * kernels made through this context is bracketed by CUDA events on the
+ * context stream. Read per kernel: launches, total device ms, and the
+ * arithmetic the launches executed (tensor-core GEMM: BF16 MMA flops of all
+ * slice products of the tiles it ran; FP64 GEMM: 2 x tile area x K of the
+ * tiles it ran). Reset by gpgp_profile_enable. */
+typedef enum gpgp_kprof_kernel {
+  GPGP_KPROF_OZ_GEMM = 0,  /* BF16-sliced tcgen05 GEMM (mixed precision) */
+  GPGP_KPROF_GEMM64 = 1,   /* FP64 GEMM / SYRK (plain precision) */
+  GPGP_NKPROF = 2
+} gpgp_kprof_kernel;
+gpgp_status gpgp_kernel_profile_read(gpgp_ctx *ctx, int32_t kernel, int64_t *launches, double *ms,
+                                     double *flops);
 
 /* ---- covariance routines: replace src/cf.cpp:9-162 (registered at
  *      src/RcppExports.cpp:76-87). Host buffers; x1 n1-by-d, x2 n2-by-d
