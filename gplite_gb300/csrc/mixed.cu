@@ -2,24 +2,29 @@
 // tensor cores through exact BF16 slicing (an Ozaki-style split).
 //
 // Every operand row is scaled by a power of two so that its largest entry is
-// in [0.5, 1) and then cut into four 8-bit fixed-point slices
-//   x = 2^e * sum_t q_t 2^-8(t+1),  q_t integers in [-256, 256]
-// which BF16 holds exactly. A product of two slices is an integer below 2^16,
-// so the level-0 and level-1 dot products of up to 256 terms stay below 2^24
-// and the FP32 accumulators of tcgen05.mma hold them exactly. The 13 slice
-// pairs with t + u <= 4 go into five level accumulators in TMEM; after every
-// 256-wide K group the levels are added into double-float (hi, lo) FP32
-// registers, and the result is written once in FP64:
-//   (A B^T)_ij = 2^(e_i + f_j - 16) sum_l 2^-8l P_l.
-// The truncation error is ~2^-33 of the row maxima, far below what the FP64
-// log-determinant and iterative refinement need for 1e-8 evidence accuracy.
+// in [0.5, 1) and then cut into S 8-bit fixed-point slices (S = 4 or 5)
+//   x = 2^e * sum_t q_t 2^-8(t+1),  q_t integers in [-256, 256].
+// Slice t is stored as the BF16 value q_t 2^-8t (exact: an 8-bit integer times
+// a power of two), so the product of slices t and u already carries its level
+// weight 2^-8(t+u) and products of different levels can share an accumulator.
+// Levels 0, 1 and 2 get their own FP32 accumulators in TMEM, levels 3.. share
+// a fourth: a level-l sum of up to 256 products has 24 significant bits for
+// l <= 2, so those sums are exact in FP32; the shared deeper levels round at
+// 2^-50 of the result. After every 256-wide K group the four accumulators are
+// added into a double-float (hi, lo) pair and applied to C in FP64:
+//   (A B^T)_ij = 2^(e_i + f_j - 16) (P_0 + P_1 + P_2 + P_3+).
+// The truncation error is ~2^-(8S+1) of the row maxima.
 //
 // Data path: slices are stored pre-tiled in the canonical no-swizzle K-major
-// UMMA layout (8-row x 16-byte core matrices), so one cp.async.bulk per slice
-// tile moves them to shared memory; one elected thread issues the MMAs and a
-// tcgen05.commit arrives on an mbarrier; all eight warps drain TMEM with
-// tcgen05.ld. Every wait is bounded: on timeout the kernel records an error,
-// releases TMEM and returns.
+// UMMA layout (8-row x 16-byte core matrices, 64-row x 32-K tiles), so one
+// cp.async.bulk per slice moves a chunk to shared memory. The GEMM kernel is
+// persistent and warp-specialised: a producer warp streams K chunks of the
+// CTA's output tiles through a ring of shared-memory stages, an MMA warp
+// issues tcgen05.mma into one of two TMEM accumulator sets and commits to
+// mbarriers, and four epilogue warps drain the other set with tcgen05.ld and
+// update C in FP64 while the next group accumulates. Every wait is bounded: on
+// timeout the kernel records an error, drains what it issued, releases TMEM
+// and returns.
 #include <math.h>
 #include <stdint.h>
 
@@ -29,39 +34,35 @@
 
 namespace gpgp {
 
-constexpr int OZ_TK = 64;           // K chunk
-// Chunks accumulated in TMEM before a flush: level-0 and level-1 sums stay below
-// 2^24 (exact in FP32) for 4 x 64 = 256 products; deeper levels may round, but
-// their rounding is below 2^-40 of the result.
-constexpr int OZ_GROUP = 4;
-constexpr int OZ_TR = 64;           // rows per slice tile
-constexpr int OZ_TILE = OZ_TR * OZ_TK;  // bf16 elements per slice tile (8 KB)
-constexpr int OZ_BM = 128;
+constexpr int OZ_TK = 32;               // K chunk (one pipeline stage)
+constexpr int OZ_GROUP = 8;             // chunks per exactly accumulated group (K = 256)
+constexpr int OZ_TR = 64;               // rows per slice tile
+constexpr int OZ_TILE = OZ_TR * OZ_TK;  // bf16 elements per slice tile (4 KB)
+constexpr int OZ_BM = 128, OZ_BN = 64;  // output tile
+constexpr int OZ_NACC = 4;              // accumulators: levels 0, 1, 2, >= 3
+constexpr int OZ_EPI_WARPS = 16;  // four per TMEM lane quarter, 16 columns each
+constexpr int OZ_EPI_COLS = OZ_BN / (OZ_EPI_WARPS / 4);
+constexpr int OZ_THREADS = 32 * (2 + OZ_EPI_WARPS);  // producer, MMA, epilogue
 
 // S slices per operand (8S-bit fixed point): levels t + u <= S are kept
-// (S = 4: 13 products, truncation 2^-33; S = 5: 19 products, 2^-41). The
-// tile is 128 x 64 for S = 4 and 128 x 32 for S = 5 so that two pipeline
-// stages of operands fit in shared memory.
+// (S = 4: 13 products, truncation 2^-33; S = 5: 19 products, 2^-41).
 template <int S>
 struct OzCfg {
-  static constexpr int LEVELS = S + 1;
-  static constexpr int BN = S == 4 ? 64 : 32;
-  static constexpr int A_STAGE = S * 2 * OZ_TILE * 2;  // S slices x 128 rows x 64 K x 2 B
-  static constexpr int B_TILE = BN * OZ_TK * 2;        // one slice of BN rows
-  static constexpr int B_STAGE = S * B_TILE;
-  static constexpr int STAGE = A_STAGE + B_STAGE;
-  static constexpr int SMEM = 2 * STAGE + 1024;
-  static constexpr uint32_t TMEM_COLS = LEVELS * BN <= 256 ? 256u : 512u;
-  static constexpr int CPT = BN / 2;  // accumulator columns per epilogue thread
+  static constexpr int A_SL = OZ_BM * OZ_TK * 2;  // bytes of one A slice chunk (8 KB)
+  static constexpr int B_SL = OZ_BN * OZ_TK * 2;  // 4 KB
+  static constexpr int STAGE = S * (A_SL + B_SL);
+  static constexpr int NST = S == 4 ? 4 : 3;      // pipeline stages
+  static constexpr int SMEM = NST * STAGE + 1024 + 1024;  // + barriers + alignment
+  static constexpr uint32_t TMEM_COLS = 2 * OZ_NACC * OZ_BN;  // two accumulator sets
 };
 
-
 // ---------------------------------------------------------------------------
-// split: FP64 rows -> 4 BF16 slices (canonical layout) + per-row exponents
+// split: FP64 rows -> S BF16 slices (canonical layout) + per-row exponents
 // ---------------------------------------------------------------------------
 // Element (r, k) of the logical rows x K operand is P[r + k*ld] (trans = 0)
-// or P[k + r*ld] (trans = 1). Tiles: [slice][kb][rb], 64 x 64 each; within a
-// tile, (r, k) lives at (r/8)*512 + (k/8)*64 + (r%8)*8 + (k%8) elements.
+// or P[k + r*ld] (trans = 1). Tiles: [slice][kc][rb], 64 rows x 32 K each
+// (kc counts 32-wide chunks, 2 per 64-wide K block); within a tile, (r, k)
+// lives at (r/8)*256 + (k/8)*64 + (r%8)*8 + (k%8) elements.
 __device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans, int64_t r,
                                           int64_t k, int64_t rows, int64_t K) {
   if (r >= rows || k >= K) return 0.0;
@@ -98,14 +99,14 @@ __global__ void oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int t
   }
 }
 
-// bf16 bits of the integer s * q, |q| <= 256
-__device__ __forceinline__ uint32_t bf16_of_digit(int q) {
+// bf16 bits of q 2^-8t, |q| <= 256 (exact: at most 8 significant bits)
+__device__ __forceinline__ uint32_t bf16_of_digit(int q, int t) {
   if (q == 0) return 0u;
   const uint32_t sgn = q < 0 ? 0x8000u : 0u;
   const uint32_t a = (uint32_t)(q < 0 ? -q : q);
   const int p = 31 - __clz(a);
   const uint32_t mant = p <= 7 ? ((a << (7 - p)) & 0x7Fu) : ((a >> (p - 7)) & 0x7Fu);
-  return sgn | ((uint32_t)(127 + p) << 7) | mant;
+  return sgn | ((uint32_t)(127 + p - 8 * t) << 7) | mant;
 }
 
 // 8S-bit fixed point |x| 2^8S (rounded to nearest) of x = P 2^-e, as balanced
@@ -145,7 +146,7 @@ __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int tr
   // thread per (row, 8-wide K group): writes 16 bytes per slice
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t rows_pad = nrb * OZ_TR;
-  const int64_t ngroups = nkb * (OZ_TK / 8);
+  const int64_t ngroups = nkb * (64 / 8);  // 8-wide K groups of the 64-padded K
   if (tid >= rows_pad * ngroups) return;
   const int64_t r = trans ? tid / ngroups : tid % rows_pad;
   const int64_t g = trans ? tid % ngroups : tid / rows_pad;
@@ -158,14 +159,14 @@ __global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int tr
     oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
     oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
 #pragma unroll
-    for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t]) | (bf16_of_digit(d1[t]) << 16);
+    for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t], t) | (bf16_of_digit(d1[t], t) << 16);
   }
   const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
-  const int64_t kb = k0 / OZ_TK, kk = k0 % OZ_TK;
-  const int64_t within = (rr / 8) * 512 + (kk / 8) * 64 + (rr % 8) * 8;
+  const int64_t kc = k0 / OZ_TK, kk = k0 % OZ_TK, nkc = 2 * nkb;
+  const int64_t within = (rr / 8) * 256 + (kk / 8) * 64 + (rr % 8) * 8;
 #pragma unroll
   for (int t = 0; t < S; ++t) {
-    const int64_t tile = ((int64_t)t * nkb + kb) * nrb + rb;
+    const int64_t tile = ((int64_t)t * nkc + kc) * nrb + rb;
     uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
     *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) = v;
   }
@@ -182,7 +183,7 @@ int64_t oz_nrb(int64_t rows) {
 void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, int trans, int64_t rows,
                       int64_t K, OzSplit *out, int64_t batch) {
   const int64_t nrb = oz_nrb(rows);
-  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
+  const int64_t nkb = (K + 63) / 64;
   out->rows = rows;
   out->K = K;
   out->nrb = nrb;
@@ -196,7 +197,7 @@ void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, i
     GPGP_CHECK_LAUNCH();
   }
   {
-    const int64_t threads = rows_pad * nkb * (OZ_TK / 8);
+    const int64_t threads = rows_pad * nkb * (64 / 8);
     dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);
     if (out->S == 5)
       oz_slice_kernel<5><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
@@ -213,8 +214,8 @@ void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t ro
 
 size_t oz_split_bytes(int64_t rows, int64_t K, int S) {
   const int64_t nrb = oz_nrb(rows);
-  const int64_t nkb = (K + OZ_TK - 1) / OZ_TK;
-  return (size_t)nrb * OZ_TR * sizeof(int) + 256 + (size_t)S * nkb * nrb * OZ_TILE * 2;
+  const int64_t nkb = (K + 63) / 64;
+  return (size_t)nrb * OZ_TR * sizeof(int) + 256 + (size_t)S * nkb * nrb * OZ_TR * 64 * 2;
 }
 
 void oz_split_bind(void *mem, int64_t rows, int64_t K, OzSplit *out, int S) {
@@ -312,6 +313,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(taddr));
+}
+
 template <int NC>
 __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[NC]) {
   if constexpr (NC == 32) tmem_ld32(taddr, r);
@@ -326,6 +334,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // float exponent is rebiased and sh added; zero and out-of-range cases take ldexp
 __device__ __forceinline__ double f2d_scaled(float f, int sh) {
   const uint32_t b = __float_as_uint(f);
+  if ((b << 1) == 0u) return 0.0;
   const uint32_t ef = (b >> 23) & 0xFFu;
   if (ef == 0u || ef == 0xFFu) return ldexp((double)f, sh);
   const int ed = (int)ef - 127 + 1023 + sh;
@@ -346,84 +355,106 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
 }
 
 // ---------------------------------------------------------------------------
-// the GEMM: C = alpha * A B^T + beta * C over the given K-chunk range
+// the GEMM: C = alpha * A B^T + beta * C over the given K range
 // ---------------------------------------------------------------------------
 struct OzGemmArgs {
   const uint16_t *a_sl;
   const int *a_ex;
-  int64_t a_nrb, a_nkb, a_rb0;  // slice-tile geometry; first 64-row tile of this operand
+  int64_t a_nrb, a_nkc, a_rb0;  // slice-tile geometry (32-wide K chunks); first 64-row tile
   const uint16_t *b_sl;
   const int *b_ex;
-  int64_t b_nrb, b_nkb, b_rb0;
+  int64_t b_nrb, b_nkc, b_rb0;
   int64_t M, N;
-  int64_t kc0, kc1;  // K chunks [kc0, kc1) of both operands
-  int kmode;         // 0 all; 1 start at max(row,col)/64; 2 start at col/64; 3 end at row/64 + 2
+  int64_t kc0, kc1;  // 32-wide K chunks [kc0, kc1) of both operands
+  int kmode;         // 0 all; 1 start at max(row,col); 2 start at col; 3 end after row
   double alpha, beta;
   double *C;
   int64_t ldc;
   int lower_only;
   int *err;
-  const int *status;  // optional: skip all work when a factorisation already failed
-  int64_t a_bs_sl, a_bs_ex, b_bs_sl, b_bs_ex, c_bs;  // batch strides (problem blockIdx.z)
+  const int *status;  // optional: skip a problem whose factorisation already failed
+  int64_t a_bs_sl, a_bs_ex, b_bs_sl, b_bs_ex, c_bs;  // per-problem strides
   int64_t status_bs;
+  int64_t gx, gy, batch;  // tile grid; tile L = (z gy + by) gx + bx
 };
 
-template <int S>
-__global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
-  using Cfg = OzCfg<S>;
-  constexpr int BN = Cfg::BN, CPT = Cfg::CPT;
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // align the dynamic shared memory base to 1024 bytes
-  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int64_t row0 = (int64_t)blockIdx.x * OZ_BM;
-  const int64_t col0 = (int64_t)blockIdx.y * BN;
-  if (g.lower_only && col0 > row0 + OZ_BM - 1) return;
-  const int64_t zb = blockIdx.z;
-  const uint16_t *a_sl = g.a_sl + zb * g.a_bs_sl;
-  const int *a_ex = g.a_ex + zb * g.a_bs_ex;
-  const uint16_t *b_sl = g.b_sl + zb * g.b_bs_sl;
-  const int *b_ex = g.b_ex + zb * g.b_bs_ex;
-  double *Cz = g.C + zb * g.c_bs;
+struct OzTile {
+  int64_t z, row0, col0, c0, nch;
+};
 
-  // K-chunk range of this tile
-  const int64_t grow0 = g.a_rb0 * OZ_TR + row0;  // absolute operand row of the tile
-  const int64_t gcol0 = g.b_rb0 * OZ_TR + col0;
-  int64_t kc0 = g.kc0, kc1 = g.kc1;
+// The work of tile L (identical in every role): false when the tile is skipped
+// (above the diagonal of a lower-only product, or its problem has failed)
+__device__ __forceinline__ bool oz_tile_at(const OzGemmArgs &g, int64_t L, OzTile &t) {
+  const int64_t per = g.gx * g.gy;
+  t.z = L / per;
+  const int64_t r = L - t.z * per;
+  const int64_t by = r / g.gx, bx = r - by * g.gx;
+  t.row0 = bx * OZ_BM;
+  t.col0 = by * OZ_BN;
+  if (g.lower_only && t.col0 > t.row0 + OZ_BM - 1) return false;
+  if (g.status && *(volatile const int *)(g.status + t.z * g.status_bs) != 0) return false;
+  const int64_t grow0 = g.a_rb0 * OZ_TR + t.row0, gcol0 = g.b_rb0 * OZ_TR + t.col0;
+  int64_t k0 = g.kc0, k1 = g.kc1;
   if (g.kmode == 1) {
     const int64_t s0 = (grow0 > gcol0 ? grow0 : gcol0) / OZ_TK;
-    kc0 = kc0 > s0 ? kc0 : s0;
+    k0 = k0 > s0 ? k0 : s0;
   }
   if (g.kmode == 2) {
     const int64_t s0 = gcol0 / OZ_TK;
-    kc0 = kc0 > s0 ? kc0 : s0;
+    k0 = k0 > s0 ? k0 : s0;
   }
   if (g.kmode == 3) {
     const int64_t e0 = (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK;
-    kc1 = kc1 < e0 ? kc1 : e0;
+    k1 = k1 < e0 ? k1 : e0;
   }
-  if (g.status && *(volatile const int *)(g.status + blockIdx.z * g.status_bs) != 0) return;
-  const int64_t nch = kc1 > kc0 ? kc1 - kc0 : 0;
+  t.c0 = k0;
+  t.nch = k1 > k0 ? k1 - k0 : 0;
+  return true;
+}
 
-  uint64_t *bars = (uint64_t *)(smem + 2 * Cfg::STAGE);
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait that also gives up when another role has aborted.
+__device__ __forceinline__ bool oz_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u && *abort_flag) return false;
+  }
+  return false;
+}
+
+template <int S>
+// 576 threads: the register cap keeps the block inside one SM's register file
+__global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
+  using Cfg = OzCfg<S>;
+  constexpr int NST = Cfg::NST;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + NST * Cfg::STAGE);
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
-  // full[s]: operands of the chunk in stage s landed; empty[s]: the MMAs that read
-  // stage s completed; flush: the MMAs of a flush group completed
-  const uint32_t full0 = smem_u32(&bars[0]), full1 = smem_u32(&bars[1]);
-  const uint32_t empty0 = smem_u32(&bars[2]), empty1 = smem_u32(&bars[3]);
-  const uint32_t flushb = smem_u32(&bars[4]);
-  if (tid == 0) {
-    mbar_init(full0, 1);
-    mbar_init(full1, 1);
-    mbar_init(empty0, 1);
-    mbar_init(empty1, 1);
-    mbar_init(flushb, 1);
+  volatile int *abort_flag = &abort_sh;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // barriers: full[NST] (operands landed), empty[NST] (MMAs that read a stage done),
+  // tfull[2] (an accumulator set is ready), tempty[2] (the epilogue drained it), drain
+  const int FULL = 0, EMPTY = NST, TFULL = 2 * NST, TEMPTY = 2 * NST + 2, DRAIN = 2 * NST + 4;
+  auto bar = [&](int i) { return smem_u32(&bars[i]); };
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NST; ++i) {
+      mbar_init(bar(FULL + i), 1);
+      mbar_init(bar(EMPTY + i), 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(bar(TFULL + i), 1);
+      mbar_init(bar(TEMPTY + i), OZ_EPI_WARPS);
+    }
+    mbar_init(bar(DRAIN), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_sh = 0;
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_sh)),
                  "r"(Cfg::TMEM_COLS));
@@ -433,156 +464,235 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(const OzGemmArgs g) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
-
-  // operand tile addresses for chunk c (global)
-  auto a_tile = [&](int s, int64_t kc) {
-    return a_sl + (((int64_t)s * g.a_nkb + kc) * g.a_nrb + g.a_rb0 + 2 * blockIdx.x) * OZ_TILE;
-  };
-  // a BN-row part of a 64-row slice tile is contiguous (rows are the outer index)
-  auto b_tile = [&](int s, int64_t kc) {
-    return b_sl + (((int64_t)s * g.b_nkb + kc) * g.b_nrb + g.b_rb0 + col0 / OZ_TR) * OZ_TILE +
-           (col0 % OZ_TR) * OZ_TK;
-  };
-  auto load_stage = [&](int st, int64_t kc) {
-    const uint32_t base = smem_u32(smem + st * Cfg::STAGE);
-    const uint32_t bar = st ? full1 : full0;
-    mbar_expect_tx(bar, Cfg::STAGE);
-    for (int s = 0; s < S; ++s) {
-      bulk_g2s(base + s * (2 * OZ_TILE * 2), a_tile(s, kc), 2 * OZ_TILE * 2, bar);
-      bulk_g2s(base + Cfg::A_STAGE + s * Cfg::B_TILE, b_tile(s, kc), Cfg::B_TILE, bar);
-    }
-  };
-
-  if (tid == 0 && nch > 0) load_stage(0, kc0);
-
-  // instruction descriptor: D F32, A/B BF16, K-major both, N = BN, M = 128
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                         ((uint32_t)(OZ_BM >> 4) << 24);
-  // no-swizzle K-major operands: 8 x 16-byte core matrices, the leading byte
-  // offset steps K (128 B), the stride byte offset steps 8 rows (1024 B)
-  const uint32_t lbo = 128u, sbo = 1024u;
-
-  // epilogue ownership: warp w reads TMEM lanes 32*(w%4).., columns CPT*(w/4)..
-  const int quarter = warp & 3, half = warp >> 2;
-  const int64_t my_row = row0 + quarter * 32 + lane;
-  float hi[CPT], lo[CPT];
+  const int64_t ntiles = g.gx * g.gy * g.batch;
+  int last_full_parity[NST];
 #pragma unroll
-  for (int c = 0; c < CPT; ++c) hi[c] = lo[c] = 0.f;
+  for (int i = 0; i < NST; ++i) last_full_parity[i] = -1;
+  bool mma_issued = false;
 
-  bool ok = true;
-  int nflush = 0;
-  for (int64_t c = 0; c < nch; ++c) {
-    const int st = (int)(c & 1);
-    const bool group_start = (c % OZ_GROUP) == 0;
-    const bool flush = ((c + 1) % OZ_GROUP) == 0 || c == nch - 1;
-    if (tid == 0) {
-      bool good = mbar_wait_bounded(st ? full1 : full0, (uint32_t)((c >> 1) & 1));
-      if (good) {
-        tc_fence_after();
-        const uint32_t abase = smem_u32(smem + st * Cfg::STAGE);
-        const uint32_t bbase = abase + Cfg::A_STAGE;
-        int first[Cfg::LEVELS];
+  if (warp == 0) {
+    // ---- producer: K chunks of this CTA's tiles into the stage ring ----
+    if (lane == 0) {
+      int st = 0;
+      uint32_t ph = 0;
+      for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x) {
+        OzTile t;
+        if (!oz_tile_at(g, L, t) || t.nch == 0) continue;
+        const uint16_t *a_sl = g.a_sl + t.z * g.a_bs_sl;
+        const uint16_t *b_sl = g.b_sl + t.z * g.b_bs_sl;
+        const int64_t arb = g.a_rb0 + t.row0 / OZ_TR, brb = g.b_rb0 + t.col0 / OZ_TR;
+        for (int64_t c = 0; c < t.nch; ++c) {
+          if (!oz_wait(bar(EMPTY + st), ph ^ 1u, abort_flag)) {
+            if (!*abort_flag) atomicExch(g.err, 1);
+            abort_sh = 1;
+            goto producer_done;
+          }
+          const uint32_t base = smem_u32(smem + st * Cfg::STAGE);
+          mbar_expect_tx(bar(FULL + st), Cfg::STAGE);
+          const int64_t kc = t.c0 + c;
 #pragma unroll
-        for (int l = 0; l < Cfg::LEVELS; ++l) first[l] = group_start ? 1 : 0;
-#pragma unroll
-        for (int t = 0; t < S; ++t) {
-#pragma unroll
-          for (int u = 0; u < S; ++u) {
-            const int lev = t + u;
-            if (lev >= Cfg::LEVELS) continue;
-#pragma unroll
-            for (int kk = 0; kk < OZ_TK / 16; ++kk) {
-              const uint64_t ad = umma_desc(abase + t * (2 * OZ_TILE * 2) + kk * 2 * 128, lbo, sbo);
-              const uint64_t bd = umma_desc(bbase + u * Cfg::B_TILE + kk * 2 * 128, lbo, sbo);
-              umma_bf16(tmem + lev * BN, ad, bd, idesc, first[lev] ? 0u : 1u);
-              first[lev] = 0;
-            }
+          for (int s = 0; s < S; ++s) {
+            bulk_g2s(base + s * Cfg::A_SL, a_sl + (((int64_t)s * g.a_nkc + kc) * g.a_nrb + arb) * OZ_TILE,
+                     Cfg::A_SL, bar(FULL + st));
+            bulk_g2s(base + S * Cfg::A_SL + s * Cfg::B_SL,
+                     b_sl + (((int64_t)s * g.b_nkc + kc) * g.b_nrb + brb) * OZ_TILE, Cfg::B_SL, bar(FULL + st));
+          }
+          last_full_parity[st] = (int)ph;
+          if (++st == NST) {
+            st = 0;
+            ph ^= 1u;
           }
         }
-        umma_commit(st ? empty1 : empty0);
-        if (flush) umma_commit(flushb);
-        // refill the other stage with chunk c + 1 once the MMAs of chunk c - 1 are done
-        if (c + 1 < nch) {
-          if (c >= 1) good = mbar_wait_bounded(st ? empty0 : empty1, (uint32_t)(((c - 1) >> 1) & 1));
-          if (good) load_stage(st ^ 1, kc0 + c + 1);
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      // D F32, A/B BF16, K-major both, N = 64, M = 128
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+                             ((uint32_t)(OZ_BM >> 4) << 24);
+      // no-swizzle K-major: core matrices of 8 rows x 16 bytes; LBO steps K (128 B),
+      // SBO steps 8 rows (8 x 32 K x 2 B = 512 B)
+      const uint32_t lbo = 128u, sbo = 512u;
+      int st = 0, b = 0;
+      uint32_t ph = 0, tph[2] = {0u, 0u};
+      for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x) {
+        OzTile t;
+        if (!oz_tile_at(g, L, t) || t.nch == 0) continue;
+        uint32_t accmask = 0;
+        for (int64_t c = 0; c < t.nch; ++c) {
+          const bool gstart = (c % OZ_GROUP) == 0;
+          const bool gend = ((c + 1) % OZ_GROUP) == 0 || c == t.nch - 1;
+          if (gstart) {
+            if (!oz_wait(bar(TEMPTY + b), tph[b] ^ 1u, abort_flag)) {
+              if (!*abort_flag) atomicExch(g.err, 2);
+              abort_sh = 1;
+              goto mma_done;
+            }
+            tc_fence_after();
+            accmask = 0;
+          }
+          if (!oz_wait(bar(FULL + st), ph, abort_flag)) {
+            if (!*abort_flag) atomicExch(g.err, 2);
+            abort_sh = 1;
+            goto mma_done;
+          }
+          tc_fence_after();
+          const uint32_t abase = smem_u32(smem + st * Cfg::STAGE);
+          const uint32_t bbase = abase + S * Cfg::A_SL;
+#pragma unroll
+          for (int kk = 0; kk < OZ_TK / 16; ++kk) {
+#pragma unroll
+            for (int ti = 0; ti < S; ++ti) {
+#pragma unroll
+              for (int ui = 0; ui < S; ++ui) {
+                if (ti + ui > S) continue;
+                const int acc = ti + ui < OZ_NACC - 1 ? ti + ui : OZ_NACC - 1;
+                const uint64_t ad = umma_desc(abase + ti * Cfg::A_SL + kk * 256, lbo, sbo);
+                const uint64_t bd = umma_desc(bbase + ui * Cfg::B_SL + kk * 256, lbo, sbo);
+                umma_bf16(tmem + (uint32_t)((b * OZ_NACC + acc) * OZ_BN), ad, bd, idesc,
+                          (accmask >> acc) & 1u);
+                accmask |= 1u << acc;
+              }
+            }
+          }
+          mma_issued = true;
+          umma_commit(bar(EMPTY + st));
+          if (++st == NST) {
+            st = 0;
+            ph ^= 1u;
+          }
+          if (gend) {
+            umma_commit(bar(TFULL + b));
+            tph[b] ^= 1u;
+            b ^= 1;
+          }
         }
       }
-      if (!good) {
-        atomicExch(g.err, 1);
-        abort_sh = 1;
-      }
+    mma_done:;
     }
-    if (flush) {
-      __syncthreads();
-      if (abort_sh) {
-        ok = false;
-        break;
-      }
-      const bool waited = mbar_wait_bounded(flushb, (uint32_t)(nflush & 1));
-      if (__syncthreads_or(!waited)) {
-        if (tid == 0) atomicExch(g.err, 2);
-        ok = false;
-        break;
-      }
-      ++nflush;
-      tc_fence_after();
-#pragma unroll 1
-      for (int lev = 0; lev < Cfg::LEVELS; ++lev) {
-        uint32_t r[CPT];
-        tmem_ld<CPT>(tmem + ((uint32_t)(quarter * 32) << 16) + lev * BN + half * CPT, r);
-        tmem_ld_wait();
-        const float sc = __uint_as_float((uint32_t)(127 - 8 * lev) << 23);  // 2^-8lev
+  } else {
+    // ---- epilogue: warps 2..17 drain TMEM lanes 32 (warp % 4).., 16 columns each ----
+    const int quarter = warp & 3, part = (warp - 2) >> 2;
+    int b = 0;
+    uint32_t tph[2] = {0u, 0u};
+    const bool unit = (g.alpha == 1.0 || g.alpha == -1.0) && (g.beta == 0.0 || g.beta == 1.0);
+    for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x) {
+      OzTile t;
+      if (!oz_tile_at(g, L, t)) continue;
+      const int64_t my_row = t.row0 + quarter * 32 + lane;
+      const bool row_ok = my_row < g.M;
+      const int64_t col_base = t.col0 + part * OZ_EPI_COLS;
+      double *crow = g.C + t.z * g.c_bs + my_row;
+      // this thread's C values, loaded before the accumulators are ready so that
+      // the loads overlap the MMAs
+      double cv[OZ_EPI_COLS];
 #pragma unroll
-        for (int j = 0; j < CPT; ++j) df_add(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+      for (int j = 0; j < OZ_EPI_COLS; ++j)
+        cv[j] = (row_ok && g.beta != 0.0 && col_base + j < g.N) ? crow[(col_base + j) * g.ldc] : 0.0;
+      if (t.nch == 0) {  // nothing accumulated: C = beta C
+        if (row_ok && g.beta != 1.0)
+#pragma unroll
+          for (int j = 0; j < OZ_EPI_COLS; ++j) {
+            const int64_t col = col_base + j;
+            if (col < g.N && !(g.lower_only && my_row < col)) crow[col * g.ldc] = g.beta * cv[j];
+          }
+        continue;
       }
-      tc_fence_before();
-      __syncthreads();
-    } else if (c % 8 == 7) {
-      // keep abort visible between flushes without a barrier per chunk
-      __syncthreads();
-      if (abort_sh) {
-        ok = false;
-        break;
+      const int *a_ex = g.a_ex + t.z * g.a_bs_ex;
+      const int *b_ex = g.b_ex + t.z * g.b_bs_ex + g.b_rb0 * OZ_TR;
+      const int ea = row_ok ? a_ex[g.a_rb0 * OZ_TR + my_row] : 0;
+      const int64_t ngr = (t.nch + OZ_GROUP - 1) / OZ_GROUP;
+      // the tile's sum over its K groups, in double-float (level-0 units)
+      float hi[OZ_EPI_COLS], lo[OZ_EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < OZ_EPI_COLS; ++j) hi[j] = lo[j] = 0.f;
+      for (int64_t gi = 0; gi < ngr; ++gi) {
+        int ok = 1;
+        if (lane == 0) ok = oz_wait(bar(TFULL + b), tph[b], abort_flag) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) {
+          if (lane == 0) {
+            if (!*abort_flag) atomicExch(g.err, 3);
+            abort_sh = 1;
+          }
+          goto epi_done;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int cb = 0; cb < OZ_EPI_COLS / 8; ++cb) {
+          uint32_t r[OZ_NACC][8];
+#pragma unroll
+          for (int acc = 0; acc < OZ_NACC; ++acc)
+            tmem_ld8(tmem + ((uint32_t)(quarter * 32) << 16) +
+                         (uint32_t)((b * OZ_NACC + acc) * OZ_BN + part * OZ_EPI_COLS + cb * 8),
+                     r[acc]);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+#pragma unroll
+            for (int acc = 0; acc < OZ_NACC; ++acc) df_add(hi[cb * 8 + j], lo[cb * 8 + j], __uint_as_float(r[acc][j]));
+          }
+        }
+        // every load of this set has completed: hand it back to the MMA warp
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar(TEMPTY + b));
+        tph[b] ^= 1u;
+        b ^= 1;
+      }
+      // C = alpha 2^(e_i + f_j - 16) (hi + lo) + beta C
+      if (row_ok) {
+#pragma unroll
+        for (int j = 0; j < OZ_EPI_COLS; ++j) {
+          const int64_t col = col_base + j;
+          if (col < g.N && !(g.lower_only && my_row < col)) {
+            const int sh = ea + b_ex[col] - 16;
+            double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
+            double out;
+            if (unit) {
+              if (g.alpha < 0.0) v = -v;
+              out = (g.beta == 0.0) ? v : cv[j] + v;
+            } else {
+              out = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * cv[j]);
+            }
+            crow[col * g.ldc] = out;
+          }
+        }
       }
     }
+  epi_done:;
+  }
+
+  __syncthreads();
+  if (abort_sh) {
+    // a wait ran out: let what was issued land (bounded) before the shared memory
+    // and TMEM are released
+    if (warp == 1 && lane == 0 && mma_issued) {
+      umma_commit(bar(DRAIN));
+      mbar_wait_bounded(bar(DRAIN), 0);
+    }
+    if (warp == 0 && lane == 0)
+      for (int i = 0; i < NST; ++i)
+        if (last_full_parity[i] >= 0) mbar_wait_bounded(bar(FULL + i), (uint32_t)last_full_parity[i]);
   }
   __syncthreads();
-  if (!ok && tid == 0) {
-    // a wait ran out: give in-flight MMAs and bulk copies a bounded chance to land
-    // before the shared memory and TMEM are released
-    mbar_wait_bounded(flushb, (uint32_t)(nflush & 1));
-    mbar_wait_bounded(empty0, 0);
-    mbar_wait_bounded(empty1, 0);
-    mbar_wait_bounded(full0, 0);
-    mbar_wait_bounded(full1, 0);
-  }
-  __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::TMEM_COLS));
   }
-  if (!ok) return;
-  // FP64 epilogue: C = alpha * 2^(e_i + f_j - 16) (hi + lo) + beta * C, with the
-  // float -> double conversion and the power of two done on the bit patterns
-  if (my_row < g.M) {
-    const int ea = a_ex[g.a_rb0 * OZ_TR + my_row];
-    const bool unit = (g.alpha == 1.0 || g.alpha == -1.0) && (g.beta == 0.0 || g.beta == 1.0);
-#pragma unroll
-    for (int j = 0; j < CPT; ++j) {
-      const int64_t col = col0 + half * CPT + j;
-      if (col < g.N && !(g.lower_only && my_row < col)) {
-        const int sh = ea + b_ex[g.b_rb0 * OZ_TR + col] - 16;
-        double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
-        double *dst = Cz + my_row + col * g.ldc;
-        if (unit) {
-          if (g.alpha < 0.0) v = -v;
-          *dst = (g.beta == 0.0) ? v : *dst + v;
-        } else {
-          *dst = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * *dst);
-        }
-      }
-    }
-  }
+}
+
+static int oz_sm_count() {
+  static const int n = [] {
+    int dev = 0, sms = 0;
+    GPGP_CUDA(cudaGetDevice(&dev));
+    GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+  }();
+  return n;
 }
 
 void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
@@ -592,10 +702,8 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   if (M <= 0 || N <= 0 || batch <= 0) return;
   if (A.S != B.S) throw CudaError{cudaErrorInvalidValue, "oz_gemm: operands split to different slice counts", __LINE__};
   static const bool attr = [] {
-    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzCfg<4>::SMEM + 1024));
-    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzCfg<5>::SMEM + 1024));
+    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<4>::SMEM));
+    GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<5>::SMEM));
     return true;
   }();
   (void)attr;
@@ -603,17 +711,18 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   g.a_sl = A.sl;
   g.a_ex = A.ex;
   g.a_nrb = A.nrb;
-  g.a_nkb = A.nkb;
+  g.a_nkc = 2 * A.nkb;
   g.a_rb0 = a_row0 / OZ_TR;
   g.b_sl = B.sl;
   g.b_ex = B.ex;
   g.b_nrb = B.nrb;
-  g.b_nkb = B.nkb;
+  g.b_nkc = 2 * B.nkb;
   g.b_rb0 = b_row0 / OZ_TR;
   g.M = M;
   g.N = N;
-  g.kc0 = kc0;
-  g.kc1 = kc1;
+  // callers count K in 64-wide blocks; the kernel in 32-wide chunks
+  g.kc0 = 2 * kc0;
+  g.kc1 = std::min<int64_t>(2 * kc1, std::min(g.a_nkc, g.b_nkc));
   g.kmode = kmode;
   g.alpha = alpha;
   g.beta = beta;
@@ -628,34 +737,35 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   g.b_bs_ex = B.bstride_ex;
   g.c_bs = sC;
   g.status_bs = status_bs;
-  {
-    // executed MMA arithmetic of the tiles this launch runs (the kernel's own tile
-    // skipping and K ranges), for the per-kernel timer
-    const int BN = A.S == 5 ? OzCfg<5>::BN : OzCfg<4>::BN;
+  g.gx = (M + OZ_BM - 1) / OZ_BM;
+  g.gy = (N + OZ_BN - 1) / OZ_BN;
+  g.batch = batch;
+  const int64_t ntiles = g.gx * g.gy * batch;
+  const int64_t grid = std::min<int64_t>(ntiles, oz_sm_count());
+  double fl = 0.0;
+  if (tl_kt) {
+    // executed MMA arithmetic of the tiles the launch runs (the kernel's own tile
+    // skipping and K ranges; failed problems are not known on the host)
     const int prods = A.S == 5 ? 19 : 13;
-    const int64_t gx = (M + OZ_BM - 1) / OZ_BM, gy = (N + BN - 1) / BN;
-    double fl = 0.0;
-    if (tl_kt) {
-      for (int64_t bx = 0; bx < gx; ++bx)
-        for (int64_t by = 0; by < gy; ++by) {
-          const int64_t row0 = bx * OZ_BM, col0 = by * BN;
-          if (lower_only && col0 > row0 + OZ_BM - 1) continue;
-          const int64_t grow0 = g.a_rb0 * OZ_TR + row0, gcol0 = g.b_rb0 * OZ_TR + col0;
-          int64_t k0 = kc0, k1 = kc1;
-          if (kmode == 1) k0 = std::max(k0, std::max(grow0, gcol0) / OZ_TK);
-          if (kmode == 2) k0 = std::max(k0, gcol0 / OZ_TK);
-          if (kmode == 3) k1 = std::min(k1, (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK);
-          if (k1 > k0) fl += 2.0 * OZ_BM * BN * OZ_TK * (double)(k1 - k0) * prods;
-        }
-    }
-    KTScope kts(GPGP_KPROF_OZ_GEMM, s, fl * (double)batch);
-    if (A.S == 5) {
-      dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch);
-      oz_gemm_kernel<5><<<grid, 256, OzCfg<5>::SMEM + 1024, s>>>(g);
-    } else {
-      dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch);
-      oz_gemm_kernel<4><<<grid, 256, OzCfg<4>::SMEM + 1024, s>>>(g);
-    }
+    for (int64_t bx = 0; bx < g.gx; ++bx)
+      for (int64_t by = 0; by < g.gy; ++by) {
+        const int64_t row0 = bx * OZ_BM, col0 = by * OZ_BN;
+        if (lower_only && col0 > row0 + OZ_BM - 1) continue;
+        const int64_t grow0 = g.a_rb0 * OZ_TR + row0, gcol0 = g.b_rb0 * OZ_TR + col0;
+        int64_t k0 = g.kc0, k1 = g.kc1;
+        if (kmode == 1) k0 = std::max(k0, std::max(grow0, gcol0) / OZ_TK);
+        if (kmode == 2) k0 = std::max(k0, gcol0 / OZ_TK);
+        if (kmode == 3) k1 = std::min(k1, (grow0 + OZ_BM + OZ_TK - 1) / OZ_TK);
+        if (k1 > k0) fl += 2.0 * OZ_BM * OZ_BN * OZ_TK * (double)(k1 - k0) * prods;
+      }
+    fl *= (double)batch;
+  }
+  {
+    KTScope kts(GPGP_KPROF_OZ_GEMM, s, fl);
+    if (A.S == 5)
+      oz_gemm_kernel<5><<<(unsigned)grid, OZ_THREADS, OzCfg<5>::SMEM, s>>>(g);
+    else
+      oz_gemm_kernel<4><<<(unsigned)grid, OZ_THREADS, OzCfg<4>::SMEM, s>>>(g);
   }
   GPGP_CHECK_LAUNCH();
 }

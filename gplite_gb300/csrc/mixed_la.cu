@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "model.cuh"
 
 namespace gpgp {
 
@@ -225,6 +226,7 @@ extern "C" gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, 
   if (!ctx || M < 1 || N < 1 || K < 1 || !max_rel_err || (slices != 4 && slices != 5))
     return GPGP_EINVAL;
   cudaStream_t s = (cudaStream_t)gpgp_stream(ctx);
+  KTBind bind(ctx);
   try {
     double *A = nullptr, *B = nullptr, *C1 = nullptr, *C2 = nullptr, *red = nullptr;
     int *err = nullptr;
@@ -270,8 +272,9 @@ extern "C" gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, 
     *max_rel_err = h[0] / (h[1] > 0 ? h[1] : 1.0);
     if (herr) return GPGP_ETIMEOUT;
     return GPGP_OK;
-  } catch (const CudaError &) {
-    return GPGP_ECUDA;
+  } catch (const CudaError &e) {
+    (void)cudaGetLastError();
+    return fail(ctx, GPGP_ECUDA, std::string("CUDA error ") + cudaGetErrorString(e.err) + " in " + e.what);
   } catch (const std::bad_alloc &) {
     return GPGP_EOOM;
   }

@@ -175,6 +175,7 @@ gpgp_status guarded(gpgp_ctx *ctx, F &&fn) {
   try {
     return fn();
   } catch (const CudaError &e) {
+    (void)cudaGetLastError();  // a launch error is not sticky: do not leave it pending
     std::string m = std::string("CUDA error ") + cudaGetErrorString(e.err) + " in " + e.what;
     return fail(ctx, GPGP_ECUDA, m);
   } catch (const std::bad_alloc &) {
