@@ -207,6 +207,20 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
                  tri_mode);
 }
 
+// 1/sqrt(x) by two Newton-Raphson steps y <- y (3 - x y^2) / 2 from the FP32
+// hardware estimate (relative error ~2^-22 -> 2^-44 -> rounding level): eight
+// FP64 operations instead of a correctly rounded square root and division,
+// which matters on a part whose FP64 pipe runs one warp instruction per 64
+// cycles. Arguments outside the FP32 range take sqrt and division.
+__device__ __forceinline__ double rsqrt_newton(double x) {
+  if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
+  double y = (double)rsqrtf((float)x);
+  const double hx = 0.5 * x;
+  y = y * fma(-hx, y * y, 1.5);
+  y = y * fma(-hx, y * y, 1.5);
+  return y;
+}
+
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
@@ -251,8 +265,8 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
           atomicCAS(status, 0, (int)(k0 + j + 1));
         }
       } else {
-        const double piv = sqrt(dj);
-        const double rp = 1.0 / piv;
+        const double rp = rsqrt_newton(dj);
+        const double piv = dj * rp;
         for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
         if (lane == 0) {
           S[j][j] = piv;
@@ -510,10 +524,12 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const double *__restrict
                                                         double *b, double *x, int trans,
                                                         const int *__restrict__ status,
                                                         unsigned *bar, int *err) {
+  __shared__ double Ws[NB][NB + 1];  // the diagonal block's inverse
   __shared__ double bk[NB];
   __shared__ double xk[NB];
+  __shared__ double part[8][33];
   if (*(volatile const int *)status != 0) return;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t nblk = (n + NB - 1) / NB;
   const unsigned G = gridDim.x;
   for (int64_t step = 0; step < nblk; ++step) {
@@ -521,34 +537,67 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const double *__restrict
     const int64_t k0 = blk * NB;
     const int kb = (int)((n - k0) < NB ? (n - k0) : NB);
     const double *W = Winv + blk * NB * NB;
+    // stage W (coalesced) and this block of b
+    for (int idx = tid; idx < NB * NB; idx += 256) Ws[idx % NB][idx / NB] = W[idx];
     if (tid < NB) bk[tid] = tid < kb ? __ldcg(b + k0 + tid) : 0.0;
     __syncthreads();
-    if (tid < NB) {
+    {
+      // xk = W bk (lower W) or W^T bk: four threads per entry, partial sums by shuffles
+      const int row = tid >> 2, p = tid & 3;
       double s = 0.0;
       if (!trans) {
-        for (int c = 0; c <= tid && c < kb; ++c) s = fma(W[tid + c * NB], bk[c], s);
+        for (int c = p; c <= row && c < kb; c += 4) s = fma(Ws[row][c], bk[c], s);
       } else {
-        for (int r = tid; r < kb; ++r) s = fma(W[r + tid * NB], bk[r], s);
+        for (int r = row + p; r < kb; r += 4) s = fma(Ws[r][row], bk[r], s);
       }
-      xk[tid] = tid < kb ? s : 0.0;
+      s += __shfl_xor_sync(0xffffffffu, s, 1);
+      s += __shfl_xor_sync(0xffffffffu, s, 2);
+      if (p == 0) xk[row] = row < kb ? s : 0.0;
     }
     __syncthreads();
     if (blockIdx.x == 0 && tid < kb) x[k0 + tid] = xk[tid];
     if (!trans) {
-      // b[r] -= L[r, k0:k0+kb] xk for rows below the block
-      for (int64_t r = k0 + kb + (int64_t)blockIdx.x * 256 + tid; r < n; r += (int64_t)G * 256) {
+      // b[r] -= L[r, k0:k0+kb] xk for the rows below the block: 32 rows per pass of a
+      // block, warp w takes columns 8w..8w+7 (coalesced over the rows), then the eight
+      // partial sums of a row are added in a fixed order
+      for (int64_t r0 = k0 + kb + (int64_t)blockIdx.x * 32; r0 < n; r0 += (int64_t)G * 32) {
+        const int64_t r = r0 + lane;
         double s = 0.0;
-        for (int c = 0; c < kb; ++c) s = fma(L[r + (k0 + c) * lda], xk[c], s);
-        b[r] = __ldcg(b + r) - s;
+        if (r < n) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int c = warp * 8 + q;
+            if (c < kb) s = fma(L[r + (k0 + c) * lda], xk[c], s);
+          }
+        }
+        part[warp][lane] = s;
+        __syncthreads();
+        if (warp == 0 && r < n) {
+          double t = 0.0;
+#pragma unroll
+          for (int w = 0; w < 8; ++w) t += part[w][lane];
+          b[r] = __ldcg(b + r) - t;
+        }
+        __syncthreads();
       }
     } else {
-      // b[c] -= sum_r L[r, c] xk[r] for columns left of the block, one warp per column
-      const int lane = tid & 31, warp = tid >> 5;
-      for (int64_t c = (int64_t)blockIdx.x * 8 + warp; c < k0; c += (int64_t)G * 8) {
+      // b[c] -= sum_r L[r, c] xk[r] for the columns left of the block: eight lanes per
+      // column, each over eight contiguous rows, four columns per warp pass
+      const int sub = lane >> 3, l8 = lane & 7;
+      for (int64_t c0 = ((int64_t)blockIdx.x * 8 + warp) * 4; c0 < k0; c0 += (int64_t)G * 32) {
+        const int64_t c = c0 + sub;
         double s = 0.0;
-        for (int r = lane; r < kb; r += 32) s = fma(L[(k0 + r) + c * lda], xk[r], s);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) b[c] = __ldcg(b + c) - s;
+        if (c < k0) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int rr = l8 * 8 + q;
+            if (rr < kb) s = fma(L[(k0 + rr) + c * lda], xk[rr], s);
+          }
+        }
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        s += __shfl_xor_sync(0xffffffffu, s, 4);
+        if (l8 == 0 && c < k0) b[c] = __ldcg(b + c) - s;
       }
     }
     if (!grid_barrier(bar, G, err)) return;
