@@ -344,7 +344,7 @@ def run_gpu(args):
         calls = np.zeros(8, dtype=np.int64)
         lib.gpgp_profile_read(ctx.h, L.ptr(ms), calls.ctypes.data_as(C.c_void_p))
         kp = {}
-        for kid, name in ((0, "oz_gemm"), (1, "gemm64")):
+        for kid, name in ((0, "oz_gemm"), (1, "gemm64"), (2, "potrf_diag"), (3, "oz_split"), (4, "trsv")):
             nl, kms, kfl = C.c_int64(), C.c_double(), C.c_double()
             lib.gpgp_kernel_profile_read(ctx.h, kid, C.byref(nl), C.byref(kms), C.byref(kfl))
             kp[name] = dict(launches=nl.value, ms=kms.value, flops=kfl.value)
@@ -427,6 +427,8 @@ def run_gpu(args):
             "gpu_launches": int(head["launches"]),
             "wall_s_timed": head["wall"],
             "phases_ms": head["phases"],
+            "kernels_ms_per_step": {k: {"launches": v["launches"] / args.steps, "ms": v["ms"] / args.steps}
+                                    for k, v in head["kernels"].items()},
             "log_evidence_last": head["lmls"][-1],
         }
         if "fp64" in res and precs[0] != "fp64":
@@ -568,6 +570,129 @@ def run_batched(args):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "autotune": out["mixed"]["info"], "gpu_launches": int(out["mixed"]["launches"]),
     }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# C1: small 1-D regression (latency) and C3: Bernoulli Laplace / EP + LOO
+# ---------------------------------------------------------------------------
+
+def _median_us(fn, reps):
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append((time.perf_counter() - t0) * 1e6)
+    ts.sort()
+    return ts[len(ts) // 2], ts[min(len(ts) - 1, int(0.99 * len(ts)))]
+
+
+def run_c1(args):
+    """n = 200, x ~ N(0,1), y = sin(3x) exp(-|x|) + N(0, 0.1^2); cf_sexp(0.3, 1) +
+    lik_gaussian(0.1); unit: one energy evaluation (gp_fit through the host-buffer C ABI
+    + gp_energy) and one gp_pred of mean + var on 300 grid points; plus a whole gp_optim."""
+    import gplite_gb300 as G
+    from gplite_gb300 import _lib as L
+    from oracle import gplite_ref as R
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(200)
+    y = np.sin(3 * x) * np.exp(-np.abs(x)) + 0.1 * rng.standard_normal(200)
+    xt = np.linspace(-4, 4, 300)
+
+    def gp0():
+        return G.gp_init(G.cf_sexp(lscale=0.3, magn=1.0), G.lik_gaussian(sigma=0.1))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        gp = G.gp_fit(gp0(), x, y, precision=prec)
+        for _ in range(20):
+            G.gp_energy(G.gp_fit(gp, x, y, precision=prec))
+        l0 = L.launch_count()
+        fit50, fit99 = _median_us(lambda: G.gp_energy(G.gp_fit(gp, x, y, precision=prec)), args.c1_reps)
+        launches = (L.launch_count() - l0) / args.c1_reps
+        pred50, pred99 = _median_us(lambda: G.gp_pred(gp, xt, var=True), args.c1_reps)
+        t0 = time.perf_counter()
+        opt = G.gp_optim(gp0(), x, y, verbose=False, precision=prec)
+        t_opt = time.perf_counter() - t0
+        out[prec] = dict(fit_p50_us=fit50, fit_p99_us=fit99, pred_p50_us=pred50, pred_p99_us=pred99,
+                         launches_per_fit=launches, optim_s=t_opt, optim_energy=float(G.gp_energy(opt)),
+                         lml=float(gp.fit["log_evidence"]))
+    og = R.gp_init([R.cf("sexp", lscale=0.3, magn=1.0)], R.lik("gaussian", sigma=0.1))
+    cfit, _ = _median_us(lambda: R.gp_fit(og, x, y), 50)
+    ogf = R.gp_fit(og, x, y)
+    cpred, _ = _median_us(lambda: R.gp_pred(ogf, xt, var=True), 50)
+    f = out["fp64"]
+    line = {"metric": "GP solves/s (C1: n=200 energy evaluations, latency)", "value": 1e6 / f["fit_p50_us"],
+            "unit": "solves/s", "n_gpus": 1, "steps": args.c1_reps, "warmup": 20, "ms_per_step": f["fit_p50_us"] / 1e3,
+            "p50_ms": f["fit_p50_us"] / 1e3, "p99_ms": f["fit_p99_us"] / 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (numpy seeded, C1 recipe)",
+            "config": {"workload": "1-D regression n=200, cf_sexp + lik_gaussian, energy + pred on 300 points"},
+            "fp64": f, "mixed": out["mixed"],
+            "lml_rel_err_vs_oracle": abs(f["lml"] - ogf.fit["log_evidence"]) / abs(ogf.fit["log_evidence"]),
+            "cpu_baseline": {"value": 1e6 / cfit, "unit": "solves/s", "cores": 1, "kind": "port",
+                             "sample": "oracle gp_fit at n=200 (median of 50); pred %.0f us" % cpred}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def make_c3(n=8192, seed=3):
+    """x ~ N(0, I_4); f ~ GP(cf_sexp(0.5, 2)) drawn with an FP64 Cholesky (GPU when present);
+    y ~ Bernoulli(logistic(f))."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, 4))
+    z = rng.standard_normal(n)
+    u = rng.uniform(size=n)
+    import torch
+    dev = torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
+    X = torch.from_numpy(x).to(dev)
+    K = 4.0 * torch.exp(-0.5 * torch.cdist(X, X) ** 2 / 0.25)
+    K.diagonal().add_(1e-6)
+    f = (torch.linalg.cholesky(K) @ torch.from_numpy(z).to(dev)).cpu().numpy()
+    del X, K
+    if dev.type == "cuda":
+        torch.cuda.empty_cache()
+    y = (u < 1 / (1 + np.exp(-f))).astype(np.float64)
+    return x, y
+
+
+def run_c3(args):
+    """n = 8192 Bernoulli: approx_laplace (Newton to 1e-6) and approx_ep (damping 0.9), then
+    gp_loo; FP64 and mixed. Unit: one Laplace fit (value), with per-Newton-iteration,
+    per-EP-sweep and LOO times beside it."""
+    import torch
+    import gplite_gb300 as G
+    from gplite_gb300 import _lib as L
+    x, y = make_c3(args.c3_n)
+    res = {}
+    for prec in ("mixed", "fp64"):
+        r = {}
+        for ap_name, ap in (("laplace", G.approx_laplace(tol=1e-6)), ("ep", G.approx_ep(damping=0.9))):
+            gp = G.gp_init(G.cf_sexp(lscale=0.5, magn=2.0), G.lik_bernoulli(), approx=ap)
+            G.gp_fit(gp, x, y, precision=prec)  # warm
+            torch.cuda.synchronize()
+            l0 = L.launch_count()
+            t0 = time.perf_counter()
+            gp = G.gp_fit(gp, x, y, precision=prec)
+            t_fit = time.perf_counter() - t0
+            launches = L.launch_count() - l0
+            t0 = time.perf_counter()
+            loo = G.gp_loo(gp, x, y)
+            t_loo = time.perf_counter() - t0
+            r[ap_name] = dict(fit_s=t_fit, iters=int(gp.fit["iters"]), s_per_iter=t_fit / max(gp.fit["iters"], 1),
+                              lml=float(gp.fit["log_evidence"]), loo_s=t_loo, loo=float(loo["loo"]),
+                              launches=launches)
+        res[prec] = r
+    m, f = res["mixed"], res["fp64"]
+    line = {"metric": "GP solves/s (C3: Bernoulli n=%d Laplace fits)" % args.c3_n, "value": 1.0 / m["laplace"]["fit_s"],
+            "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": m["laplace"]["fit_s"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (bf16-split tensor updates)", "data": "synthetic (numpy seeded, C3 recipe)",
+            "config": {"workload": "Bernoulli classification n=%d d=4, cf_sexp(0.5, 2), Laplace tol 1e-6 / "
+                                   "EP damping 0.9, gp_loo" % args.c3_n},
+            "mixed": m, "fp64": f,
+            "mixed_over_fp64": {k: f[k]["fit_s"] / m[k]["fit_s"] for k in m},
+            "lml_rel_err_mixed_vs_fp64": {k: abs(m[k]["lml"] - f[k]["lml"]) / abs(f[k]["lml"]) for k in m},
+            "gpu_launches": int(m["laplace"]["launches"])}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -752,7 +877,9 @@ def main():
     ap.add_argument("--n", type=int, default=N_FULL)
     ap.add_argument("--cpu-n", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batched", "served"])
+    ap.add_argument("--workload", default="full", choices=["full", "batched", "served", "c1", "c3"])
+    ap.add_argument("--c1-reps", type=int, default=200)
+    ap.add_argument("--c3-n", type=int, default=8192)
     ap.add_argument("--window", type=float, default=2.0)
     ap.add_argument("--workers", type=int, default=6)
     ap.add_argument("--plain-budget", type=float, default=40.0)
@@ -764,6 +891,10 @@ def main():
         return run_batched(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "c1":
+        return run_c1(args)
+    if args.workload == "c3":
+        return run_c3(args)
     return run_gpu(args)
 
 

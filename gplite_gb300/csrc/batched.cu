@@ -409,8 +409,11 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
   } else {
     for (int64_t k0 = 0, blk = 0; k0 < nb; k0 += NB, ++blk) {
       double *Akk = k.Bm.p + k0 + k0 * nb;
-      potrf_diag_kernel<<<(unsigned)P, 256, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB, k.ldp.p + blk,
-                                                     k.status.p, k0, nb * nb, nb * NB, nbl);
+      {
+        KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
+        potrf_diag_kernel<<<(unsigned)P, 256, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB, k.ldp.p + blk,
+                                                       k.status.p, k0, nb * nb, nb * NB, nbl);
+      }
       GPGP_CHECK_LAUNCH();
       const int64_t m = nb - k0 - NB;
       if (m <= 0) continue;

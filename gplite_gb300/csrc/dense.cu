@@ -364,7 +364,10 @@ void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, doub
     const int kb = (int)std::min<int64_t>(NB, n - k0);
     double *Akk = A + k0 + k0 * lda;
     double *W = Winv + blk * NB * NB;
-    potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0, 0, 0, 0);
+    {
+      KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * kb * kb * kb / 3);
+      potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0, 0, 0, 0);
+    }
     GPGP_CHECK_LAUNCH();
     const int64_t m = n - k0 - kb;
     if (m > 0) {
@@ -384,8 +387,11 @@ void potrf_batched(cudaStream_t s, double *A, int64_t n, int64_t lda, int64_t sA
   for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
     const int kb = (int)std::min<int64_t>(NB, n - k0);
     double *Akk = A + k0 + k0 * lda;
-    potrf_diag_kernel<<<(unsigned)batch, 256, 0, s>>>(Akk, kb, lda, Winv + blk * NB * NB, logdet_part + blk,
-                                                      status, k0, sA, sW, sL);
+    {
+      KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * kb * kb * kb / 3 * (double)batch);
+      potrf_diag_kernel<<<(unsigned)batch, 256, 0, s>>>(Akk, kb, lda, Winv + blk * NB * NB, logdet_part + blk,
+                                                        status, k0, sA, sW, sL);
+    }
     GPGP_CHECK_LAUNCH();
     const int64_t m = n - k0 - kb;
     if (m > 0) {
@@ -618,6 +624,7 @@ void trsv_coop(cudaStream_t s, const double *L, int64_t n, int64_t lda, const do
   int tr = trans ? 1 : 0;
   void *args[] = {(void *)&L, (void *)&n, (void *)&lda, (void *)&Winv, (void *)&b, (void *)&x,
                   (void *)&tr, (void *)&status, (void *)&bar, (void *)&err};
+  KTScope kts(GPGP_KPROF_TRSV, s, (double)n * (double)n);
   GPGP_CUDA(cudaLaunchCooperativeKernel((const void *)trsv_coop_kernel, dim3(g_coop_blocks), dim3(256),
                                         args, 0, s));
   GPGP_LAUNCHED();

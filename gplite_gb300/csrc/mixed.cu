@@ -190,6 +190,7 @@ void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, i
   out->nkb = nkb;
   const int64_t rows_pad = nrb * OZ_TR;
   const int64_t sE = out->bstride_ex, sS = out->bstride_sl;
+  KTScope kts(GPGP_KPROF_OZ_SPLIT, s, 0.0);
   {
     const int64_t threads = rows_pad * 32;
     dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);

@@ -60,7 +60,10 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
       const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
       const int64_t blk = j0 / NB;
       double *Wb = Winv + blk * NB * NB;
-      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
+      {
+        KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * jb * jb * jb / 3);
+        potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
+      }
       GPGP_CHECK_LAUNCH();
       const int64_t m = n - j0 - jb;
       if (m <= 0) continue;

@@ -192,9 +192,12 @@ gpgp_status gpgp_profile_read(gpgp_ctx *ctx, double *ms, int64_t *calls);
  * slice products of the tiles it ran; FP64 GEMM: 2 x tile area x K of the
  * tiles it ran). Reset by gpgp_profile_enable. */
 typedef enum gpgp_kprof_kernel {
-  GPGP_KPROF_OZ_GEMM = 0,  /* BF16-sliced tcgen05 GEMM (mixed precision) */
-  GPGP_KPROF_GEMM64 = 1,   /* FP64 GEMM / SYRK (plain precision) */
-  GPGP_NKPROF = 2
+  GPGP_KPROF_OZ_GEMM = 0,     /* BF16-sliced tcgen05 GEMM (mixed precision) */
+  GPGP_KPROF_GEMM64 = 1,      /* FP64 GEMM / SYRK (plain precision) */
+  GPGP_KPROF_POTRF_DIAG = 2,  /* 64 x 64 diagonal-block factor + inverse (flops: 2 x 64^3 / 3) */
+  GPGP_KPROF_OZ_SPLIT = 3,    /* FP64 -> BF16 slices (flops: 0; elements split) */
+  GPGP_KPROF_TRSV = 4,        /* cooperative triangular solve (flops: n^2) */
+  GPGP_NKPROF = 5
 } gpgp_kprof_kernel;
 gpgp_status gpgp_kernel_profile_read(gpgp_ctx *ctx, int32_t kernel, int64_t *launches, double *ms,
                                      double *flops);
