@@ -841,6 +841,12 @@ def run_served(args):
     ok = np.isfinite(a) & np.isfinite(b)
     rel = np.abs(a[ok] - b[ok]) / np.maximum(np.abs(b[ok]), ns[ok])
     m = res["mixed"]
+    kinds = [r["kind"] for r in reqs]
+    failures = [(kinds[i], int(ns[i]), p, int(o["status"])) for p in ("mixed", "fp64")
+                for i, o in enumerate(res[p]["out"]) if o["status"] not in (0, 1)]
+    idx_ok = np.nonzero(ok)[0]
+    worst = [(kinds[idx_ok[j]], int(ns[idx_ok[j]]), float(a[idx_ok[j]]), float(b[idx_ok[j]]), float(rel[j]))
+             for j in np.argsort(rel)[::-1][:3]]
     line = {
         "metric": "GP solves/s + p99 ms (served stream: Poisson 2000 req/s fit+predict 256)",
         "value": m["solves"], "unit": "requests/s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -859,7 +865,7 @@ def run_served(args):
         "offered_tflops": flops / args.window / 1e12, "served_fp64_equiv_tflops": flops / m["wall"] / 1e12,
         "lml_rel_err_mixed_vs_fp64": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
                                       "norm": "max(|LML|, n)"},
-        "failed": m["failed"], "batches": m["stats"]["batches"],
+        "failed": m["failed"], "failures": failures[:10], "lml_worst": worst, "batches": m["stats"]["batches"],
         "batched_requests": m["stats"]["batched_requests"], "bytes_peak": m["stats"]["bytes_peak"],
         "clocks": clk, "gpu_launches": int(m["launches"]),
     }
