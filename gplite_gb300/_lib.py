@@ -61,7 +61,8 @@ class FitOpts(C.Structure):
 
 class FitResult(C.Structure):
     _fields_ = [("log_evidence", C.c_double), ("status", C.c_int32), ("iters", C.c_int32),
-                ("info", C.c_int64), ("quad_ok", C.c_int32), ("converged", C.c_int32)]
+                ("info", C.c_int64), ("quad_ok", C.c_int32), ("converged", C.c_int32),
+                ("precision_used", C.c_int32)]
 
 
 class BatchProblem(C.Structure):
@@ -85,8 +86,9 @@ class Request(C.Structure):
 
 class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("lane", C.c_int32), ("log_evidence", C.c_double),
-                ("model", C.c_int64), ("queue_ms", C.c_double), ("run_ms", C.c_double),
-                ("total_ms", C.c_double)]
+                ("converged", C.c_int32), ("iters", C.c_int32), ("precision_used", C.c_int32),
+                ("reserved", C.c_int32), ("model", C.c_int64), ("queue_ms", C.c_double),
+                ("run_ms", C.c_double), ("total_ms", C.c_double)]
 
 
 class ServerStats(C.Structure):

@@ -713,6 +713,37 @@ gpgp_status gpgp_cf_nn(const double *x1, int64_t n1, const double *x2, int64_t n
   return one_term(GPGP_CF_NN, x1, n1, x2, n2, d, 1.0, magn, sigma0, sigma, diag_only, out);
 }
 
+// A mixed-precision Laplace / EP fit that breaks down (a pseudo-variance <= 0,
+// NaN sites or quadrature) is redone in FP64, so that the mixed path never fails
+// where the plain one would not: on the oscillating iterations that lead there
+// the trajectories of the two precisions separate. A fit that merely reaches the
+// iteration limit is returned as it is, flagged not converged, in either
+// precision (the reference warns and returns its last iterate).
+static gpgp_status fit_with_fallback(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                                     const gpgp_method *method, const gpgp_approx *approx,
+                                     const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                                     const double *y, const double *trials, const double *offset,
+                                     gpgp_model **model, gpgp_fit_result *result, bool on_device) {
+  gpgp_status st = fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
+                              result, on_device);
+  const bool mixed = opts && opts->precision == GPGP_PREC_MIXED;
+  if (result) result->precision_used = opts ? opts->precision : GPGP_PREC_FP64;
+  if (!mixed || !lik || lik->kind == GPGP_LIK_GAUSSIAN) return st;
+  const bool breakdown = st == GPGP_EUNSUPPORTED || st == GPGP_ENAN ||
+                         (st == GPGP_OK && (result->status == GPGP_ENAN || result->status == GPGP_EUNSUPPORTED ||
+                                            (approx && approx->kind == GPGP_APPROX_EP && !result->quad_ok)));
+  if (!breakdown) return st;
+  if (*model) {
+    gpgp_model_free(*model);
+    *model = nullptr;
+  }
+  gpgp_fit_opts o64 = *opts;
+  o64.precision = GPGP_PREC_FP64;
+  st = fit_common(ctx, k, lik, method, approx, &o64, x, n, d, y, trials, offset, model, result, on_device);
+  result->precision_used = GPGP_PREC_FP64;
+  return st;
+}
+
 gpgp_status gpgp_fit(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
                      const gpgp_method *method, const gpgp_approx *approx,
                      const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
@@ -720,8 +751,8 @@ gpgp_status gpgp_fit(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
                      gpgp_model **model, gpgp_fit_result *result) {
   return guarded(ctx, [&]() {
     if (ctx) GPGP_CUDA(cudaSetDevice(ctx->device));
-    return fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
-                      result, false);
+    return fit_with_fallback(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
+                             result, false);
   });
 }
 
@@ -732,8 +763,8 @@ gpgp_status gpgp_fit_dev(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *li
                          gpgp_model **model, gpgp_fit_result *result) {
   return guarded(ctx, [&]() {
     if (ctx) GPGP_CUDA(cudaSetDevice(ctx->device));
-    return fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
-                      result, true);
+    return fit_with_fallback(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
+                             result, true);
   });
 }
 

@@ -72,32 +72,8 @@ __device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans
 // Row exponents and slices are computed from the FP64 bit patterns with
 // integer instructions only (the FP64 pipe of this part is slow).
 
-__global__ void oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
-                                 int64_t K, int64_t rows_pad, int *__restrict__ ex, int64_t sP,
-                                 int64_t sE) {
-  P += blockIdx.y * sP;  // batched: problem blockIdx.y
-  ex += blockIdx.y * sE;
-  // one warp per row: the largest |P| by an unsigned compare of the sign-cleared bits
-  const int lane = threadIdx.x & 31;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= rows_pad) return;
-  unsigned long long mx = 0ull;
-  if (r < rows)
-    for (int64_t k = lane; k < K; k += 32) {
-      const unsigned long long b =
-          (unsigned long long)__double_as_longlong(trans ? P[k + r * ld] : P[r + k * ld]) & 0x7FFFFFFFFFFFFFFFull;
-      mx = b > mx ? b : mx;
-    }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = t > mx ? t : mx;
-  }
-  if (lane == 0) {
-    // frexp exponent of the row maximum: max = 0.1m x 2^e; zero, subnormal or non-finite rows -> 0
-    const int E = (int)(mx >> 52);
-    ex[r] = (E == 0 || E == 2047) ? 0 : E - 1022;
-  }
-}
+// Row exponents and slices are computed from the FP64 bit patterns with
+// integer instructions only (the FP64 pipe of this part is slow).
 
 // bf16 bits of q 2^-8t, |q| <= 256 (exact: at most 8 significant bits)
 __device__ __forceinline__ uint32_t bf16_of_digit(int q, int t) {
@@ -136,39 +112,86 @@ __device__ __forceinline__ void oz_digits(double v, int e, int d[S]) {
   for (int t = 0; t < S; ++t) d[t] = sg * u[t];
 }
 
+// One-pass split: a block takes 32 rows, finds their maxima (coalesced for either
+// layout: lanes over rows when columns are contiguous, over K when rows are),
+// then writes every slice of those rows.
 template <int S>
-__global__ void oz_slice_kernel(const double *__restrict__ P, int64_t ld, int trans, int64_t rows,
-                                int64_t K, int64_t nrb, int64_t nkb, const int *__restrict__ ex,
-                                uint16_t *__restrict__ sl, int64_t sP, int64_t sE, int64_t sS) {
-  P += blockIdx.y * sP;  // batched: problem blockIdx.y
+__global__ void __launch_bounds__(256) oz_split_kernel(const double *__restrict__ P, int64_t ld, int trans,
+                                                       int64_t rows, int64_t K, int64_t nrb, int64_t nkb,
+                                                       int *__restrict__ ex, uint16_t *__restrict__ sl,
+                                                       int64_t sP, int64_t sE, int64_t sS) {
+  P += blockIdx.y * sP;
   ex += blockIdx.y * sE;
   sl += blockIdx.y * sS;
-  // thread per (row, 8-wide K group): writes 16 bytes per slice
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t rows_pad = nrb * OZ_TR;
-  const int64_t ngroups = nkb * (64 / 8);  // 8-wide K groups of the 64-padded K
-  if (tid >= rows_pad * ngroups) return;
-  const int64_t r = trans ? tid / ngroups : tid % rows_pad;
-  const int64_t g = trans ? tid % ngroups : tid / rows_pad;
-  const int64_t k0 = g * 8;
-  const int e = ex[r];
-  uint32_t packed[S][4];
+  __shared__ unsigned long long part[8][32];
+  __shared__ int exs[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  if (!trans) {
+    const int64_t r = r0 + lane;
+    unsigned long long mx = 0ull;
+    if (r < rows)
+      for (int64_t k = warp; k < K; k += 8) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(P[r + k * ld]) & 0x7FFFFFFFFFFFFFFFull;
+        mx = b > mx ? b : mx;
+      }
+    part[warp][lane] = mx;
+  } else {
 #pragma unroll
-  for (int j = 0; j < 8; j += 2) {
-    int d0[S], d1[S];
-    oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
-    oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
-#pragma unroll
-    for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t], t) | (bf16_of_digit(d1[t], t) << 16);
+    for (int q = 0; q < 4; ++q) {
+      const int rl = warp * 4 + q;
+      const int64_t r = r0 + rl;
+      unsigned long long mx = 0ull;
+      if (r < rows)
+        for (int64_t k = lane; k < K; k += 32) {
+          const unsigned long long b = (unsigned long long)__double_as_longlong(P[k + r * ld]) & 0x7FFFFFFFFFFFFFFFull;
+          mx = b > mx ? b : mx;
+        }
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = t > mx ? t : mx;
+      }
+      if (lane == 0) part[0][rl] = mx;
+    }
   }
-  const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
-  const int64_t kc = k0 / OZ_TK, kk = k0 % OZ_TK, nkc = 2 * nkb;
-  const int64_t within = (rr / 8) * 256 + (kk / 8) * 64 + (rr % 8) * 8;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned long long mx = part[0][lane];
+    if (!trans)
 #pragma unroll
-  for (int t = 0; t < S; ++t) {
-    const int64_t tile = ((int64_t)t * nkc + kc) * nrb + rb;
-    uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
-    *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) = v;
+      for (int w = 1; w < 8; ++w) mx = part[w][lane] > mx ? part[w][lane] : mx;
+    // frexp exponent of the row maximum: max = 0.1m x 2^e; zero, subnormal or non-finite rows -> 0
+    const int E = (int)(mx >> 52);
+    const int e = (E == 0 || E == 2047) ? 0 : E - 1022;
+    exs[lane] = e;
+    if (r0 + lane < nrb * OZ_TR) ex[r0 + lane] = e;
+  }
+  __syncthreads();
+  const int64_t ngroups = nkb * 8, nkc = 2 * nkb;
+  for (int64_t item = threadIdx.x; item < 32 * ngroups; item += 256) {
+    const int rl = trans ? (int)(item / ngroups) : (int)(item % 32);
+    const int64_t g = trans ? item % ngroups : item / 32;
+    const int64_t r = r0 + rl, k0 = g * 8;
+    if (r >= nrb * OZ_TR) continue;
+    const int e = exs[rl];
+    uint32_t packed[S][4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      int d0[S], d1[S];
+      oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
+      oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
+#pragma unroll
+      for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t], t) | (bf16_of_digit(d1[t], t) << 16);
+    }
+    const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
+    const int64_t kc = k0 / OZ_TK, kk = k0 % OZ_TK;
+    const int64_t within = (rr / 8) * 256 + (kk / 8) * 64 + (rr % 8) * 8;
+#pragma unroll
+    for (int t = 0; t < S; ++t) {
+      const int64_t tile = ((int64_t)t * nkc + kc) * nrb + rb;
+      *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) =
+          make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
+    }
   }
 }
 
@@ -191,21 +214,12 @@ void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, i
   const int64_t rows_pad = nrb * OZ_TR;
   const int64_t sE = out->bstride_ex, sS = out->bstride_sl;
   KTScope kts(GPGP_KPROF_OZ_SPLIT, s, 0.0);
-  {
-    const int64_t threads = rows_pad * 32;
-    dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);
-    oz_rowexp_kernel<<<g, 256, 0, s>>>(P, ld, trans, rows, K, rows_pad, out->ex, sP, sE);
-    GPGP_CHECK_LAUNCH();
-  }
-  {
-    const int64_t threads = rows_pad * nkb * (64 / 8);
-    dim3 g((unsigned)((threads + 255) / 256), (unsigned)batch);
-    if (out->S == 5)
-      oz_slice_kernel<5><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
-    else
-      oz_slice_kernel<4><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
-    GPGP_CHECK_LAUNCH();
-  }
+  dim3 g((unsigned)(rows_pad / 32), (unsigned)batch);
+  if (out->S == 5)
+    oz_split_kernel<5><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
+  else
+    oz_split_kernel<4><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
+  GPGP_CHECK_LAUNCH();
 }
 
 void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t rows, int64_t K,

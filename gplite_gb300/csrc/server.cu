@@ -247,6 +247,9 @@ void run_request(gpgp_server *s, Worker &w, Req *r) {
                 r->trials.empty() ? nullptr : r->trials.data(), r->offset.empty() ? nullptr : r->offset.data(),
                 &model, &fr);
   r->res.log_evidence = fr.log_evidence;
+  r->res.converged = fr.converged;
+  r->res.iters = fr.iters;
+  r->res.precision_used = fr.precision_used;
   if (st == GPGP_OK && r->m > 0) st = gpgp_pred(model, r->xt.data(), r->m, 0, r->mean, r->var);
   r->res.status = st;
   if (st == GPGP_OK && r->keep) {
@@ -325,6 +328,9 @@ void batch_loop(gpgp_server *s) {
         if (r->var) std::memcpy(r->var, var.data() + off, r->m * sizeof(double));
         r->res.log_evidence = lml[i];
         r->res.status = std::isinf(lml[i]) && lml[i] < 0 ? GPGP_ENOT_PD : GPGP_OK;
+        r->res.converged = 1;
+        r->res.iters = 1;
+        r->res.precision_used = s->o.precision;
       } else {
         r->res.status = st;
       }

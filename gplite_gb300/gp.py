@@ -244,6 +244,7 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     gp.x = x
     gp.fit = dict(type="analytic", log_evidence=res.log_evidence, iters=res.iters,
                   quad_ok=bool(res.quad_ok), status=res.status, jitter=op.jitter, n=n,
+                  converged=bool(res.converged), precision_used="mixed" if res.precision_used == 1 else "fp64",
                   y=y, trials=tr, offset=of)
     gp.fitted = True
     return gp

@@ -104,6 +104,8 @@ class GPServer:
             return None
         L.check(st, None)
         return dict(status=r.status, lane="batch" if r.lane == 0 else "worker", log_evidence=r.log_evidence,
+                    converged=bool(r.converged), iters=r.iters,
+                    precision_used="mixed" if r.precision_used == 1 else "fp64",
                     model=r.model, queue_ms=r.queue_ms, run_ms=r.run_ms, total_ms=r.total_ms,
                     mean=ticket.mean, var=ticket.var)
 

@@ -151,6 +151,8 @@ typedef struct gpgp_fit_result {
   int64_t info;        /* first non-PD pivot (1-based) when status == GPGP_ENOT_PD */
   int32_t quad_ok;     /* EP quadrature produced no NaN (R/lik.R:250-257) */
   int32_t converged;   /* 0 if the iteration limit was reached */
+  int32_t precision_used; /* GPGP_PREC_FP64 when a mixed Laplace / EP fit broke down
+                             (pseudo-variance <= 0, NaN) and was redone in FP64 */
 } gpgp_fit_result;
 
 typedef struct gpgp_ctx gpgp_ctx;
@@ -345,6 +347,9 @@ typedef struct gpgp_request_result {
   int32_t status;              /* gpgp_status of the request */
   int32_t lane;                /* 0 batch lane, 1 worker stream */
   double log_evidence;         /* fit requests */
+  int32_t converged, iters;    /* of the Laplace / EP iteration (Gaussian: 1, 1) */
+  int32_t precision_used;      /* as gpgp_fit_result.precision_used */
+  int32_t reserved;
   int64_t model;               /* id of the resident model (keep = 1), else -1 */
   double queue_ms, run_ms, total_ms; /* admission wait, service, submit -> done */
 } gpgp_request_result;
