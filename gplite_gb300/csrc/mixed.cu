@@ -347,13 +347,15 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 
 // (double)f * 2^sh, exact, by moving the float's fields into a double: the
 // float exponent is rebiased and sh added; zero and out-of-range cases take ldexp
+// out of line so that the common path is never if-converted into FP64 work
+__device__ __noinline__ double f2d_scaled_slow(float f, int sh) { return ldexp((double)f, sh); }
+
 __device__ __forceinline__ double f2d_scaled(float f, int sh) {
   const uint32_t b = __float_as_uint(f);
   if ((b << 1) == 0u) return 0.0;
   const uint32_t ef = (b >> 23) & 0xFFu;
-  if (ef == 0u || ef == 0xFFu) return ldexp((double)f, sh);
   const int ed = (int)ef - 127 + 1023 + sh;
-  if (ed <= 0 || ed >= 2047) return ldexp((double)f, sh);
+  if (ef == 0u || ef == 0xFFu || ed <= 0 || ed >= 2047) return f2d_scaled_slow(f, sh);
   const unsigned long long db = ((unsigned long long)(b >> 31) << 63) |
                                 ((unsigned long long)ed << 52) |
                                 ((unsigned long long)(b & 0x7FFFFFu) << 29);
@@ -592,7 +594,10 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
     const int quarter = warp & 3, part = (warp - 2) >> 2;
     int b = 0;
     uint32_t tph[2] = {0u, 0u};
+    // alpha and beta tests once, as integers (the FP64 pipe is the scarce unit)
     const bool unit = (g.alpha == 1.0 || g.alpha == -1.0) && (g.beta == 0.0 || g.beta == 1.0);
+    const bool beta0 = g.beta == 0.0, beta1 = g.beta == 1.0;
+    const uint32_t negmask = g.alpha < 0.0 ? 0x80000000u : 0u;
     for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x) {
       OzTile t;
       if (!oz_tile_at(g, L, t)) continue;
@@ -605,9 +610,9 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
       double cv[OZ_EPI_COLS];
 #pragma unroll
       for (int j = 0; j < OZ_EPI_COLS; ++j)
-        cv[j] = (row_ok && g.beta != 0.0 && col_base + j < g.N) ? crow[(col_base + j) * g.ldc] : 0.0;
+        cv[j] = (row_ok && !beta0 && col_base + j < g.N) ? crow[(col_base + j) * g.ldc] : 0.0;
       if (t.nch == 0) {  // nothing accumulated: C = beta C
-        if (row_ok && g.beta != 1.0)
+        if (row_ok && !beta1)
 #pragma unroll
           for (int j = 0; j < OZ_EPI_COLS; ++j) {
             const int64_t col = col_base + j;
@@ -664,13 +669,16 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
           const int64_t col = col_base + j;
           if (col < g.N && !(g.lower_only && my_row < col)) {
             const int sh = ea + b_ex[col] - 16;
-            double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
             double out;
             if (unit) {
-              if (g.alpha < 0.0) v = -v;
-              out = (g.beta == 0.0) ? v : cv[j] + v;
+              // the sign of alpha goes onto the FP32 pair
+              const float h = __uint_as_float(__float_as_uint(hi[j]) ^ negmask);
+              const float l = __uint_as_float(__float_as_uint(lo[j]) ^ negmask);
+              const double v = f2d_scaled(h, sh) + f2d_scaled(l, sh);
+              out = beta0 ? v : cv[j] + v;
             } else {
-              out = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * cv[j]);
+              const double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
+              out = beta0 ? g.alpha * v : fma(g.alpha, v, g.beta * cv[j]);
             }
             crow[col * g.ldc] = out;
           }
