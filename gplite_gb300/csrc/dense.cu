@@ -224,9 +224,9 @@ __device__ __forceinline__ double rsqrt_newton(double x) {
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
-// Factor: right-looking over the 64 columns; warp 0 takes the pivot (one
-// square root and one reciprocal) and scales the column, then all threads
-// apply the rank-1 update. Inverse W = L^-1 by forward substitution over the
+// Factor: right-looking over the 64 columns; warp 0 takes the pivots (Newton
+// inverse square root) one column ahead while warps 1-7 apply the rank-1
+// updates, one barrier per column. Inverse W = L^-1 by forward substitution over the
 // rows, all columns at once with four threads per column (partial dot
 // products combined by shuffles); a column only depends on itself, so rows
 // advance with warp synchronisation alone. log L_jj are summed in a fixed
@@ -255,37 +255,46 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   }
   if (tid == 0) failed = 0;
   __syncthreads();
-  for (int j = 0; j < kb; ++j) {
+  // pivot of column j by warp 0: L_jj and the scaled column below it
+  auto pivot = [&](int j) {
+    const double dj = S[j][j];
+    if (!(dj > 0.0) || !isfinite(dj)) {
+      if (lane == 0) {
+        failed = 1;
+        atomicCAS(status, 0, (int)(k0 + j + 1));
+      }
+      return;
+    }
+    const double rp = rsqrt_newton(dj);
+    const double piv = dj * rp;
+    for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
+    if (lane == 0) {
+      S[j][j] = piv;
+      rdiag[j] = rp;
+    }
+  };
+  if (warp == 0) pivot(0);
+  __syncthreads();
+  if (failed) return;
+  // Step j: warp 0 looks ahead (column j+1 takes its update from column j, then
+  // its pivot), while warps 1-7 update columns j+2.. with column j; the serial
+  // pivot chain so overlaps the rank-1 work, with one barrier per column.
+  for (int j = 0; j + 1 < kb; ++j) {
     if (warp == 0) {
-      const double dj = S[j][j];
-      const bool bad = !(dj > 0.0) || !isfinite(dj);
-      if (bad) {
-        if (lane == 0) {
-          failed = 1;
-          atomicCAS(status, 0, (int)(k0 + j + 1));
-        }
-      } else {
-        const double rp = rsqrt_newton(dj);
-        const double piv = dj * rp;
-        for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
-        if (lane == 0) {
-          S[j][j] = piv;
-          rdiag[j] = rp;
-        }
+      const double l = S[j + 1][j];
+      for (int r = j + 1 + lane; r < kb; r += 32) S[r][j + 1] -= S[r][j] * l;
+      __syncwarp();
+      pivot(j + 1);
+    } else {
+      // pairs (r, c), j+2 <= c <= r < kb, over a 16 x 14 thread grid
+      const int t = tid - 32, tr = t & 15, tc = t >> 4;
+      for (int c = j + 2 + tc; c < kb; c += 14) {
+        const double lc = S[c][j];
+        for (int r = c + ((tr - (c - (j + 2)) % 16 + 16) % 16); r < kb; r += 16) S[r][c] -= S[r][j] * lc;
       }
     }
     __syncthreads();
     if (failed) return;
-    const int m = kb - j - 1;
-    if (m > 0) {
-      // pairs (r, c), j < c <= r < kb, as a 16 x 16 thread grid stepping over the block
-      const int tr = tid & 15, tc = tid >> 4;
-      for (int c = j + 1 + tc; c < kb; c += 16) {
-        const double lc = S[c][j];
-        for (int r = c + ((tr - (c - (j + 1)) % 16 + 16) % 16); r < kb; r += 16) S[r][c] -= S[r][j] * lc;
-      }
-    }
-    __syncthreads();
   }
   // write the factor back (lower part of the block)
   for (int idx = tid; idx < kb * kb; idx += 256) {
