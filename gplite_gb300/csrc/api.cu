@@ -160,8 +160,27 @@ __global__ void refine_residual_kernel(int64_t n, const double *__restrict__ rhs
   if (i < n) r[i] = rhs[i] - (u[i] + s[i] * Kalpha[i]);
 }
 
+// FP64 iterative refinement in B-space on the current factor: r = s z - B u with
+// B u = u + s (K alpha); u += B^-1 r; alpha = s u; fnew = K alpha. w.rhs holds s z
+// and w.u the current solution.
+void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters) {
+  cudaStream_t st = m->ctx->stream;
+  const int64_t n = m->n;
+  unsigned *bar = (unsigned *)w.flags.p + 2;
+  for (int it = 0; it < iters; ++it) {
+    refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
+    GPGP_CHECK_LAUNCH();
+    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
+    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
+    vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
+    vec_mul(st, n, m->s.p, w.u.p, alpha);
+    gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+  }
+}
+
+// refine < 0: the model's own refinement count (mixed precision only)
 int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
-                         double *fnew, double *logdetL, bool force_fp64 = false) {
+                         double *fnew, double *logdetL, bool force_fp64 = false, int refine = -1) {
   gpgp_ctx *ctx = m->ctx;
   cudaStream_t st = ctx->stream;
   const int64_t n = m->n;
@@ -187,18 +206,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, true, w.status.p, bar, m->errflag.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
-    if (mixed) {
-      // FP64 iterative refinement in B-space: r = s z - B u, B u = u + s (K alpha)
-      for (int it = 0; it < std::max(1, m->opts.refine_iters); ++it) {
-        refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
-        GPGP_CHECK_LAUNCH();
-        trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
-        trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
-        vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
-        vec_mul(st, n, m->s.p, w.u.p, alpha);
-        gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
-      }
-    }
+    if (mixed) refine_alpha(m, w, alpha, fnew, refine < 0 ? std::max(1, m->opts.refine_iters) : refine);
   }
   const int64_t nblk = (n + NB - 1) / NB;
   sum_vec(st, w.logdet_part.p, nblk, logdetL);
@@ -214,7 +222,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     // definite in FP64. Redo this factorisation on the FP64 pipe, whose
     // verdict is the reference's.
     ++m->fp64_fallbacks;
-    return factor_and_solve(m, w, zvec, alpha, fnew, logdetL, true);
+    return factor_and_solve(m, w, zvec, alpha, fnew, logdetL, true, refine);
   }
   return hstatus;
 }
@@ -315,7 +323,11 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
                     "non-log-concave branch (some pseudo-variance <= 0, R/laplace.R:40-117) is "
                     "not implemented");
       }
-      int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL);
+      // mixed precision: the Newton iterates only steer the iteration, so their
+      // solves go unrefined; the final alpha and f are refined once it stops
+      const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
+      int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
+                                      (mixed && maxiter > 1) ? 0 : -1);
       if (info != 0) {
         res->status = GPGP_ENOT_PD;
         res->info = info;
@@ -324,6 +336,8 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       }
       max_abs_diff(st, n, m->fmean.p, fnew.p, red);
       diff = read_scalar(ctx, red + 64);
+      const bool last = diff < m->approx.tol || it == maxiter;
+      if (last && mixed && maxiter > 1) refine_alpha(m, w, m->alpha.p, fnew.p, std::max(1, m->opts.refine_iters));
       GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
       if (diff < m->approx.tol) break;
     }
