@@ -137,6 +137,11 @@ __global__ void sub_from_kernel(int64_t n, const double *__restrict__ a, double 
 }
 
 
+__global__ void nonfinite_kernel(int64_t n, const double *__restrict__ v, int *__restrict__ flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(v[i])) atomicOr(flag, 1);
+}
+
 void make_B(cudaStream_t st, const double *K, int64_t n, const double *s, double *B) {
   dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
   make_B_kernel<<<g, 256, 0, st>>>(K, n, s, B);
@@ -506,6 +511,24 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   GPGP_CUDA(cudaMemsetAsync(m->errflag.p, 0, sizeof(int), s));
   copy_in(s, m->x, x, (size_t)n * d, on_device);
   copy_in(s, m->y, y, n, on_device);
+  {
+    // NaN or Inf in x or y: an error here rather than NaN evidences further on
+    IBuf bad;
+    bad.alloc(s, 1);
+    GPGP_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    nonfinite_kernel<<<g1((int64_t)n * d), 256, 0, s>>>((int64_t)n * d, m->x.p, bad.p);
+    GPGP_CHECK_LAUNCH();
+    nonfinite_kernel<<<g1(n), 256, 0, s>>>(n, m->y.p, bad.p);
+    GPGP_CHECK_LAUNCH();
+    int hb = 0;
+    GPGP_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    if (hb) {
+      result->status = GPGP_ENAN;
+      result->log_evidence = NAN;
+      return fail(ctx, GPGP_ENAN, "x or y holds NaN or Inf");
+    }
+  }
   if (trials) {
     copy_in(s, m->trials, trials, n, on_device);
     m->has_trials = true;

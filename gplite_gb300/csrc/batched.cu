@@ -515,6 +515,11 @@ std::string check_problems(const gpgp_batch_problem *probs, int32_t nprob) {
         !(p.sigma > 0) || !(p.lscale > 0) ||
         (p.kind != GPGP_CF_SEXP && p.kind != GPGP_CF_MATERN32 && p.kind != GPGP_CF_MATERN52))
       return "batched problem " + std::to_string(i) + " is invalid";
+    bool finite = true;
+    for (int64_t k = 0; k < (int64_t)p.n * p.d && finite; ++k) finite = std::isfinite(p.x[k]);
+    for (int64_t k = 0; k < p.n && finite; ++k) finite = std::isfinite(p.y[k]);
+    for (int64_t k = 0; k < (int64_t)p.m * p.d && finite; ++k) finite = std::isfinite(p.xt[k]);
+    if (!finite) return "batched problem " + std::to_string(i) + " holds NaN or Inf";
   }
   return std::string();
 }

@@ -31,6 +31,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "model.cuh"
 
 namespace gpgp {
 
@@ -802,3 +803,43 @@ void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B,
 
 
 }  // namespace gpgp
+
+// ---------------------------------------------------------------------------
+// bounded-wait self-test: an mbarrier that is never completed (two arrivals
+// expected, one made), polled with the same loop as the GEMM's waits but with a
+// caller-chosen bound; the kernel records the timeout and returns
+// ---------------------------------------------------------------------------
+namespace gpgp {
+__global__ void wait_selftest_kernel(uint32_t polls, int *err) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_sh;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 2);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_sh = 0;
+    mbar_arrive(smem_u32(&bar));
+    bool done = false;
+    for (uint32_t it = 0; it < polls && !done; ++it) done = mbar_try_wait(smem_u32(&bar), 0);
+    if (!done) atomicExch(err, 4);
+  }
+  __syncthreads();
+}
+}  // namespace gpgp
+
+extern "C" gpgp_status gpgp_wait_selftest(gpgp_ctx *ctx, int32_t polls) {
+  if (!ctx || polls < 1) return GPGP_EINVAL;
+  return gpgp::guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    gpgp::IBuf err;
+    err.alloc(s, 1);
+    GPGP_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+    gpgp::wait_selftest_kernel<<<1, 32, 0, s>>>((uint32_t)polls, err.p);
+    GPGP_CHECK_LAUNCH();
+    int h = 0;
+    GPGP_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    if (h) return gpgp::fail(ctx, GPGP_ETIMEOUT, "a bounded device wait ran out (self-test)");
+    return GPGP_OK;
+  });
+}

@@ -59,6 +59,7 @@ struct Req {
   int64_t resident = 0;  // bytes that stay while the model is kept
   double work = 0;       // flop estimate (worker load balance)
   bool batchable = false;
+  bool bad_input = false;  // NaN or Inf in x, y or xt: fails with GPGP_ENAN, never runs
   int worker = -1;
   bool done = false;
   Clock::time_point t_submit, t_admit, t_start, t_done;
@@ -443,6 +444,11 @@ gpgp_status gpgp_server_submit(gpgp_server *s, const gpgp_request *q, int64_t *i
       if (!r->meth.inducing || r->meth.num_inducing < 1) return GPGP_EINVAL;
       r->inducing.assign(r->meth.inducing, r->meth.inducing + (int64_t)r->meth.num_inducing * q->d);
     }
+    bool finite = true;
+    for (double v : r->x) finite = finite && std::isfinite(v);
+    for (double v : r->y) finite = finite && std::isfinite(v);
+    for (double v : r->xt) finite = finite && std::isfinite(v);
+    r->bad_input = !finite;
     r->batchable = !r->keep && r->lik.kind == GPGP_LIK_GAUSSIAN && r->meth.kind == GPGP_METHOD_FULL &&
                    !q->trials && !q->offset && q->d <= 8 && q->n <= s->o.batch_max_n &&
                    is_stationary_single(r->k, q->d) && r->k.term[0].lscale > 0 && r->lik.sigma > 0;
@@ -456,8 +462,8 @@ gpgp_status gpgp_server_submit(gpgp_server *s, const gpgp_request *q, int64_t *i
   ++s->unfinished;
   Req *rp = r.get();
   s->reqs[r->id] = std::move(r);
-  if (rp->bytes > s->budget) {
-    fail_now(s, rp, GPGP_EOOM);
+  if (rp->bad_input || rp->bytes > s->budget) {
+    fail_now(s, rp, rp->bad_input ? GPGP_ENAN : GPGP_EOOM);
     s->cv_done.notify_all();
     return GPGP_OK;
   }

@@ -397,6 +397,12 @@ gpgp_status gpgp_fit_gaussian_noalloc(gpgp_ctx *ctx, const gpgp_kernel *k, doubl
 gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K, int32_t slices,
                                 double *max_rel_err);
 
+/* ---- bounded-wait self-test: a kernel polls an mbarrier that nothing completes
+ *      for `polls` iterations (the same loop as the tensor-core kernels' waits,
+ *      whose bound is 2^24), records the timeout and returns; the call returns
+ *      GPGP_ETIMEOUT and the context stays usable. ---- */
+gpgp_status gpgp_wait_selftest(gpgp_ctx *ctx, int32_t polls);
+
 #ifdef __cplusplus
 }
 #endif
