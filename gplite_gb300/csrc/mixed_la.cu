@@ -93,22 +93,76 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
 // ---------------------------------------------------------------------------
 // recursive triangular inverse: W = L^-1, W21 = -W22 (L21 W11)
 // ---------------------------------------------------------------------------
-static void copy_diag_inverse(cudaStream_t s, const double *Winv, int64_t blk, int kb, double *W,
-                              int64_t ldw) {
-  GPGP_CUDA(cudaMemcpy2DAsync(W, ldw * sizeof(double), Winv + blk * NB * NB, NB * sizeof(double),
-                              kb * sizeof(double), kb, cudaMemcpyDeviceToDevice, s));
+// every 64 x 64 diagonal-block inverse into W's diagonal, one kernel
+__global__ void put_diag_inverses_kernel(const double *__restrict__ Winv, int64_t n, double *__restrict__ W,
+                                         int64_t ldw) {
+  const int64_t blk = blockIdx.x, k0 = blk * NB;
+  const int kb = (int)((n - k0) < NB ? (n - k0) : NB);
+  const double *src = Winv + blk * NB * NB;
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx % NB, c = idx / NB;
+    if (r < kb && c < kb) W[(k0 + r) + (k0 + c) * ldw] = src[r + c * NB];
+  }
 }
 
-static void trtri_rec(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
-                      int64_t off, double *W, int64_t ldw, double *T, int *err) {
-  if (n <= NB) {
-    copy_diag_inverse(s, Winv, off / NB, (int)n, W, ldw);
-    return;
+constexpr int64_t TRTRI_BASE = 512;  // diagonal blocks inverted level by level, batched
+
+// Batched scratch for a level: `count` split operands of rows x K each.
+struct SplitBatch {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  OzSplit sp;
+  SplitBatch(cudaStream_t st, int64_t rows, int64_t K, int64_t count) : s(st) {
+    const size_t per = (oz_split_bytes(rows, K) + 1023) / 1024 * 1024;
+    if (cudaMallocAsync(&p, per * count, st) != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    oz_split_bind(p, rows, K, &sp);
+    sp.bstride_ex = (int64_t)(per / sizeof(int));
+    sp.bstride_sl = (int64_t)(per / sizeof(uint16_t));
   }
-  const int64_t n1 = ((n / 2) + NB - 1) / NB * NB;
+  ~SplitBatch() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+// One level of the blocked inverse for every full b x b diagonal block at
+// offsets k b (k < count), whose two halves are already inverted:
+// W21 = -W22 (L21 W11), all blocks of the level in two batched GEMMs.
+static void trtri_level(cudaStream_t s, const double *L, int64_t lda, double *W, int64_t ldw, int64_t b,
+                        int64_t count, double *T, int *err) {
+  const int64_t h = b / 2;
+  {
+    SplitBatch a(s, h, h, count), bb(s, h, h, count);
+    oz_split_batched(s, L + h, lda, b * (lda + 1), 0, h, h, &a.sp, count);
+    oz_split_batched(s, W, ldw, b * (ldw + 1), 1, h, h, &bb.sp, count);
+    oz_gemm_batched(s, a.sp, 0, bb.sp, 0, h, h, 0, bb.sp.nkb, 2, 1.0, 0.0, T, h, h * h, false, err, nullptr, 0,
+                    count);
+  }
+  {
+    SplitBatch a(s, h, h, count), bb(s, h, h, count);
+    oz_split_batched(s, W + h + h * ldw, ldw, b * (ldw + 1), 0, h, h, &a.sp, count);
+    oz_split_batched(s, T, h, h * h, 1, h, h, &bb.sp, count);
+    oz_gemm_batched(s, a.sp, 0, bb.sp, 0, h, h, 0, a.sp.nkb, 3, -1.0, 0.0, W + h, ldw, b * (ldw + 1), false, err,
+                    nullptr, 0, count);
+  }
+}
+
+// recursive triangular inverse: W = L^-1, W21 = -W22 (L21 W11). Nodes already
+// inverted (64-blocks from the factorisation, and full aligned 128 / 256 / 512
+// blocks from the batched levels) are skipped; above the base the split points
+// are multiples of the base so that its blocks line up.
+static void trtri_rec(cudaStream_t s, const double *L, int64_t n, int64_t lda, int64_t off, int64_t ntot,
+                      double *W, int64_t ldw, double *T, int *err) {
+  if (n <= NB) return;
+  if ((n == 128 || n == 256 || n == TRTRI_BASE) && off % n == 0 && off + n <= ntot) return;
+  const int64_t g = n > TRTRI_BASE ? TRTRI_BASE : NB;
+  const int64_t n1 = ((n / 2) + g - 1) / g * g;
   const int64_t n2 = n - n1;
-  trtri_rec(s, L, n1, lda, Winv, off, W, ldw, T, err);
-  trtri_rec(s, L + n1 + n1 * lda, n2, lda, Winv, off + n1, W + n1 + n1 * ldw, ldw, T, err);
+  trtri_rec(s, L, n1, lda, off, ntot, W, ldw, T, err);
+  trtri_rec(s, L + n1 + n1 * lda, n2, lda, off + n1, ntot, W + n1 + n1 * ldw, ldw, T, err);
   // T = L21 W11  (n2 x n1): A = L21 (rows n2, K n1), B rows j = columns of W11 (W11[k, j], k >= j)
   {
     SplitBuf a(s, n2, n1), b(s, n1, n1);
@@ -138,14 +192,19 @@ void trtri_mixed(cudaStream_t s, const double *L, int64_t n, int64_t lda, const 
   dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
   zero_upper_kernel<<<g, 256, 0, s>>>(W, n, ldw);
   GPGP_CHECK_LAUNCH();
+  put_diag_inverses_kernel<<<(unsigned)((n + NB - 1) / NB), 256, 0, s>>>(Winv, n, W, ldw);
+  GPGP_CHECK_LAUNCH();
   double *T = nullptr;
-  const int64_t h = (n / 2 + NB) * (n / 2 + NB);
+  const int64_t h = (n / 2 + TRTRI_BASE) * (n / 2 + TRTRI_BASE);
   if (cudaMallocAsync((void **)&T, (size_t)h * sizeof(double), s) != cudaSuccess) {
     (void)cudaGetLastError();
     throw std::bad_alloc();
   }
   try {
-    trtri_rec(s, L, n, lda, Winv, 0, W, ldw, T, err);
+    // the full aligned diagonal blocks of 128, 256 and 512, all blocks of a size at once
+    for (int64_t b = 2 * NB; b <= TRTRI_BASE; b *= 2)
+      if (n / b > 0) trtri_level(s, L, lda, W, ldw, b, n / b, T, err);
+    trtri_rec(s, L, n, lda, 0, n, W, ldw, T, err);
   } catch (...) {
     cudaFreeAsync(T, s);
     throw;
