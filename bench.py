@@ -120,7 +120,9 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    n = args.cpu_n
+    # a bounded sample per step (n = 4096, scaled by (16384/4096)^3) so that the
+    # whole --steps/--warmup run ends within a few minutes
+    n = min(args.cpu_n, 4096)
     x, y = make_data(n, seed=2)
     for k in range(args.warmup):
         cpu_energy_grad(x, y, theta_sequence(k))
