@@ -280,7 +280,15 @@ void worker_loop(gpgp_server *s, Worker *w) {
     run_request(s, *w, r);
     std::lock_guard<std::mutex> lk(s->mu);
     w->load -= r->work;
-    if (r->kind != REQ_RELEASE) finish(s, r);
+    if (r->kind != REQ_RELEASE) {
+      finish(s, r);
+    } else {
+      for (auto it = s->internal.begin(); it != s->internal.end(); ++it)
+        if (it->get() == r) {
+          s->internal.erase(it);
+          break;
+        }
+    }
     try_admit(s);
     s->cv_done.notify_all();
   }
