@@ -412,6 +412,87 @@ def gauss_hermite_points(p):
 # LOO (R/gp_loo.R:73-175)
 # ----------------------------------------------------------------------------
 
+def _response(lik, f):
+    """get_response (R/lik.R:460-498): the inverse link applied to latent values."""
+    if lik.link == "identity":
+        return f
+    if lik.link == "logit":
+        return 1.0 / (1.0 + np.exp(-f))
+    if lik.link == "probit":
+        from scipy.stats import norm
+        return norm.cdf(f)
+    return np.exp(f)
+
+
+def _generate_target(lik, f, rng, trials=None):
+    """generate_target (R/lik.R:504-537): observations drawn given latent values."""
+    if lik.kind == "gaussian":
+        return rng.standard_normal(f.shape) * lik.sigma + f
+    mu = _response(lik, f)
+    if lik.kind == "bernoulli":
+        return rng.binomial(1, mu).astype(float)
+    if lik.kind == "binomial":
+        t = np.broadcast_to(np.asarray(trials, dtype=np.int64).reshape(-1, 1), f.shape)
+        return rng.binomial(t, mu).astype(float)
+    if lik.kind == "poisson":
+        return rng.poisson(mu).astype(float)
+    a, b = mu / lik.phi, (1 - mu) / lik.phi
+    t = np.broadcast_to(np.asarray(trials, dtype=np.int64).reshape(-1, 1), f.shape)
+    return rng.binomial(t, rng.beta(a, b)).astype(float)
+
+
+def gp_pred_cov(gp, xnew, cfind=None, jitter=None):
+    """gp_pred_post(cov = TRUE) / gp_pred_prior(cov = TRUE) for method_full
+    (R/gp_pred.R:140-153, 202-232): mean and the full covariance + jitter I."""
+    xnew = _as_x(xnew)
+    m = xnew.shape[0]
+    jit = JITTER_DEFAULT if jitter is None else float(jitter)
+    if not _is_fitted(gp):
+        if gp.method.kind == "fitc":
+            raise NotImplementedError("prior covariance of method_fitc")
+        return np.zeros(m), eval_cf(gp.cfs, xnew, xnew, cfind) + jit * np.eye(m)
+    if gp.method.kind == "fitc":
+        raise NotImplementedError("the full predictive covariance of method_fitc")
+    mean = np.empty(m)
+    cov = np.empty((m, m), order="F")
+    xf = L.fortran(xnew)
+    st = L.load().gpgp_pred_cov(gp._model, L.ptr(xf), m, _group_mask(gp, cfind), jit, L.ptr(mean),
+                                cov.ctypes.data_as(C.c_void_p))
+    L.check(st, None)
+    return mean, cov
+
+
+def gp_draw(gp, xnew, draws=None, transform=True, target=False, marginal=False, cfind=None, jitter=None,
+            seed=None, offset=None, trials=None, device=0):
+    """gp_draw (R/gp_draw.R:1-143): draws of the latent function at xnew from the posterior
+    (fitted gp) or the prior, as an m x draws matrix; transform applies the inverse link,
+    target draws observations. The multivariate normal draw (Cholesky of the predictive
+    covariance, mean + L z) runs on the device; R's random stream cannot be reproduced, so
+    the standard normals come from numpy's generator seeded by `seed`."""
+    xnew = _as_x(xnew)
+    m = xnew.shape[0]
+    draws = 1 if draws is None else int(draws)
+    rng = np.random.default_rng(seed)
+    z = np.asfortranarray(rng.standard_normal((m, draws)))
+    if marginal and _is_fitted(gp):
+        pred = gp_pred(gp, xnew, var=True, cfind=cfind)
+        sample = pred["mean"][:, None] + np.sqrt(pred["var"])[:, None] * z
+    else:
+        mean, cov = gp_pred_cov(gp, xnew, cfind=cfind, jitter=jitter)
+        ctx = L.default_context(device)
+        sample = np.empty((m, draws), order="F")
+        st = L.load().gpgp_mvn_draw(ctx.h, L.ptr(np.ascontiguousarray(mean)), cov.ctypes.data_as(C.c_void_p), m,
+                                    z.ctypes.data_as(C.c_void_p), draws, sample.ctypes.data_as(C.c_void_p))
+        L.check(st, ctx.h)
+    if offset is not None:
+        sample = sample + np.asarray(offset, dtype=np.float64).reshape(-1, 1)
+    if target:
+        return _generate_target(gp.lik, sample, rng, trials)
+    if transform:
+        return _response(gp.lik, sample)
+    return sample
+
+
 def gp_loo(gp, x, y, quadrature=True, quad_order=11, draws=4000, jitter=None, seed=None, **kw):
     """gp_loo (R/gp_loo.R:73-109) with Gauss-Hermite quadrature, on the fitted data."""
     if not _is_fitted(gp):

@@ -267,6 +267,21 @@ gpgp_status gpgp_pred(gpgp_model *model, const double *xt, int64_t m, uint32_t g
 gpgp_status gpgp_pred_dev(gpgp_model *model, const double *xt, int64_t m, uint32_t group_mask,
                           double *mean, double *var);
 
+/* ---- full predictive covariance: gp_pred_post(cov = TRUE).method_full
+ *      (R/gp_pred.R:202-232): mean (m) and cov (m x m, column-major)
+ *      = K(xt, xt) - aux^T aux + jitter I, aux = C_chol^-1 K(x, xt). FP64.
+ *      method_fitc returns GPGP_EUNSUPPORTED. ---- */
+gpgp_status gpgp_pred_cov(gpgp_model *model, const double *xt, int64_t m, uint32_t group_mask,
+                          double jitter, double *mean, double *cov);
+
+/* ---- multivariate normal draws: mvnrnd (R/gp_draw.R:182-199),
+ *      out = mean 1^T + t(chol(cov)) z for a caller-drawn standard-normal
+ *      z (d x draws, column-major); FP64 Cholesky on the device. A
+ *      covariance that is not positive definite gives GPGP_ENOT_PD (an error
+ *      of R's chol in the reference). ---- */
+gpgp_status gpgp_mvn_draw(gpgp_ctx *ctx, const double *mean, const double *cov, int64_t d,
+                          const double *z, int64_t draws, double *out);
+
 /* ---- LOO: replaces loo_posteriors + the quadrature of gp_loo
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
