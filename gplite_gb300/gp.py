@@ -198,6 +198,60 @@ def learn_scales(gp, x):
 # fit / energy
 # ----------------------------------------------------------------------------
 
+def kmeans(x, k, init, max_iter=10, device=0):
+    """Lloyd's k-means on the device (gpgp_kmeans) from the given initial centres:
+    (centres k x d, iterations used, within-cluster sum of squares)."""
+    x = L.fortran(_as_x(x))
+    n, d = x.shape
+    init = L.fortran(np.asarray(init, dtype=np.float64).reshape(k, d))
+    ctx = L.default_context(device)
+    centers = np.empty((k, d), order="F")
+    it = C.c_int32(0)
+    wss = C.c_double(0.0)
+    L.check(L.load().gpgp_kmeans(ctx.h, L.ptr(x), n, d, int(k), L.ptr(init), int(max_iter),
+                                 centers.ctypes.data_as(C.c_void_p), C.byref(it), C.byref(wss)), ctx.h)
+    return centers, it.value, wss.value
+
+
+def _kmeans_scaled(x, k, rng, device):
+    """scale(x), k-means of the scaled rows (initial centres: k distinct rows drawn by
+    rng, as stats::kmeans samples them), centres mapped back (R/gp_fit.R:228-233)."""
+    mu = x.mean(0)
+    sd = x.std(0, ddof=1) if x.shape[0] > 1 else np.ones(x.shape[1])
+    xs = (x - mu) / sd
+    init = xs[rng.choice(xs.shape[0], k, replace=False)]
+    centers, _, _ = kmeans(xs, k, init, max_iter=10, device=device)
+    return centers * sd + mu
+
+
+def _bin(x, nbins, var):
+    """bin (R/gp_fit.R:239-259): rows of x split into nbins equal-width bins of column var."""
+    lo = x[:, var].min() - 2 * np.finfo(float).eps
+    hi = x[:, var].max() + 2 * np.finfo(float).eps
+    cut = np.linspace(lo, hi, nbins + 1)
+    return [x[(x[:, var] > cut[i]) & (x[:, var] < cut[i + 1])] for i in range(nbins)]
+
+
+def get_inducing(gp, x, device=0):
+    """get_inducing (R/gp_fit.R:192-236): the given inducing inputs, or k-means centres of
+    the standardised inputs (per bin of `bin_along` when set). The reference seeds R's
+    stream with method$seed; numpy's generator is seeded with it here."""
+    me = gp.method
+    if me.inducing is not None:
+        return me.inducing
+    x = _as_x(x)
+    rng = np.random.default_rng(me.seed)
+    if me.bin_along is None:
+        return _kmeans_scaled(x, me.num_inducing, rng, device)
+    bins = _bin(x, me.bin_count, int(me.bin_along))
+    sizes = np.array([len(b) for b in bins])
+    order = np.argsort(-sizes, kind="stable")
+    per_bin = np.full(me.bin_count, me.num_inducing // me.bin_count)
+    per_bin[: me.num_inducing - per_bin.sum()] += 1
+    zs = [_kmeans_scaled(bins[o], int(per_bin[i]), rng, device) for i, o in enumerate(order) if per_bin[i] > 0]
+    return np.vstack(zs)
+
+
 def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", device=0):
     """gp_fit (R/gp_fit.R:54-60): posterior approximation with the current hyperparameters."""
     x = _as_x(x)
@@ -217,8 +271,7 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     ind = None
     if gp.method.kind == "fitc":
         if gp.method.inducing is None:
-            raise NotImplementedError("method_fitc needs explicit inducing points (k-means placement "
-                                      "is not implemented)")
+            gp.method.inducing = get_inducing(gp, x, device=device)
         ind = L.fortran(gp.method.inducing)
         me.num_inducing = ind.shape[0]
         me.inducing = ind.ctypes.data

@@ -282,6 +282,15 @@ gpgp_status gpgp_pred_cov(gpgp_model *model, const double *xt, int64_t m, uint32
 gpgp_status gpgp_mvn_draw(gpgp_ctx *ctx, const double *mean, const double *cov, int64_t d,
                           const double *z, int64_t draws, double *out);
 
+/* ---- k-means of the inducing inputs: stats::kmeans in get_inducing
+ *      (R/gp_fit.R:192-236). Lloyd's algorithm from the caller's initial
+ *      centres (k x d), at most max_iter iterations; deterministic centre
+ *      sums. x n x d column-major, d <= 16, k d <= 6144. Writes the centres
+ *      (k x d), the iterations used and the within-cluster sum of squares. */
+gpgp_status gpgp_kmeans(gpgp_ctx *ctx, const double *x, int64_t n, int32_t d, int32_t k,
+                        const double *init, int32_t max_iter, double *centers, int32_t *iters,
+                        double *wss);
+
 /* ---- LOO: replaces loo_posteriors + the quadrature of gp_loo
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
