@@ -11,9 +11,17 @@
 // a fourth: a level-l sum of up to 256 products has 24 significant bits for
 // l <= 2, so those sums are exact in FP32; the shared deeper levels round at
 // 2^-50 of the result. After every 256-wide K group the four accumulators are
-// added into a double-float (hi, lo) pair and applied to C in FP64:
+// added into a double-float (hi, lo) pair; at the end of the tile the pair is
+// turned into a double with integer instructions and added to C (one FP64 add):
 //   (A B^T)_ij = 2^(e_i + f_j - 16) (P_0 + P_1 + P_2 + P_3+).
 // The truncation error is ~2^-(8S+1) of the row maxima.
+//
+// A tcgen05.mma costs about the same whatever its N (measured: N = 32..128 and
+// M = 64 or 128 all take ~88 cycles per instruction here), so the products are
+// issued as few, wide instructions: the B slices are adjacent in shared memory,
+// and A_t times B slices 0..3-t is one MMA of N = 64 (4 - t) whose column blocks
+// are the accumulators of levels t..3. S = 4 takes 7 instructions per K step
+// instead of 13, S = 5 takes 13 instead of 19.
 //
 // Data path: slices are stored pre-tiled in the canonical no-swizzle K-major
 // UMMA layout (8-row x 16-byte core matrices, 64-row x 32-K tiles), so one
@@ -21,8 +29,8 @@
 // persistent and warp-specialised: a producer warp streams K chunks of the
 // CTA's output tiles through a ring of shared-memory stages, an MMA warp
 // issues tcgen05.mma into one of two TMEM accumulator sets and commits to
-// mbarriers, and four epilogue warps drain the other set with tcgen05.ld and
-// update C in FP64 while the next group accumulates. Every wait is bounded: on
+// mbarriers, and sixteen epilogue warps drain the other set with tcgen05.ld
+// and update C while the next group accumulates. Every wait is bounded: on
 // timeout the kernel records an error, drains what it issued, releases TMEM
 // and returns.
 #include <math.h>
@@ -69,9 +77,6 @@ __device__ __forceinline__ double oz_elem(const double *P, int64_t ld, int trans
   if (r >= rows || k >= K) return 0.0;
   return trans ? P[k + r * ld] : P[r + k * ld];
 }
-
-// Row exponents and slices are computed from the FP64 bit patterns with
-// integer instructions only (the FP64 pipe of this part is slow).
 
 // Row exponents and slices are computed from the FP64 bit patterns with
 // integer instructions only (the FP64 pipe of this part is slow).
@@ -372,6 +377,44 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
   lo = __fadd_rn(lo, e);
 }
 
+__device__ __noinline__ double df2d_scaled_slow(float hi, float lo, int sh) {
+  return f2d_scaled_slow(hi, sh) + f2d_scaled_slow(lo, sh);
+}
+
+// (hi + lo) 2^sh as a double without FP64 instructions. The pair is first
+// renormalised (TwoSum), so |lo| <= ulp_float(hi) / 2 = 2^28 units in the last
+// place of hi's double. hi's double has its low 29 mantissa bits clear, so lo,
+// counted in those units, is added to or subtracted from the bit pattern of |hi|
+// directly; a subtraction below a power of two lands in the binade beneath, whose
+// unit is half as large, and takes twice the count. lo bits below the double's
+// last place are dropped (an error under one unit). Zero, subnormal and
+// out-of-range cases go to the FP64 path out of line.
+__device__ __forceinline__ double df2d_scaled(float hi, float lo, int sh) {
+  {
+    const float s = __fadd_rn(hi, lo);
+    const float bp = __fsub_rn(s, hi);
+    lo = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(lo, bp));
+    hi = s;
+  }
+  const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
+  const uint32_t eh = (bh >> 23) & 0xFFu, el = (bl >> 23) & 0xFFu;
+  const int ed = (int)eh - 127 + 1023 + sh;
+  const int shift = (int)el - (int)eh + 29;
+  if (eh == 0u || eh == 0xFFu || el == 0xFFu || ed <= 1 || ed >= 2047 || shift > 5)
+    return df2d_scaled_slow(hi, lo, sh);
+  const uint32_t mh = bh & 0x7FFFFFu;
+  uint32_t k = 0u;
+  if (el != 0u) {
+    const uint32_t ml = (bl & 0x7FFFFFu) | 0x800000u;
+    k = shift >= 0 ? (ml << shift) : (shift > -24 ? (ml >> -shift) : 0u);
+  }
+  const bool opposite = ((bh ^ bl) >> 31) != 0u;
+  if (opposite && mh == 0u) k <<= 1;
+  unsigned long long mag = ((unsigned long long)ed << 52) | ((unsigned long long)mh << 29);
+  mag = opposite ? mag - k : mag + k;
+  return __longlong_as_double((long long)(mag | ((unsigned long long)(bh >> 31) << 63)));
+}
+
 // ---------------------------------------------------------------------------
 // the GEMM: C = alpha * A B^T + beta * C over the given K range
 // ---------------------------------------------------------------------------
@@ -527,9 +570,8 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
   } else if (warp == 1) {
     // ---- MMA issuer ----
     if (lane == 0) {
-      // D F32, A/B BF16, K-major both, N = 64, M = 128
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
-                             ((uint32_t)(OZ_BM >> 4) << 24);
+      // D F32, A/B BF16, K-major both, M = 128; N is set per instruction
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BM >> 4) << 24);
       // no-swizzle K-major: core matrices of 8 rows x 16 bytes; LBO steps K (128 B),
       // SBO steps 8 rows (8 x 32 K x 2 B = 512 B)
       const uint32_t lbo = 128u, sbo = 512u;
@@ -538,7 +580,7 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
       for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x) {
         OzTile t;
         if (!oz_tile_at(g, L, t) || t.nch == 0) continue;
-        uint32_t accmask = 0;
+        uint32_t fresh = 0;  // 1 while the group's accumulators are still to be overwritten
         for (int64_t c = 0; c < t.nch; ++c) {
           const bool gstart = (c % OZ_GROUP) == 0;
           const bool gend = ((c + 1) % OZ_GROUP) == 0 || c == t.nch - 1;
@@ -549,7 +591,7 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
               goto mma_done;
             }
             tc_fence_after();
-            accmask = 0;
+            fresh = 1;
           }
           if (!oz_wait(bar(FULL + st), ph, abort_flag)) {
             if (!*abort_flag) atomicExch(g.err, 2);
@@ -559,22 +601,34 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
           tc_fence_after();
           const uint32_t abase = smem_u32(smem + st * Cfg::STAGE);
           const uint32_t bbase = abase + S * Cfg::A_SL;
+          // Descriptors of the stage; slices and K steps are offsets in 16-byte units
+          // (shared addresses stay below 2^18, so the 14-bit address field never carries).
+          const uint64_t ad0 = umma_desc(abase, lbo, sbo), bd0 = umma_desc(bbase, lbo, sbo);
+          const uint32_t d0 = tmem + (uint32_t)(b * OZ_NACC * OZ_BN);
 #pragma unroll
           for (int kk = 0; kk < OZ_TK / 16; ++kk) {
 #pragma unroll
             for (int ti = 0; ti < S; ++ti) {
+              const uint64_t ad = ad0 + (uint64_t)((ti * Cfg::A_SL + kk * 256) >> 4);
+              // The B slices lie back to back with one 8-row stride, so slices
+              // 0..3-ti read as one operand of 64 (4 - ti) rows: a single MMA puts
+              // A_ti B_u^T (level ti + u) into accumulators ti..3, which are adjacent
+              // column blocks. Its first issue in a group overwrites all four.
+              if (ti < OZ_NACC)
+                umma_bf16(d0 + (uint32_t)(ti * OZ_BN), ad, bd0 + (uint64_t)((kk * 256) >> 4),
+                          idesc | ((uint32_t)((OZ_NACC - ti) * OZ_BN >> 3) << 17),
+                          (kk == 0 && ti == 0) ? (fresh ^ 1u) : 1u);
+              // the remaining products of levels > 3 go one by one into the last accumulator
 #pragma unroll
-              for (int ui = 0; ui < S; ++ui) {
+              for (int ui = ti < OZ_NACC ? OZ_NACC - ti : 0; ui < S; ++ui) {
                 if (ti + ui > S) continue;
-                const int acc = ti + ui < OZ_NACC - 1 ? ti + ui : OZ_NACC - 1;
-                const uint64_t ad = umma_desc(abase + ti * Cfg::A_SL + kk * 256, lbo, sbo);
-                const uint64_t bd = umma_desc(bbase + ui * Cfg::B_SL + kk * 256, lbo, sbo);
-                umma_bf16(tmem + (uint32_t)((b * OZ_NACC + acc) * OZ_BN), ad, bd, idesc,
-                          (accmask >> acc) & 1u);
-                accmask |= 1u << acc;
+                umma_bf16(d0 + (uint32_t)((OZ_NACC - 1) * OZ_BN), ad,
+                          bd0 + (uint64_t)((ui * Cfg::B_SL + kk * 256) >> 4),
+                          idesc | ((uint32_t)(OZ_BN >> 3) << 17), 1u);
               }
             }
           }
+          fresh = 0;
           mma_issued = true;
           umma_commit(bar(EMPTY + st));
           if (++st == NST) {
@@ -675,7 +729,7 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
               // the sign of alpha goes onto the FP32 pair
               const float h = __uint_as_float(__float_as_uint(hi[j]) ^ negmask);
               const float l = __uint_as_float(__float_as_uint(lo[j]) ^ negmask);
-              const double v = f2d_scaled(h, sh) + f2d_scaled(l, sh);
+              const double v = df2d_scaled(h, l, sh);
               out = beta0 ? v : cv[j] + v;
             } else {
               const double v = f2d_scaled(hi[j], sh) + f2d_scaled(lo[j], sh);
