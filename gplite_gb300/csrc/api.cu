@@ -175,8 +175,8 @@ void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters
   for (int it = 0; it < iters; ++it) {
     refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
     GPGP_CHECK_LAUNCH();
-    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
-    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
+    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
+    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
     vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
@@ -207,8 +207,8 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     GPGP_CHECK_LAUNCH();
     GPGP_CUDA(cudaMemcpyAsync(w.rhs.p, w.t1.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     unsigned *bar = (unsigned *)w.flags.p + 2;
-    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
-    trsv_coop(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, true, w.status.p, bar, m->errflag.p);
+    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
+    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, true, w.status.p, bar, m->errflag.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
     if (mixed) refine_alpha(m, w, alpha, fnew, refine < 0 ? std::max(1, m->opts.refine_iters) : refine);
@@ -286,7 +286,7 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
   w.logdet_part.alloc(st, (n + NB - 1) / NB + 1);
   w.tmpv.alloc(st, n);
   w.status.alloc(st, 1);
-  w.flags.alloc(st, 4);  // [0] site flags, [2..3] grid barrier of the solves
+  w.flags.alloc(st, 4 + (n + NB - 1) / NB);  // [0] site flags, [2..] ticket and block flags of the solves
   m->L.alloc(st, (size_t)n * n);
   m->Winv.alloc(st, (size_t)((n + NB - 1) / NB) * NB * NB);
   m->s.alloc(st, n);

@@ -170,10 +170,11 @@ void trsv_lower(cudaStream_t s, const double *L, int64_t n, int64_t lda, const d
                 double *b, double *x, const int *status);    // x = L^-1 b
 void trsv_lower_t(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
                   double *b, double *x, const int *status);  // x = L^-T b
-// Single-launch versions (cooperative grid with a bounded grid barrier): bar
-// holds two unsigned words of device scratch; err is set when a wait runs out.
-void trsv_coop(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
-               double *b, double *x, bool trans, const int *status, unsigned *bar, int *err);
+// Single-launch versions (blocks ordered by device flags, bounded waits): sync
+// holds n / 64 + 2 unsigned words of device scratch; err is set when a wait runs
+// out. b is not modified; x must not alias b.
+void trsv_flow(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
+               const double *b, double *x, bool trans, const int *status, unsigned *sync, int *err);
 // Substitution solves with a small lower factor L (M x M), as forwardsolve /
 // backsolve: rows of the n x M matrix B (mode 0: X = B L^-T, mode 1: X = B L^-1),
 // and vectors (x = L^-1 b, or L^-T b when trans).

@@ -500,143 +500,194 @@ void trsv_lower_t(cudaStream_t s, const double *L, int64_t n, int64_t lda, const
 }
 
 // ---------------------------------------------------------------------------
-// single-launch triangular solves: a cooperative grid walks the diagonal blocks
-// and meets at a bounded grid barrier after every block
+// single-launch triangular solves, ordered by per-block flags
 // ---------------------------------------------------------------------------
-// bar[0] = arrival count, bar[1] = generation; both zero at launch. Returns
-// false (and sets *err) when the wait runs out; every block then leaves.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *err) {
-  __shared__ int ok_sh;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok_sh = 1;
-    volatile unsigned *gen = bar + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    const unsigned arrived = atomicAdd(bar, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      unsigned it = 0;
-      while (*gen == g) {
-        if (++it > (1u << 26)) {
-          atomicExch(err, 3);
-          ok_sh = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return ok_sh != 0;
-}
+// A persistent grid takes the 64-row blocks of x in dependency order from a
+// ticket (forward: first block first; transposed: last block first), so every
+// block a CTA waits for belongs to a CTA that is already running. The CTA of
+// block i subtracts L_ij x_j (L_ji^T x_j when transposed) for each earlier block
+// j as soon as that block's flag is set, then multiplies by the diagonal block's
+// inverse W_ii, writes x_i and sets its flag. Each thread visits the blocks in a
+// fixed order, so the result does not depend on timing. Waits are bounded: when
+// one runs out the kernel sets *err = 3 and every CTA leaves.
+// sync: [0] ticket, [1 + blk] done flag of block blk; zeroed before the launch.
+constexpr int FLOW_BATCH = 8;  // earlier blocks applied per round
 
-__global__ void __launch_bounds__(256) trsv_coop_kernel(const double *__restrict__ L, int64_t n,
-                                                        int64_t lda, const double *__restrict__ Winv,
-                                                        double *b, double *x, int trans,
-                                                        const int *__restrict__ status,
-                                                        unsigned *bar, int *err) {
-  __shared__ double Ws[NB][NB + 1];  // the diagonal block's inverse
-  __shared__ double bk[NB];
-  __shared__ double xk[NB];
-  __shared__ double part[8][33];
+__global__ void __launch_bounds__(256) trsv_flow_kernel(const double *__restrict__ L, int64_t n, int64_t lda,
+                                                        const double *__restrict__ Winv,
+                                                        const double *__restrict__ b, double *x, int trans,
+                                                        const int *__restrict__ status, unsigned *sync,
+                                                        int *err) {
+  __shared__ double Ws[NB][NB + 1];
+  __shared__ double xs[FLOW_BATCH][NB];
+  __shared__ double vs[NB];
+  __shared__ double red[4][NB + 1];
+  __shared__ int64_t step_sh;
+  __shared__ int k_sh;
   if (*(volatile const int *)status != 0) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t nblk = (n + NB - 1) / NB;
-  const unsigned G = gridDim.x;
-  for (int64_t step = 0; step < nblk; ++step) {
+  volatile unsigned *done = sync + 1;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) step_sh = (int64_t)atomicAdd(sync, 1u);
+    __syncthreads();
+    const int64_t step = step_sh;
+    if (step >= nblk) return;
     const int64_t blk = trans ? nblk - 1 - step : step;
     const int64_t k0 = blk * NB;
     const int kb = (int)((n - k0) < NB ? (n - k0) : NB);
     const double *W = Winv + blk * NB * NB;
-    // stage W (coalesced) and this block of b
     for (int idx = tid; idx < NB * NB; idx += 256) Ws[idx % NB][idx / NB] = W[idx];
-    if (tid < NB) bk[tid] = tid < kb ? __ldcg(b + k0 + tid) : 0.0;
-    __syncthreads();
-    {
-      // xk = W bk (lower W) or W^T bk: four threads per entry, partial sums by shuffles
-      const int row = tid >> 2, p = tid & 3;
-      double s = 0.0;
+    // forward: thread (r, p) takes row r of the block and columns 16p..16p+15 of
+    // every earlier block; transposed: warp w takes columns 8w..8w+7 of this block
+    // and lane l rows l, l + 32 of every later block
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    const int r = tid & 63, p = tid >> 6;
+    const int64_t ndep = trans ? nblk - 1 - blk : blk;
+    // This thread's 16 entries of the L tile of earlier block number d; the tile of
+    // the next block is always in flight (loaded before the wait for its flag and
+    // before the products with the current one).
+    auto load_tile = [&](int64_t d, double (&t)[16]) {
+      const int64_t j = trans ? nblk - 1 - d : d;
+      const int64_t j0 = j * NB;
+      const int jb = (int)((n - j0) < NB ? (n - j0) : NB);
       if (!trans) {
-        for (int c = p; c <= row && c < kb; c += 4) s = fma(Ws[row][c], bk[c], s);
+        const double *Lr = L + (k0 + r) + (j0 + 16 * p) * lda;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) t[q] = (r < kb && 16 * p + q < jb) ? Lr[q * lda] : 0.0;
       } else {
-        for (int r = row + p; r < kb; r += 4) s = fma(Ws[r][row], bk[r], s);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = warp * 8 + q;
+          const double *Lc = L + j0 + (k0 + c) * lda;
+          t[2 * q] = (c < kb && lane < jb) ? Lc[lane] : 0.0;
+          t[2 * q + 1] = (c < kb && lane + 32 < jb) ? Lc[lane + 32] : 0.0;
+        }
       }
+    };
+    double tnext[16];
+    if (ndep > 0) load_tile(0, tnext);
+    for (int64_t d0 = 0; d0 < ndep;) {
+      // warp 0 finds how many of the next (up to) eight blocks are done
+      if (warp == 0) {
+        const int avail = (int)((ndep - d0) < FLOW_BATCH ? (ndep - d0) : FLOW_BATCH);
+        int k = -1;
+        for (uint32_t it = 0; it < (1u << 21); ++it) {
+          const int64_t jl = trans ? nblk - 1 - (d0 + lane) : d0 + lane;
+          const bool ready = lane < avail && done[jl] != 0u;
+          const unsigned m = __ballot_sync(0xffffffffu, ready);
+          const int run = __ffs(~m) - 1;  // consecutive done blocks from d0
+          if (run > 0) {
+            k = run;
+            break;
+          }
+          if ((it & 1023u) == 1023u && *(volatile const int *)err != 0) break;
+          __nanosleep(64);
+        }
+        if (lane == 0) {
+          if (k < 0) atomicExch(err, 3);
+          k_sh = k;
+        }
+      }
+      __syncthreads();
+      const int k = k_sh;
+      if (k < 0) return;
+      __threadfence();
+      for (int idx = tid; idx < k * NB; idx += 256) {
+        const int dd = idx / NB, c = idx % NB;
+        const int64_t j = trans ? nblk - 1 - (d0 + dd) : d0 + dd;
+        xs[dd][c] = j * NB + c < n ? __ldcg(x + j * NB + c) : 0.0;
+      }
+      __syncthreads();
+      for (int dd = 0; dd < k; ++dd) {
+        double tc[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tc[q] = tnext[q];
+        if (d0 + dd + 1 < ndep) load_tile(d0 + dd + 1, tnext);
+        if (!trans) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) acc[q & 7] = fma(tc[q], xs[dd][16 * p + q], acc[q & 7]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[q] += fma(tc[2 * q + 1], xs[dd][lane + 32], tc[2 * q] * xs[dd][lane]);
+        }
+      }
+      __syncthreads();
+      d0 += k;
+    }
+    // v = b_blk - (the sum over the earlier blocks)
+    if (!trans) {
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) t += acc[q];
+      red[p][r] = t;
+      __syncthreads();
+      if (tid < NB) vs[tid] = tid < kb ? b[k0 + tid] - (((red[0][tid] + red[1][tid]) + red[2][tid]) + red[3][tid]) : 0.0;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        double t = acc[q];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        acc[q] = t;
+      }
+      if (lane < 8) {
+        const int c = warp * 8 + lane;
+        double t = acc[0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q) t = lane == q ? acc[q] : t;
+        vs[c] = c < kb ? b[k0 + c] - t : 0.0;
+      }
+    }
+    __syncthreads();
+    // x_blk = W v (lower W) or W^T v: four threads per entry, partial sums by shuffles
+    {
+      const int row = tid >> 2, pp = tid & 3;
+      double s0 = 0.0, s1 = 0.0;
+      if (!trans) {
+        for (int c = pp; c <= row && c < kb; c += 8) {
+          s0 = fma(Ws[row][c], vs[c], s0);
+          if (c + 4 <= row && c + 4 < kb) s1 = fma(Ws[row][c + 4], vs[c + 4], s1);
+        }
+      } else {
+        for (int rr = row + pp; rr < kb; rr += 8) {
+          s0 = fma(Ws[rr][row], vs[rr], s0);
+          if (rr + 4 < kb) s1 = fma(Ws[rr + 4][row], vs[rr + 4], s1);
+        }
+      }
+      double s = s0 + s1;
       s += __shfl_xor_sync(0xffffffffu, s, 1);
       s += __shfl_xor_sync(0xffffffffu, s, 2);
-      if (p == 0) xk[row] = row < kb ? s : 0.0;
+      if (pp == 0 && row < kb) {
+        x[k0 + row] = s;
+        __threadfence();
+      }
     }
     __syncthreads();
-    if (blockIdx.x == 0 && tid < kb) x[k0 + tid] = xk[tid];
-    if (!trans) {
-      // b[r] -= L[r, k0:k0+kb] xk for the rows below the block: 32 rows per pass of a
-      // block, warp w takes columns 8w..8w+7 (coalesced over the rows), then the eight
-      // partial sums of a row are added in a fixed order
-      for (int64_t r0 = k0 + kb + (int64_t)blockIdx.x * 32; r0 < n; r0 += (int64_t)G * 32) {
-        const int64_t r = r0 + lane;
-        double s = 0.0;
-        if (r < n) {
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int c = warp * 8 + q;
-            if (c < kb) s = fma(L[r + (k0 + c) * lda], xk[c], s);
-          }
-        }
-        part[warp][lane] = s;
-        __syncthreads();
-        if (warp == 0 && r < n) {
-          double t = 0.0;
-#pragma unroll
-          for (int w = 0; w < 8; ++w) t += part[w][lane];
-          b[r] = __ldcg(b + r) - t;
-        }
-        __syncthreads();
-      }
-    } else {
-      // b[c] -= sum_r L[r, c] xk[r] for the columns left of the block: eight lanes per
-      // column, each over eight contiguous rows, four columns per warp pass
-      const int sub = lane >> 3, l8 = lane & 7;
-      for (int64_t c0 = ((int64_t)blockIdx.x * 8 + warp) * 4; c0 < k0; c0 += (int64_t)G * 32) {
-        const int64_t c = c0 + sub;
-        double s = 0.0;
-        if (c < k0) {
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int rr = l8 * 8 + q;
-            if (rr < kb) s = fma(L[(k0 + rr) + c * lda], xk[rr], s);
-          }
-        }
-        s += __shfl_xor_sync(0xffffffffu, s, 1);
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        s += __shfl_xor_sync(0xffffffffu, s, 4);
-        if (l8 == 0 && c < k0) b[c] = __ldcg(b + c) - s;
-      }
+    if (tid == 0) {
+      __threadfence();
+      atomicExch((unsigned *)(done + blk), 1u);
     }
-    if (!grid_barrier(bar, G, err)) return;
   }
 }
 
-void trsv_coop(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
-               double *b, double *x, bool trans, const int *status, unsigned *bar, int *err) {
+void trsv_flow(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv, const double *b,
+               double *x, bool trans, const int *status, unsigned *sync, int *err) {
   if (n <= 0) return;
-  static const int g_coop_blocks = [] {
-    int dev = 0, sms = 0, per = 0;
+  static const int g_sms = [] {
+    int dev = 0, sms = 0;
     GPGP_CUDA(cudaGetDevice(&dev));
     GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    GPGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop_kernel, 256, 0));
-    return sms * std::max(1, std::min(per, 2));
+    return sms;
   }();
-  GPGP_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
-  int tr = trans ? 1 : 0;
-  void *args[] = {(void *)&L, (void *)&n, (void *)&lda, (void *)&Winv, (void *)&b, (void *)&x,
-                  (void *)&tr, (void *)&status, (void *)&bar, (void *)&err};
+  const int64_t nblk = (n + NB - 1) / NB;
+  GPGP_CUDA(cudaMemsetAsync(sync, 0, (size_t)(nblk + 1) * sizeof(unsigned), s));
+  const unsigned grid = (unsigned)std::min<int64_t>(nblk, g_sms);
   KTScope kts(GPGP_KPROF_TRSV, s, (double)n * (double)n);
-  GPGP_CUDA(cudaLaunchCooperativeKernel((const void *)trsv_coop_kernel, dim3(g_coop_blocks), dim3(256),
-                                        args, 0, s));
-  GPGP_LAUNCHED();
+  trsv_flow_kernel<<<grid, 256, 0, s>>>(L, n, lda, Winv, b, x, trans ? 1 : 0, status, sync, err);
+  GPGP_CHECK_LAUNCH();
 }
 
 // ---------------------------------------------------------------------------
