@@ -207,25 +207,33 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
                  tri_mode);
 }
 
-// 1/sqrt(x) by two Newton-Raphson steps y <- y (3 - x y^2) / 2 from the FP32
-// hardware estimate (relative error ~2^-22 -> 2^-44 -> rounding level): eight
-// FP64 operations instead of a correctly rounded square root and division,
-// which matters on a part whose FP64 pipe runs one warp instruction per 64
-// cycles. Arguments outside the FP32 range take sqrt and division.
-__device__ __forceinline__ double rsqrt_newton(double x) {
-  if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
-  double y = (double)rsqrtf((float)x);
-  const double hx = 0.5 * x;
-  y = y * fma(-hx, y * y, 1.5);
-  y = y * fma(-hx, y * y, 1.5);
-  return y;
+__device__ __noinline__ double rsqrt_slow(double x) { return 1.0 / sqrt(x); }
+
+// 1/sqrt(x) for a positive finite x. The FP32 estimate rsqrtf(x) comes from a
+// float built out of x's bits with integer operations (and goes back the same
+// way), so no FP64 conversion or compare sits on the pivot chain; the estimate
+// y0 (relative error ~2^-22) is refined by the binomial series
+//   (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 + O(e^3),  e = 1 - x y0^2,
+// four dependent FP64 operations whose neglected terms are ~2^-66. Arguments
+// outside the float range take sqrt and division out of line.
+__device__ __forceinline__ double rsqrt_fast(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)(b >> 52);
+  if (E < 1023 - 125 || E > 1023 + 125) return rsqrt_slow(x);
+  const float xf = __uint_as_float(((uint32_t)(E - 1023 + 127) << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+  const uint32_t yb = __float_as_uint(rsqrtf(xf));
+  const double y0 = __longlong_as_double(
+      (long long)(((unsigned long long)(((yb >> 23) & 0xFFu) - 127u + 1023u) << 52) |
+                  ((unsigned long long)(yb & 0x7FFFFFu) << 29)));
+  const double e = fma(-(x * y0), y0, 1.0);
+  return fma(y0 * e, fma(e, 0.375, 0.5), y0);
 }
 
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
-// Factor: right-looking over the 64 columns; warp 0 takes the pivots (Newton
-// inverse square root) one column ahead while warps 1-7 apply the rank-1
+// Factor: right-looking over the 64 columns; warp 0 takes the pivots (inverse
+// square root, rsqrt_fast) one column ahead while warps 1-7 apply the rank-1
 // updates, one barrier per column. Inverse W = L^-1 by forward substitution over the
 // rows, all columns at once with four threads per column (partial dot
 // products combined by shuffles); a column only depends on itself, so rows
@@ -258,14 +266,16 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   // pivot of column j by warp 0: L_jj and the scaled column below it
   auto pivot = [&](int j) {
     const double dj = S[j][j];
-    if (!(dj > 0.0) || !isfinite(dj)) {
+    // not positive (sign bit or zero) or not finite, tested on the bits
+    const long long djb = __double_as_longlong(dj);
+    if (djb <= 0ll || (djb >> 52) >= 0x7FFll) {
       if (lane == 0) {
         failed = 1;
         atomicCAS(status, 0, (int)(k0 + j + 1));
       }
       return;
     }
-    const double rp = rsqrt_newton(dj);
+    const double rp = rsqrt_fast(dj);
     const double piv = dj * rp;
     for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
     if (lane == 0) {
