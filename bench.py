@@ -440,7 +440,10 @@ def run_gpu(args):
             "kernels_ms_per_step": {k: {"launches": v["launches"], "ms": v["ms"]}
                                     for k, v in head["kernels"].items()},
             "profile_note": "phases_ms and kernels_ms_per_step: per step, from a separate profiled pass of 2 "
-                            "steps (CUDA events around phases and launches); the timed steps run without them",
+                            "steps (CUDA events around phases and launches); the timed steps run without them. "
+                            "In the profiled pass the mixed Cholesky runs on one stream, so that every launch is "
+                            "timed alone; the timed steps overlap each panel with the previous trailing update "
+                            "(a second stream), so their potrf phase is shorter than phases_ms shows",
             "log_evidence_last": head["lmls"][-1],
         }
         if "fp64" in res and precs[0] != "fp64":
@@ -905,7 +908,7 @@ def main():
     ap.add_argument("--c1-reps", type=int, default=200)
     ap.add_argument("--c3-n", type=int, default=8192)
     ap.add_argument("--window", type=float, default=2.0)
-    ap.add_argument("--workers", type=int, default=6)
+    ap.add_argument("--workers", type=int, default=12)
     ap.add_argument("--plain-budget", type=float, default=40.0)
     ap.add_argument("--batch-count", type=int, default=4096)
     args = ap.parse_args()

@@ -196,7 +196,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   {
     Phase ph(ctx, GPGP_PHASE_POTRF);
     if (mixed)
-      potrf_mixed(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p, m->errflag.p);
+      potrf_mixed(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p, m->errflag.p, &ctx->side);
     else
       potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
   }
@@ -595,6 +595,10 @@ gpgp_status gpgp_create(gpgp_ctx **out, int device) {
     GPGP_CUDA(cudaSetDevice(device));
     c->device = device;
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    GPGP_CUDA(cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking));
+    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming));
+    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.a, cudaEventDisableTiming));
+    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.l, cudaEventDisableTiming));
     GPGP_CUDA(cudaMallocHost((void **)&c->h_pinned, 64 * sizeof(double)));
     return GPGP_OK;
   });
@@ -609,6 +613,12 @@ gpgp_status gpgp_destroy(gpgp_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
   }
+  if (ctx->side.s) {
+    cudaStreamSynchronize(ctx->side.s);
+    cudaStreamDestroy(ctx->side.s);
+  }
+  for (cudaEvent_t e : {ctx->side.fork, ctx->side.a, ctx->side.l})
+    if (e) cudaEventDestroy(e);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   delete ctx;
   return GPGP_OK;

@@ -219,6 +219,21 @@ void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t ro
 void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
              int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
              double *C, int64_t ldc, bool lower_only, int *err, const int *status = nullptr);
+// Grid cap of the sliced GEMM on this thread (0: one CTA per SM), for launches
+// that share the GPU with work on another stream.
+extern thread_local int tl_oz_grid_cap;
+struct OzGridCap {
+  int old;
+  explicit OzGridCap(int cap) : old(tl_oz_grid_cap) { tl_oz_grid_cap = cap; }
+  ~OzGridCap() { tl_oz_grid_cap = old; }
+};
+int oz_sms();  // SMs of the current device
+// A second stream with three events, owned by a context, for work that runs
+// beside its main stream.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, a = nullptr, l = nullptr;
+};
 // Batched versions: problem z uses P + z sP and the split's batch strides (set
 // bstride_ex / bstride_sl before splitting); C + z sC; status + z status_bs.
 void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, int trans, int64_t rows,
@@ -229,8 +244,10 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
                      const int *status, int64_t status_bs, int64_t batch);
 
 // Mixed-precision factorisation and inverses (same outputs as the FP64 versions).
+// With a side stream, panel p + 1 is factored on it while the main stream
+// finishes the trailing update of panel p (identical results).
 void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,
-                 double *logdet_part, int *status, int *err);
+                 double *logdet_part, int *status, int *err, const SideStream *side = nullptr);
 void trtri_mixed(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv,
                  double *W, int64_t ldw, int *err);
 // Binv (lower) = W^T W for lower-triangular W

@@ -763,6 +763,8 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
   }
 }
 
+thread_local int tl_oz_grid_cap = 0;
+
 static int oz_sm_count() {
   static const int n = [] {
     int dev = 0, sms = 0;
@@ -819,7 +821,8 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   g.gy = (N + OZ_BN - 1) / OZ_BN;
   g.batch = batch;
   const int64_t ntiles = g.gx * g.gy * batch;
-  const int64_t grid = std::min<int64_t>(ntiles, oz_sm_count());
+  const int64_t cap = tl_oz_grid_cap > 0 ? std::min(tl_oz_grid_cap, oz_sm_count()) : oz_sm_count();
+  const int64_t grid = std::min<int64_t>(ntiles, cap);
   double fl = 0.0;
   if (tl_kt) {
     // executed MMA arithmetic of the tiles the launch runs (the kernel's own tile
@@ -847,6 +850,8 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
   }
   GPGP_CHECK_LAUNCH();
 }
+
+int oz_sms() { return oz_sm_count(); }
 
 void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
              int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,

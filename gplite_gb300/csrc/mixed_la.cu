@@ -47,45 +47,102 @@ struct SplitBuf {
 };
 
 constexpr int64_t NBO = 256;  // outer panel width of the mixed Cholesky
+// Lookahead: a trailing update of at least LOOK_MIN_ROWS rows leaves LOOK_PANEL_SMS
+// SMs to the next panel's factorisation, whose GEMMs are capped to them.
+constexpr int64_t LOOK_MIN_ROWS = 6144;
+constexpr int LOOK_PANEL_SMS = 32;
+
+// The 64-wide blocks of the outer panel [k0, k0 + kbo): FP64 factor and inverse of
+// the diagonal block, L21 = A21 W^T for every row below it (sliced GEMM), then the
+// update of the panel's remaining columns.
+void factor_panel(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
+                  int *status, int *err, int64_t k0, int64_t kbo, SplitBuf &a, SplitBuf &w) {
+  for (int64_t j0 = k0; j0 < k0 + kbo; j0 += NB) {
+    const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
+    const int64_t blk = j0 / NB;
+    double *Wb = Winv + blk * NB * NB;
+    {
+      KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * jb * jb * jb / 3);
+      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
+    }
+    GPGP_CHECK_LAUNCH();
+    const int64_t m = n - j0 - jb;
+    if (m <= 0) continue;
+    double *A21 = A + (j0 + jb) + j0 * lda;
+    // L21 = A21 W^T (W = L11^-1): sliced GEMM, result written over A21
+    oz_split(s, A21, lda, 0, m, jb, &a.sp);
+    oz_split(s, Wb, NB, 0, jb, jb, &w.sp);
+    oz_gemm(s, a.sp, 0, w.sp, 0, m, jb, 0, 1, 0, 1.0, 0.0, A21, lda, false, err, status);
+    // update of the remaining columns of this outer panel
+    const int64_t nc = k0 + kbo - (j0 + jb);
+    if (nc > 0) {
+      oz_split(s, A21, lda, 0, m, jb, &a.sp);
+      oz_gemm(s, a.sp, 0, a.sp, 0, m, nc, 0, 1, 0, -1.0, 1.0, A + (j0 + jb) + (j0 + jb) * lda, lda,
+              true, err, status);
+    }
+  }
+}
 
 }  // namespace
 
 void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,
-                 double *logdet_part, int *status, int *err) {
+                 double *logdet_part, int *status, int *err, const SideStream *side) {
   SplitBuf a(s, n, NBO);   // panel operand (rows below the current block)
   SplitBuf w(s, NB, NB);   // inverse of the diagonal block
-  for (int64_t k0 = 0; k0 < n; k0 += NBO) {
-    const int64_t kbo = std::min<int64_t>(NBO, n - k0);
-    for (int64_t j0 = k0; j0 < k0 + kbo; j0 += NB) {
-      const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
-      const int64_t blk = j0 / NB;
-      double *Wb = Winv + blk * NB * NB;
-      {
-        KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * jb * jb * jb / 3);
-        potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
-      }
-      GPGP_CHECK_LAUNCH();
-      const int64_t m = n - j0 - jb;
-      if (m <= 0) continue;
-      double *A21 = A + (j0 + jb) + j0 * lda;
-      // L21 = A21 W^T (W = L11^-1): sliced GEMM, result written over A21
-      oz_split(s, A21, lda, 0, m, jb, &a.sp);
-      oz_split(s, Wb, NB, 0, jb, jb, &w.sp);
-      oz_gemm(s, a.sp, 0, w.sp, 0, m, jb, 0, 1, 0, 1.0, 0.0, A21, lda, false, err, status);
-      // update of the remaining columns of this outer panel
-      const int64_t nc = k0 + kbo - (j0 + jb);
-      if (nc > 0) {
-        oz_split(s, A21, lda, 0, m, jb, &a.sp);
-        oz_gemm(s, a.sp, 0, a.sp, 0, m, nc, 0, 1, 0, -1.0, 1.0, A + (j0 + jb) + (j0 + jb) * lda, lda,
-                true, err, status);
+  cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
+  GPGP_CUDA(cudaStreamIsCapturing(s, &cap_st));
+  // Per-kernel timers (tl_kt) time each launch alone, so a profiled call runs the
+  // single-stream schedule.
+  if (!side || !side->s || n <= 2 * NBO || cap_st != cudaStreamCaptureStatusNone || tl_kt) {
+    for (int64_t k0 = 0; k0 < n; k0 += NBO) {
+      const int64_t kbo = std::min<int64_t>(NBO, n - k0);
+      factor_panel(s, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w);
+      const int64_t m2 = n - k0 - kbo;
+      if (m2 > 0) {
+        double *P = A + (k0 + kbo) + k0 * lda;
+        oz_split(s, P, lda, 0, m2, kbo, &a.sp);
+        oz_gemm(s, a.sp, 0, a.sp, 0, m2, m2, 0, (kbo + 63) / 64, 0, -1.0, 1.0,
+                A + (k0 + kbo) + (k0 + kbo) * lda, lda, true, err, status);
       }
     }
+    return;
+  }
+  // Lookahead. The side stream factors the panels; the main stream applies each
+  // finished panel p to the next panel's columns first, releases the side stream
+  // (event a), and then applies p to the rest of the trailing matrix while panel
+  // p + 1 is factored beside it (the two touch disjoint columns). Every product
+  // is the one the plain schedule computes, so the factor is the same.
+  SplitBuf t(s, n, NBO);  // panel p as the trailing update's operand
+  cudaStream_t x = side->s;
+  GPGP_CUDA(cudaEventRecord(side->fork, s));
+  GPGP_CUDA(cudaStreamWaitEvent(x, side->fork, 0));
+  const int sms = oz_sms();
+  int panel_cap = 0;
+  for (int64_t k0 = 0; k0 < n; k0 += NBO) {
+    const int64_t kbo = std::min<int64_t>(NBO, n - k0);
+    {
+      OzGridCap cap(panel_cap);
+      factor_panel(x, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w);
+    }
+    GPGP_CUDA(cudaEventRecord(side->l, x));
+    GPGP_CUDA(cudaStreamWaitEvent(s, side->l, 0));
     const int64_t m2 = n - k0 - kbo;
-    if (m2 > 0) {
-      double *P = A + (k0 + kbo) + k0 * lda;
-      oz_split(s, P, lda, 0, m2, kbo, &a.sp);
-      oz_gemm(s, a.sp, 0, a.sp, 0, m2, m2, 0, (kbo + 63) / 64, 0, -1.0, 1.0,
-              A + (k0 + kbo) + (k0 + kbo) * lda, lda, true, err, status);
+    if (m2 <= 0) break;
+    double *P = A + (k0 + kbo) + k0 * lda;
+    double *C = A + (k0 + kbo) + (k0 + kbo) * lda;
+    oz_split(s, P, lda, 0, m2, kbo, &t.sp);
+    const int64_t nb2 = std::min<int64_t>(NBO, m2);
+    oz_gemm(s, t.sp, 0, t.sp, 0, m2, nb2, 0, (kbo + 63) / 64, 0, -1.0, 1.0, C, lda, true, err, status);
+    GPGP_CUDA(cudaEventRecord(side->a, s));
+    GPGP_CUDA(cudaStreamWaitEvent(x, side->a, 0));
+    const int64_t m3 = m2 - nb2;
+    panel_cap = 0;
+    if (m3 > 0) {
+      const bool share = m3 >= LOOK_MIN_ROWS && sms > 2 * LOOK_PANEL_SMS;
+      if (share) panel_cap = LOOK_PANEL_SMS;
+      OzGridCap cap(share ? sms - LOOK_PANEL_SMS : 0);
+      oz_gemm(s, t.sp, nb2, t.sp, nb2, m3, m3, 0, (kbo + 63) / 64, 0, -1.0, 1.0, C + nb2 + nb2 * lda, lda,
+              true, err, status);
     }
   }
 }

@@ -21,6 +21,7 @@ struct gpgp_ctx {
   double prof_ms[GPGP_NPHASE] = {0};
   int64_t prof_calls[GPGP_NPHASE] = {0};
   gpgp::KernelTimer kt;
+  gpgp::SideStream side;  // lookahead stream of the mixed Cholesky
 };
 
 namespace gpgp {
