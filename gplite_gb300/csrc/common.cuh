@@ -216,6 +216,8 @@ void oz_split(cudaStream_t s, const double *P, int64_t ld, int trans, int64_t ro
               OzSplit *out);
 // C = alpha A B^T + beta C on K chunks [kc0, kc1) (64 wide); a_row0/b_row0 multiples of 64.
 // kmode: 0 all chunks; 1 start at max(row, col); 2 start at col; 3 stop after row.
+// status (optional): the launch is skipped for a problem whose word is nonzero; the
+// word must not change while the launch runs (each role of a CTA reads it).
 void oz_gemm(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
              int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha, double beta,
              double *C, int64_t ldc, bool lower_only, int *err, const int *status = nullptr);

@@ -141,8 +141,10 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
       const bool share = m3 >= LOOK_MIN_ROWS && sms > 2 * LOOK_PANEL_SMS;
       if (share) panel_cap = LOOK_PANEL_SMS;
       OzGridCap cap(share ? sms - LOOK_PANEL_SMS : 0);
+      // no status word: the side stream's diagonal kernels may set it while this
+      // launch runs, and every role of a GEMM CTA must see the same value
       oz_gemm(s, t.sp, nb2, t.sp, nb2, m3, m3, 0, (kbo + 63) / 64, 0, -1.0, 1.0, C + nb2 + nb2 * lda, lda,
-              true, err, status);
+              true, err, nullptr);
     }
   }
 }
