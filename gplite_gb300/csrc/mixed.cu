@@ -397,6 +397,9 @@ __device__ __forceinline__ double df2d_scaled(float hi, float lo, int sh) {
     hi = s;
   }
   const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
+  // a zero sum (hi = 0 forces lo = 0 after TwoSum): common in zero-padded and
+  // triangular operands, so it stays off the slow path
+  if ((bh << 1) == 0u) return 0.0;
   const uint32_t eh = (bh >> 23) & 0xFFu, el = (bl >> 23) & 0xFFu;
   const int ed = (int)eh - 127 + 1023 + sh;
   const int shift = (int)el - (int)eh + 29;
