@@ -6,11 +6,11 @@
 // R/laplace.R:30, R/gp_pred.R:209).
 //
 // The factorisation is blocked right-looking with NB = 64: the diagonal block
-// is factored by one CTA in shared memory, which also inverts it; the panel
-// below is the product with that inverse (stable here because every diagonal
-// block of B = I + V^-1/2 K V^-1/2 has eigenvalues >= 1); the trailing update
-// is a lower-only GEMM. Only the trailing update is a contraction worth the
-// tensor cores; on this part the plain FP64 path runs it on the FP64 pipe.
+// is factored by one CTA in shared memory, which also inverts it (the inverses
+// serve the solves); the panel below is solved by row-parallel substitution,
+// which stays backward stable when a diagonal block is ill-conditioned (FITC's
+// K_z); the trailing update is a lower-only GEMM on the FP64 pipe. The
+// triangular solves are single launches ordered by per-block flags.
 #include <math.h>
 
 #include <algorithm>
