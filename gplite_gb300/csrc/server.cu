@@ -141,8 +141,10 @@ void estimate(const gpgp_server *s, Req *r) {
     return;
   }
   const double iters = r->lik.kind == GPGP_LIK_GAUSSIAN ? 1.0 : 8.0;
-  r->bytes = (int64_t)(8.0 * ((mixed ? 5.0 : 3.0) * n * n + 2.0 * n * std::min(m, 4096.0) + 64.0 * n +
-                              20.0 * n) + (4 << 20));
+  // n x 64 diagonal inverses; mixed adds two n x 256 four-slice panel operands
+  // (the Cholesky's panel and its lookahead trailing update), 256 n doubles each
+  r->bytes = (int64_t)(8.0 * ((mixed ? 5.0 : 3.0) * n * n + 2.0 * n * std::min(m, 4096.0) +
+                              (mixed ? 576.0 : 64.0) * n + 20.0 * n) + (4 << 20));
   r->resident = (int64_t)(8.0 * (2.0 * n * n + 64.0 * n + 12.0 * n));
   r->work = iters * n * n * n / 3.0 + n * n * m;
 }
