@@ -116,6 +116,16 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
   cudaStream_t x = side->s;
   GPGP_CUDA(cudaEventRecord(side->fork, s));
   GPGP_CUDA(cudaStreamWaitEvent(x, side->fork, 0));
+  // The main stream waits for the side stream before the buffers above are freed,
+  // also when an error leaves the loop early (destroyed before them).
+  struct Join {
+    const SideStream *sd;
+    cudaStream_t main;
+    ~Join() {
+      cudaEventRecord(sd->l, sd->s);
+      cudaStreamWaitEvent(main, sd->l, 0);
+    }
+  } join{side, s};
   const int sms = oz_sms();
   int panel_cap = 0;
   for (int64_t k0 = 0; k0 < n; k0 += NBO) {
