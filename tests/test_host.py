@@ -79,3 +79,21 @@ def test_gauss_hermite_host_matches_oracle():
         a, wa = gauss_hermite_points(q)
         b, wb = R.gauss_hermite_points(q)
         assert np.allclose(a, b, rtol=0, atol=1e-13) and np.allclose(wa, wb, rtol=1e-12)
+
+
+def test_stale_fit_is_refused_before_any_device_call():
+    """test_pred.R:85-120 / test_loo.R:114-144: after set_param, gp_pred, gp_draw, gp_loo
+    and gp_energy refuse a model that still holds the old posterior, until it is refitted;
+    the check is host logic and runs before any device work."""
+    import pytest
+    gp = G.gp_init(G.cf_sexp(), G.lik_gaussian())
+    gp.fit = {"type": "analytic"}  # a posterior from an earlier fit
+    _, p = G.get_param(gp)
+    p[0] = 0.0
+    G.set_param(gp, p)
+    x = np.zeros((3, 1))
+    for call in (lambda: G.gp_pred(gp, x, var=True), lambda: G.gp_pred(gp, x),
+                 lambda: G.gp_draw(gp, x, draws=1), lambda: G.gp_loo(gp, x, np.zeros(3)),
+                 lambda: G.gp_energy(gp)):
+        with pytest.raises(RuntimeError, match="refit"):
+            call()
