@@ -159,6 +159,9 @@ typedef struct gpgp_ctx gpgp_ctx;
 typedef struct gpgp_model gpgp_model;
 
 /* ---- context ---------------------------------------------------------- */
+/* A context owns a CUDA stream (all its work is ordered on it) and a side
+   stream that the mixed-precision Cholesky uses for its lookahead; calls on one
+   context must not overlap, separate contexts may run from separate threads. */
 gpgp_status gpgp_create(gpgp_ctx **ctx, int device);
 gpgp_status gpgp_destroy(gpgp_ctx *ctx);
 const char *gpgp_status_string(gpgp_status s);
