@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -61,6 +62,31 @@ struct KTScope {
     GPGP_LAUNCHED();                     \
     GPGP_CUDA(cudaPeekAtLastError());    \
   } while (0)
+
+// A value computed once per device: function attributes (dynamic shared-memory
+// limits) and device properties belong to the device that is current when
+// they are set or read, so a process that drives several GPUs must set them
+// on each. per_device(pd, fn) returns fn() for the current device, calling it
+// at most once per device (devices >= 64 call it every time). Thread-safe.
+struct PerDevice {
+  std::mutex mu;
+  uint64_t done = 0;
+  int val[64] = {0};
+};
+template <class F>
+int per_device(PerDevice &pd, F &&fn) {
+  int dev = 0;
+  GPGP_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fn();
+  std::lock_guard<std::mutex> g(pd.mu);
+  if (!((pd.done >> dev) & 1ull)) {
+    pd.val[dev] = fn();
+    pd.done |= 1ull << dev;
+  }
+  return pd.val[dev];
+}
+// SMs of the current device (cached per device).
+int device_sms();
 
 // ---------------------------------------------------------------------------
 // covariance program on the device

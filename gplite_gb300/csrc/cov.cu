@@ -17,6 +17,16 @@ std::atomic<int64_t> g_launches{0};
 thread_local bool tl_capturing = false;
 thread_local KernelTimer *tl_kt = nullptr;
 
+int device_sms() {
+  static PerDevice sms;
+  return per_device(sms, [] {
+    int dev = 0, n = 0;
+    GPGP_CUDA(cudaGetDevice(&dev));
+    GPGP_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    return n;
+  });
+}
+
 KTScope::KTScope(int kernel, cudaStream_t st, double flops) : s(st), k(kernel) {
   if (!tl_kt || tl_capturing) return;
   if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
@@ -353,12 +363,12 @@ void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const 
   if (n1 == 0 || n2 == 0) return;
   const int lds = (dk.nfeat | 1);
   size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
-  static const bool attr_set = [] {
+  static PerDevice attr;
+  per_device(attr, [] {
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    2 * CT * 65 * 8 + CT * (CT + 1) * 8));
-    return true;
-  }();
-  (void)attr_set;
+    return 1;
+  });
   const int64_t T1 = (n1 + CT - 1) / CT, T2 = (n2 + CT - 1) / CT;
   if (sym) {
     int64_t nt = T1 * (T1 + 1) / 2;
@@ -443,12 +453,12 @@ void cov_matvec(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const 
   if (n1 == 0) return;
   const int lds = (dk.nfeat | 1);
   size_t smem = (size_t)(2 * CT * lds + CT + 4 * CT) * sizeof(double);
-  static const bool attr_set = [] {
+  static PerDevice attr;
+  per_device(attr, [] {
     GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (2 * CT * 65 + 5 * CT) * 8));
-    return true;
-  }();
-  (void)attr_set;
+    return 1;
+  });
   unsigned nb = (unsigned)((n1 + CT - 1) / CT);
   cov_matvec_kernel<<<nb, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, v, out);
   GPGP_CHECK_LAUNCH();
@@ -632,12 +642,12 @@ gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double 
                               int64_t n, const double *W, int64_t ldw, double *part, double *g) {
   const int lds = (dk.nfeat | 1);
   size_t smem = (size_t)(2 * GT * lds + 256) * sizeof(double);
-  static const bool attr_set = [] {
+  static PerDevice attr;
+  per_device(attr, [] {
     GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (2 * GT * 65 + 256) * 8));
-    return true;
-  }();
-  (void)attr_set;
+    return 1;
+  });
   int64_t T = (n + GT - 1) / GT;
   int64_t nt = T * (T + 1) / 2;
   cov_grad_kernel<<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);

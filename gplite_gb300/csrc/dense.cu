@@ -686,12 +686,7 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const double *__restrict
 void trsv_flow(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv, const double *b,
                double *x, bool trans, const int *status, unsigned *sync, int *err) {
   if (n <= 0) return;
-  static const int g_sms = [] {
-    int dev = 0, sms = 0;
-    GPGP_CUDA(cudaGetDevice(&dev));
-    GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    return sms;
-  }();
+  const int g_sms = device_sms();
   const int64_t nblk = (n + NB - 1) / NB;
   GPGP_CUDA(cudaMemsetAsync(sync, 0, (size_t)(nblk + 1) * sizeof(unsigned), s));
   const unsigned grid = (unsigned)std::min<int64_t>(nblk, g_sms);

@@ -768,15 +768,7 @@ __global__ void __maxnreg__(96) oz_gemm_kernel(const OzGemmArgs g) {
 
 thread_local int tl_oz_grid_cap = 0;
 
-static int oz_sm_count() {
-  static const int n = [] {
-    int dev = 0, sms = 0;
-    GPGP_CUDA(cudaGetDevice(&dev));
-    GPGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    return sms;
-  }();
-  return n;
-}
+static int oz_sm_count() { return device_sms(); }
 
 void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzSplit &B, int64_t b_row0,
                      int64_t M, int64_t N, int64_t kc0, int64_t kc1, int kmode, double alpha,
@@ -784,12 +776,12 @@ void oz_gemm_batched(cudaStream_t s, const OzSplit &A, int64_t a_row0, const OzS
                      const int *status, int64_t status_bs, int64_t batch) {
   if (M <= 0 || N <= 0 || batch <= 0) return;
   if (A.S != B.S) throw CudaError{cudaErrorInvalidValue, "oz_gemm: operands split to different slice counts", __LINE__};
-  static const bool attr = [] {
+  static PerDevice attr;
+  per_device(attr, [] {
     GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<4>::SMEM));
     GPGP_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<5>::SMEM));
-    return true;
-  }();
-  (void)attr;
+    return 1;
+  });
   OzGemmArgs g;
   g.a_sl = A.sl;
   g.a_ex = A.ex;

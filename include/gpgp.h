@@ -407,11 +407,13 @@ gpgp_status gpgp_server_destroy(gpgp_server *s);
  * All scratch lives in one fixed device array of the library (about 4.8 MB,
  * held by every GPU that loads the library until the process exits), so the
  * call never allocates. Limits: n <= 512 and at most 64 feature columns,
- * otherwise GPGP_EINVAL. The first call on a device looks up the array's
- * device address (make it before any stream capture) and needs the
- * context's device current. Calls share the array: calls whose GPU work
- * overlaps race on it and must be serialised. Returns GPGP_ENOT_PD (and
- * -Inf) when the factorisation fails. */
+ * otherwise GPGP_EINVAL. The call makes the context's device current; its
+ * first call for a device also looks up the array's device address, so make
+ * that first call before any stream capture begins. Calls share the array:
+ * calls whose GPU work overlaps race on it and must be serialised. Each call
+ * waits for its own GPU work before it returns. Returns GPGP_ENAN (and a NaN
+ * evidence) for NaN or Inf in x or y, GPGP_ENOT_PD (and -Inf) when the
+ * factorisation fails. */
 gpgp_status gpgp_fit_gaussian_noalloc(gpgp_ctx *ctx, const gpgp_kernel *k, double sigma,
                                       double jitter, const double *x, int64_t n, int32_t d,
                                       const double *y, double *alpha, double *log_evidence);

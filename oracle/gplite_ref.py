@@ -108,24 +108,25 @@ def get_param(gp):
     return names + n_, np.array(vals + v_, dtype=np.float64)
 
 
-def _set_param_cf(cf, vals):
-    """set_param.cf / .cf_periodic / .cf_prod (R/cf.R:348-396). Returns #consumed."""
+def _set_param_cf(cf, vals, exp=math.exp):
+    """set_param.cf / .cf_periodic / .cf_prod (R/cf.R:348-396). Returns #consumed.
+    (exp = np.exp lets the complex-step derivative check set complex values.)"""
     if cf.kind == "prod":
         j = 0
         for c in cf.cfs:
-            j += _set_param_cf(c, vals[j:])
+            j += _set_param_cf(c, vals[j:], exp)
         return j
     if cf.kind == "periodic":
         j = 0
         if not _is_fixed(cf, "period"):
-            cf.period = math.exp(vals[0])
+            cf.period = exp(vals[0])
             j = 1
-        return j + _set_param_cf(cf.base, vals[j:])
+        return j + _set_param_cf(cf.base, vals[j:], exp)
     j = 0
     for nm in PARAM_NAMES[cf.kind]:
         if _is_fixed(cf, nm):
             continue
-        setattr(cf, nm, math.exp(vals[j]))
+        setattr(cf, nm, exp(vals[j]))
         j += 1
     return j
 
@@ -197,7 +198,9 @@ def lpdf_prior(gp):
 # ----------------------------------------------------------------------------
 
 def as_matrix(x):
-    x = np.asarray(x, dtype=np.float64)
+    x = np.asarray(x)
+    if not np.iscomplexobj(x):  # complex only in the complex-step derivative check
+        x = x.astype(np.float64, copy=False)
     return x.reshape(-1, 1) if x.ndim == 1 else x
 
 
@@ -228,7 +231,8 @@ def learn_scales(cfs, x):
 
 def _sqdist(x1, x2):
     # sum(square(x1.row(i) - x2.row(j))) accumulated over columns in order (src/cf.cpp:37)
-    r2 = np.zeros((x1.shape[0], x2.shape[0]))
+    # (complex inputs only arise in the complex-step derivative check of the gradient)
+    r2 = np.zeros((x1.shape[0], x2.shape[0]), dtype=np.result_type(x1, x2, np.float64))
     for k in range(x1.shape[1]):
         diff = x1[:, k][:, None] - x2[:, k][None, :]
         r2 += diff * diff
@@ -237,7 +241,7 @@ def _sqdist(x1, x2):
 
 def _sqdist_diag(x1, x2):
     n = min(x1.shape[0], x2.shape[0])
-    r2 = np.zeros(n)
+    r2 = np.zeros(n, dtype=np.result_type(x1, x2, np.float64))
     for k in range(x1.shape[1]):
         diff = x1[:n, k] - x2[:n, k]
         r2 += diff * diff
@@ -314,9 +318,20 @@ def eval_cf_one(cf, x1, x2, diag_only=False):
     raise ValueError(cf.kind)
 
 
-def eval_cf(cfs, x1, x2, cfind=None, diag_only=False):
-    """eval_cf.list (R/cf.R:402-411): sum over the selected covariance functions."""
+def eval_cf(cfs, x1, x2, cfind=None, diag_only=False, threads=1):
+    """eval_cf.list (R/cf.R:402-411): sum over the selected covariance functions.
+    threads > 1 evaluates row blocks of x1 in parallel threads (every covariance
+    function is row-separable, so the values are the same)."""
     idx = range(len(cfs)) if cfind is None else cfind
+    x1 = as_matrix(x1)
+    if threads > 1 and not diag_only and x1.shape[0] >= 4 * 256:
+        from concurrent.futures import ThreadPoolExecutor
+        bounds = np.linspace(0, x1.shape[0], 4 * threads + 1).astype(int)
+        with ThreadPoolExecutor(threads) as ex:
+            parts = list(ex.map(lambda b: eval_cf(cfs, x1[b[0]:b[1]], x2, cfind),
+                                zip(bounds[:-1], bounds[1:])))
+        return np.vstack([np.broadcast_to(p, (b1 - b0, as_matrix(x2).shape[0]))
+                          for p, b0, b1 in zip(parts, bounds[:-1], bounds[1:])])
     K = 0.0
     for k in idx:
         K = K + eval_cf_one(cfs[k], x1, x2, diag_only)
@@ -785,8 +800,9 @@ def ep_fitc(lik, Kz, Kz_chol, Kxz, K_diag, D, y, damping=0.9, damping_min=0.1, m
 # R/gp_pred.R:88-296, R/gp_loo.R:73-133)
 # ----------------------------------------------------------------------------
 
-def gp_fit(gp, x, y, trials=None, offset=None, jitter=None):
-    """gp_fit (R/gp_fit.R:54-60) -> fit_laplace/fit_ep.method_full/fitc."""
+def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, threads=1):
+    """gp_fit (R/gp_fit.R:54-60) -> fit_laplace/fit_ep.method_full/fitc. threads > 1
+    evaluates the covariance matrix in parallel row blocks (same values)."""
     x = as_matrix(x)
     y = np.asarray(y, dtype=np.float64)
     jitter = 1e-6 if jitter is None else jitter
@@ -796,7 +812,8 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None):
     if ap.kind == "ep" and gp.lik.kind == "gaussian":
         raise ValueError("approx_ep disabled for lik_gaussian")
     if me.kind == "full":
-        K = eval_cf(gp.cfs, x, x) + jitter * np.eye(n)
+        K = eval_cf(gp.cfs, x, x, threads=threads)
+        K[np.diag_indices(n)] += jitter  # + jitter * diag(n) (R/gp_fit.R:95)
         if ap.kind == "laplace":
             fit = laplace_full(gp.lik, K, y, ap.maxiter, ap.tol, trials, offset)
         else:
@@ -832,6 +849,210 @@ def gp_energy(gp, include_prior=True):
     if include_prior:
         e = e - lpdf_prior(gp)
     return e
+
+
+# ----------------------------------------------------------------------------
+# energy gradient. The reference has none: gp_optim minimises gp_energy with
+# Nelder-Mead (R/gp_optim.R:76-94). This is restated from the mathematics to
+# check the device gradient: d log_evidence / d log(theta) of a Gaussian
+# full-method fit is (1/2) tr((alpha alpha^T - C^-1) dC/dlog(theta)) with
+# C = K + jitter I + sigma^2 I. The analytic derivatives of each covariance
+# function are pinned by complex-step differentiation of eval_cf itself
+# (Squire & Trapp 1998: df/dt = Im f(t + ih) / h, exact to rounding).
+# ----------------------------------------------------------------------------
+
+_STATIONARY = ("sexp", "matern32", "matern52")
+
+
+def _nn_parts(cf, x1, x2):
+    """cf_nn_c's intermediate quantities (src/cf.cpp:148-160): A, B, C, q, u, K."""
+    s0 = cf.sigma0 * cf.sigma0 * cf.sigma * cf.sigma
+    a1, a2 = x1 * cf.sigma, x2 * cf.sigma
+    A = s0 + a1 @ a2.T
+    B = (s0 + (a1 * a1).sum(1))[:, None]
+    Cc = (s0 + (a2 * a2).sum(1))[None, :]
+    q = np.sqrt((1 + 2 * B) * (1 + 2 * Cc))
+    u = 2 * A / q
+    K = cf.magn ** 2 * (2.0 / math.pi) * np.arcsin(u)
+    return A, B, Cc, q, u, K
+
+
+def _stationary_parts(cf, x1, x2):
+    """K, dK/dlog(lscale) and dK/d(r^2) of sexp / matern32 / matern52 (src/cf.cpp:35-117)."""
+    r2 = _sqdist(x1, x2)
+    m2, ls = cf.magn ** 2, cf.lscale
+    if cf.kind == "sexp":
+        K = m2 * np.exp(-0.5 * r2 / (ls * ls))
+        return K, K * r2 / (ls * ls), -0.5 * K / (ls * ls)
+    c = math.sqrt(3.0 if cf.kind == "matern32" else 5.0) / ls
+    a = c * np.sqrt(r2)
+    e = np.exp(-a)
+    if cf.kind == "matern32":
+        return m2 * (1 + a) * e, m2 * a * a * e, -0.5 * m2 * c * c * e
+    return (m2 * (1 + a + a * a / 3) * e, m2 * a * a * (1 + a) / 3 * e,
+            -m2 * c * c * (1 + a) * e / 6)
+
+
+def kernel_and_grads(cf, x1, x2):
+    """K(x1, x2) of one covariance function and dK/dlog(theta) for each of its free
+    parameters, in get_param order (R/cf.R:313-344)."""
+    if cf.kind == "prod":
+        parts = [kernel_and_grads(c, x1, x2) for c in cf.cfs]
+        K = 1.0
+        for Kc, _ in parts:
+            K = K * Kc
+        grads = []
+        for i, (_, gc) in enumerate(parts):
+            others = 1.0
+            for j, (Ko, _) in enumerate(parts):
+                if j != i:
+                    others = others * Ko
+            grads += [g * others for g in gc]
+        return K, grads
+    x1 = prepare_inputmat(cf, x1)
+    x2 = prepare_inputmat(cf, x2)
+    n1, n2 = x1.shape[0], x2.shape[0]
+    if cf.kind == "periodic":
+        w = 2 * math.pi / cf.period
+        t1 = np.hstack([np.sin(w * x1), np.cos(w * x1)])
+        t2 = np.hstack([np.sin(w * x2), np.cos(w * x2)])
+        K, gb = kernel_and_grads(cf.base, t1, t2)
+        if _is_fixed(cf, "period"):
+            return K, gb
+        # S = sum_k d_k sin(w d_k), d = x1_k - x2_k; dw/dlog(period) = -w
+        S = np.zeros((n1, n2))
+        for k in range(x1.shape[1]):
+            d = x1[:, k][:, None] - x2[:, k][None, :]
+            S += d * np.sin(w * d)
+        b = cf.base
+        if b.kind == "const":
+            dp = np.zeros((n1, n2))
+        elif b.kind == "lin":  # K = m^2 sum_k cos(w d_k)
+            dp = b.magn ** 2 * w * S
+        elif b.kind in _STATIONARY:  # r^2 = sum_k 2 - 2 cos(w d_k)
+            _, _, dk_dr2 = _stationary_parts(b, t1, t2)
+            dp = dk_dr2 * (-2.0 * w * S)
+        elif b.kind == "nn":  # A = s0 + sigma^2 sum_k cos(w d_k); B, C do not depend on w
+            _, _, _, q, u, _ = _nn_parts(b, t1, t2)
+            dp = b.magn ** 2 * (2.0 / math.pi) / np.sqrt(1 - u * u) * (2.0 * b.sigma ** 2 * w * S / q)
+        else:
+            raise ValueError(b.kind)
+        return K, [dp] + gb
+    grads = {}
+    if cf.kind == "const":
+        K = np.full((n1, n2), cf.magn ** 2)
+    elif cf.kind == "lin":
+        K = cf.magn ** 2 * (x1 @ x2.T)
+    elif cf.kind in _STATIONARY:
+        K, grads["lscale"], _ = _stationary_parts(cf, x1, x2)
+    elif cf.kind == "nn":
+        A, B, Cc, q, u, K = _nn_parts(cf, x1, x2)
+        dk_du = cf.magn ** 2 * (2.0 / math.pi) / np.sqrt(1 - u * u)
+        s0 = cf.sigma0 ** 2 * cf.sigma ** 2
+        # dlog(sigma0): dA = dB = dC = 2 s0; dlog(sigma): dA = 2A, dB = 2B, dC = 2C
+        grads["sigma0"] = dk_du * (4 * s0 / q - u * (2 * s0 / (1 + 2 * B) + 2 * s0 / (1 + 2 * Cc)))
+        grads["sigma"] = dk_du * (4 * A / q - u * (2 * B / (1 + 2 * B) + 2 * Cc / (1 + 2 * Cc)))
+    else:
+        raise ValueError(cf.kind)
+    grads["magn"] = 2.0 * K
+    return K, [grads[nm] for nm in PARAM_NAMES[cf.kind] if not _is_fixed(cf, nm)]
+
+
+def kernel_grads_complex_step(cfs, x1, x2, h=1e-20):
+    """dK/dlog(theta) of eval_cf.list for every free covariance parameter (get_param
+    order) by complex-step differentiation of eval_cf: the independent pin of
+    kernel_and_grads."""
+    import cmath
+    import copy
+    vals = []
+    for cf in cfs:
+        vals += get_param_cf(cf)[1]
+    out = []
+    for j in range(len(vals)):
+        cc = copy.deepcopy(cfs)
+        v = np.array(vals, dtype=np.complex128)
+        v[j] += 1j * h
+        k = 0
+        for cf in cc:
+            k += _set_param_cf(cf, v[k:], exp=cmath.exp)
+        out.append(np.imag(eval_cf(cc, x1, x2)) / h)
+    return out
+
+
+def dlpdf_prior(gp):
+    """Derivative of lpdf_prior (R/priors.R:96-112) with respect to the log-parameters."""
+    def one(prior, param):
+        if prior is None or prior.kind in ("fixed", "logunif"):
+            return 0.0
+        if prior.kind == "lognormal":
+            return -(param - prior.loc) / prior.scale ** 2
+        if prior.kind == "half_t":
+            t = math.exp(param) / prior.scale
+            return 1.0 - (prior.df + 1) * t * t / (prior.df + t * t)
+        raise ValueError(prior.kind)
+
+    def cf_terms(cf):
+        if cf.kind == "prod":
+            return sum((cf_terms(c) for c in cf.cfs), [])
+        if cf.kind == "periodic":
+            t = [] if _is_fixed(cf, "period") else [one(cf.priors.get("period"), math.log(cf.period))]
+            return t + cf_terms(cf.base)
+        return [one(cf.priors.get(nm), math.log(getattr(cf, nm)))
+                for nm in PARAM_NAMES[cf.kind] if not _is_fixed(cf, nm)]
+    g = sum((cf_terms(cf) for cf in gp.cfs), [])
+    g += [one(gp.lik.priors.get(nm), math.log(getattr(gp.lik, nm)))
+          for nm in PARAM_NAMES[gp.lik.kind] if not _is_fixed(gp.lik, nm)]
+    return np.array(g, dtype=np.float64)
+
+
+def log_evidence_grad(gp, threads=1, block=1024):
+    """d log_evidence / d log(theta) of a fitted lik_gaussian + method_full GP, for the
+    free parameters in get_param order: (1/2) sum_ij W_ij dK_ij per covariance
+    parameter, W = alpha alpha^T - C^-1, and sigma^2 (alpha^T alpha - tr C^-1) for
+    the noise. Row blocks of W and dK are formed one at a time (threads of them in
+    parallel); their sums are added in block order."""
+    from scipy.linalg import lapack
+    if gp.lik.kind != "gaussian" or gp.method.kind != "full":
+        raise ValueError("the gradient is defined for lik_gaussian with method_full")
+    x = gp.x
+    n = x.shape[0]
+    alpha = gp.fit["alpha"]
+    Ci, info = lapack.dpotri(gp.fit["C_chol"], lower=1)
+    if info != 0:
+        raise np.linalg.LinAlgError("potri failed")
+    il = np.tril_indices(n, -1)
+    Ci[il[1], il[0]] = Ci[il]  # symmetric fill from the lower triangle
+    bounds = list(range(0, n, block)) + [n]
+
+    def part(b):
+        i0, i1 = b
+        grads = []
+        for cf in gp.cfs:
+            grads += kernel_and_grads(cf, x[i0:i1], x)[1]
+        Wb = alpha[i0:i1, None] * alpha[None, :] - Ci[i0:i1]
+        return np.array([(Wb * g).sum() for g in grads])
+    blocks = list(zip(bounds[:-1], bounds[1:]))
+    if threads > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(threads) as ex:
+            parts = list(ex.map(part, blocks))
+    else:
+        parts = [part(b) for b in blocks]
+    g = 0.5 * np.sum(parts, axis=0) if parts and len(parts[0]) else np.zeros(0)
+    g = list(g)
+    for nm in PARAM_NAMES[gp.lik.kind]:
+        if not _is_fixed(gp.lik, nm):
+            s2 = gp.lik.sigma ** 2
+            g.append(s2 * (alpha @ alpha - np.trace(Ci)))
+    return np.array(g, dtype=np.float64)
+
+
+def gp_energy_grad(gp, include_prior=True, threads=1):
+    """Gradient of gp_energy (R/gp.R:138-147) with respect to the log-parameters."""
+    g = -log_evidence_grad(gp, threads=threads)
+    if include_prior:
+        g = g - dlpdf_prior(gp)
+    return g
 
 
 def gp_pred_post_full(gp, xt, var=False, cfind=None):

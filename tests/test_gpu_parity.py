@@ -211,33 +211,29 @@ def test_not_positive_definite_is_an_error():
     assert np.isfinite(gp.fit["log_evidence"])
 
 
-def test_energy_gradient_matches_finite_differences():
-    """The gradient has no counterpart in the reference (it optimises with Nelder-Mead):
-    parity unpinned by the reference, checked against central differences of the
-    oracle's energy."""
+def test_energy_gradient_matches_oracle():
+    """The gradient has no counterpart in the reference (it optimises with Nelder-Mead,
+    R/gp_optim.R:76-94). The oracle's gradient (analytic covariance derivatives pinned by
+    complex-step differentiation of eval_cf, the trace formula by finite differences of the
+    oracle energy, both in tests/test_oracle.py) holds the device gradient to 1e-10
+    relative per component (components below 1e-10 of the largest are held absolutely).
+    One-ulp input changes move the oracle's own gradient by <= 1.2e-13 here."""
     rng = np.random.default_rng(5)
     n = 150
     x = rng.uniform(-1, 1, (n, 3))
     y = np.sin(2 * x[:, 0]) + x[:, 1] ** 2 + 0.05 * rng.standard_normal(n)
     for cfs in ([G.cf_matern52(lscale=0.7), G.cf_const(1.0)], [G.cf_sexp(lscale=0.5, magn=1.2)],
-                [G.cf_matern32(vars=[0, 2]) * G.cf_lin(vars=[1])], [G.cf_nn(), G.cf_periodic(period=1.7)]):
+                [G.cf_matern32(vars=[0, 2]) * G.cf_lin(vars=[1])], [G.cf_nn(), G.cf_periodic(period=1.7)],
+                [G.cf_periodic(period=0.9, cf_base=G.cf_matern52(lscale=0.8)), G.cf_lin(normalize=True)]):
         with warnings.catch_warnings():
             warnings.simplefilter("ignore")
             gp = G.gp_init(cfs, G.lik_gaussian(sigma=0.1, prior_sigma=G.prior_lognormal()))
-        gp = G.gp_fit(gp, x, y)
-        g = G.gp_energy_grad(gp)
-        _, p0 = G.get_param(gp)
         og = oracle_gp(gp)
-        fd = np.zeros_like(p0)
-        h = 1e-5
-        for i in range(len(p0)):
-            for sgn in (1, -1):
-                q = p0.copy()
-                q[i] += sgn * h
-                R.set_param(og, q)
-                R.gp_fit(og, x, y)
-                fd[i] += sgn * R.gp_energy(og) / (2 * h)
-        assert close(g, fd, 1e-5, 1e-6), (cfs, g, fd)
+        gp = G.gp_fit(gp, x, y)
+        og = R.gp_fit(og, x, y)
+        g = G.gp_energy_grad(gp)
+        go = R.gp_energy_grad(og)
+        assert close(g, go, RTOL, RTOL * np.max(np.abs(go))), (cfs, g, go)
 
 
 FITC_LIKS = [("gaussian", "laplace"), ("poisson", "laplace"), ("bernoulli", "laplace"),

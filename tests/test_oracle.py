@@ -153,3 +153,54 @@ def test_ep_and_laplace_agree_roughly():
 def test_gp_init_rejects_ep_gaussian():
     with pytest.raises(ValueError):
         R.gp_init([R.cf("sexp")], R.lik("gaussian"), approx=R.approx_ep())
+
+
+def test_kernel_derivatives_match_complex_step():
+    """The oracle's analytic dK/dlog(theta) (the reference has no gradient) against
+    complex-step differentiation of eval_cf itself, for every covariance function,
+    pair and triple product of test_basic.R, with vars subsets and normalisation."""
+    rng = np.random.default_rng(3)
+    x1 = rng.standard_normal((15, 2))
+    x2 = rng.standard_normal((11, 2))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        cases = models() + [[R.cf("matern32", vars=[1], normalize=True), R.cf("lin", vars=[0])],
+                            [R.cf_periodic(period=0.7, base=R.cf("nn")), R.cf_periodic(base=R.cf("lin"))],
+                            [R.cf_periodic(period=1.3, base=R.cf("matern52"))]]
+    for cfs in cases:
+        R.learn_scales(cfs, x1)
+        an = []
+        for c in cfs:
+            an += R.kernel_and_grads(c, x1, x2)[1]
+        K = sum(R.kernel_and_grads(c, x1, x2)[0] for c in cfs)
+        assert np.allclose(K, R.eval_cf(cfs, x1, x2), rtol=1e-14, atol=1e-15)
+        cs = R.kernel_grads_complex_step(cfs, x1, x2)
+        assert len(an) == len(cs)
+        for a, c in zip(an, cs):
+            assert np.max(np.abs(a - c)) <= 1e-12 * max(np.max(np.abs(c)), 1e-300), cfs
+
+
+def test_energy_gradient_matches_finite_differences_of_energy():
+    """gp_energy_grad of the oracle (0.5 tr(W dC) + noise + prior terms) against central
+    differences of the oracle's own gp_energy (R/gp.R:138-147), including priors."""
+    rng = np.random.default_rng(5)
+    n = 60
+    x = rng.uniform(-1, 1, (n, 3))
+    y = np.sin(2 * x[:, 0]) + x[:, 1] ** 2 + 0.05 * rng.standard_normal(n)
+    for cfs in ([R.cf("matern52", lscale=0.7), R.cf("const", magn=1.0)],
+                [R.cf_prod(R.cf("matern32", vars=[0, 2]), R.cf("lin", vars=[1]))],
+                [R.cf("nn"), R.cf_periodic(period=1.7)]):
+        lk = R.lik("gaussian", sigma=0.1, priors=dict(sigma=R.prior("lognormal", loc=0.0, scale=1.0)))
+        gp = R.gp_fit(R.gp_init(copy.deepcopy(cfs), lk), x, y)
+        g = R.gp_energy_grad(gp)
+        _, p0 = R.get_param(gp)
+        fd = np.zeros_like(p0)
+        h = 1e-5
+        for i in range(len(p0)):
+            for sgn in (1, -1):
+                q = p0.copy()
+                q[i] += sgn * h
+                og = R.set_param(copy.deepcopy(gp), q)
+                R.gp_fit(og, x, y)
+                fd[i] += sgn * R.gp_energy(og) / (2 * h)
+        assert np.allclose(g, fd, rtol=2e-6, atol=2e-7), (cfs, g, fd)
