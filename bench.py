@@ -40,6 +40,13 @@ SIGMA = 0.05
 LSCALE, MAGN, CMAGN = 0.7, 1.0, 1.0
 NPRED = 8192
 
+# DRAM traffic of the sliced GEMM per launch of the n = 16384 mixed step, from one
+# ncu capture of all oz_gemm launches of one step (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass; the profile summary under profiles/ gives the
+# command). Filled in from that capture; None until it exists.
+OZ_TRAFFIC_PER_LAUNCH = {}
+OZ_TRAFFIC_SOURCE = None
+
 
 def theta_sequence(k):
     """Log-hyperparameters of step k: [log lscale, log magn, log const magn, log sigma]."""
@@ -83,28 +90,16 @@ def make_data(n, seed=2):
 # CPU leg: the oracle (restatement of gplite's R path) + the same gradient
 # ----------------------------------------------------------------------------
 
-def cpu_energy_grad(x, y, theta):
-    """One energy + gradient on the CPU: the oracle's gp_fit (B factorisation,
-    R/laplace.R:13-39) plus the gradient 1/2 tr((aa^T - C^-1) dC) in numpy."""
+def cpu_energy_grad(x, y, theta, threads=1):
+    """One energy + gradient on the CPU with the oracle: its gp_fit (B factorisation,
+    R/laplace.R:13-39; covariance rows in `threads` threads, LAPACK on OpenBLAS's
+    threads) and its gradient 1/2 tr((alpha alpha^T - C^-1) dC/dlog theta) (the
+    reference has none: gp_optim uses Nelder-Mead, R/gp_optim.R:76-94)."""
     from oracle import gplite_ref as R
-    from scipy import linalg as sla
     ls, mg, cm, sg = np.exp(theta)
     gp = R.gp_init([R.cf("matern52", lscale=ls, magn=mg), R.cf("const", magn=cm)], R.lik("gaussian", sigma=sg))
-    gp = R.gp_fit(gp, x, y)
-    n = len(y)
-    Lc = gp.fit["C_chol"]
-    alpha = gp.fit["alpha"]
-    Ci = sla.cho_solve((Lc, True), np.eye(n))
-    W = np.outer(alpha, alpha) - Ci
-    del Ci
-    from scipy.spatial.distance import cdist
-    a = math.sqrt(5.0) * cdist(x, x) / ls
-    e = np.exp(-a)
-    dls = mg * mg * a * a * (1 + a) / 3 * e
-    dm = 2 * mg * mg * (1 + a + a * a / 3) * e
-    g = np.array([0.5 * (W * dls).sum(), 0.5 * (W * dm).sum(), 0.5 * W.sum() * 2 * cm * cm,
-                  sg * sg * (alpha @ alpha - np.trace(sla.cho_solve((Lc, True), np.eye(n))))])
-    return gp.fit["log_evidence"], g
+    gp = R.gp_fit(gp, x, y, threads=threads)
+    return gp.fit["log_evidence"], R.log_evidence_grad(gp, threads=threads)
 
 
 def cpu_threads():
@@ -114,34 +109,85 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def cpu_steps(x, y, warmup, steps, threads, budget_s):
+    """Whole energy + gradient steps of the oracle on (x, y): `warmup` untimed, then up
+    to `steps` timed, stopping early (never below 3 timed when steps >= 3) once the next
+    step would pass budget_s of timed work. Returns (seconds per step, timed, warm-up)."""
+    for k in range(warmup):
+        cpu_energy_grad(x, y, theta_sequence(k), threads)
+    ts = []
+    for k in range(steps):
+        t0 = time.perf_counter()
+        cpu_energy_grad(x, y, theta_sequence(warmup + k), threads)
+        ts.append(time.perf_counter() - t0)
+        if len(ts) >= min(3, steps) and sum(ts) + ts[-1] > budget_s:
+            break
+    return sum(ts) / len(ts), len(ts), warmup
+
+
+def cpu_one_thread_subprocess(x, y):
+    """Start one whole oracle step on (x, y) at one thread (OpenBLAS pinned to 1) in a
+    child process; the inputs travel through a temporary .npz file."""
+    import tempfile
+    fd, path = tempfile.mkstemp(suffix=".npz")
+    os.close(fd)
+    np.savez(path, x=x, y=y)
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1",
+               CUDA_VISIBLE_DEVICES="")
+    p = subprocess.Popen([sys.executable, os.path.abspath(__file__), "--cpu-step", path],
+                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, env=env)
+    p.data_path = path
+    return p
+
+
+def collect_one_thread(p, timeout):
+    try:
+        out, _ = p.communicate(timeout=timeout)
+        return json.loads(out.strip().splitlines()[-1])
+    except Exception:
+        p.kill()
+        p.communicate()
+        return None
+    finally:
+        try:
+            os.unlink(p.data_path)
+        except OSError:
+            pass
+
+
+def run_cpu_step(args):
+    """--cpu-step PATH: one whole step at one thread on the inputs in PATH."""
+    d = np.load(args.cpu_step)
+    t, k, w = cpu_steps(d["x"], d["y"], 0, 1, 1, 1e9)
+    print(json.dumps({"s_per_step": t, "n": int(len(d["y"])), "threads": 1}), flush=True)
+    return 0
+
+
 def run_reference(args):
-    """--impl reference: the reference's path on the host cores (R is unavailable,
-    so the oracle restatement, all threads)."""
+    """--impl reference: the reference's path on the host cores. The reference is R
+    calling LAPACK and R is not available, so the oracle (a line-by-line NumPy
+    restatement) runs it, on the headline configuration itself (n = 16384, whole
+    steps, all host threads): 1 untimed step, then up to K timed steps within a
+    time budget (at least 3)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    # a bounded sample per step (n = 4096, scaled by (16384/4096)^3) so that the
-    # whole --steps/--warmup run ends within a few minutes
-    n = min(args.cpu_n, 4096)
+    n = args.n
+    thr = cpu_threads()
+    warm = min(args.warmup, 1)
     x, y = make_data(n, seed=2)
-    for k in range(args.warmup):
-        cpu_energy_grad(x, y, theta_sequence(k))
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        cpu_energy_grad(x, y, theta_sequence(args.warmup + k))
-    t = (time.perf_counter() - t0) / args.steps
-    scale = (N_FULL / n) ** 3
-    val = 1.0 / (t * scale)
+    t, k, w = cpu_steps(x, y, warm, args.steps, thr, args.cpu_budget)
+    val = 1.0 / t
     line = {
         "impl": "reference", "metric": "GP solves/s (energy+gradient, n=16384 full GP)", "value": val,
-        "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t * scale * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (numpy seeded; GP draw matern52+const)",
-        "config": {"workload": "full GP regression energy+gradient, n=16384 d=8 matern52+const", "n": N_FULL,
-                   "d": D, "sample_n": n},
-        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
-                         "sample": "oracle fit + numpy gradient at n=%d per step (R unavailable), time "
-                                   "scaled by (16384/%d)^3" % (n, n)},
+        "unit": "solves/s", "n_gpus": args.gpus, "steps": k, "warmup": w, "steps_requested": args.steps,
+        "warmup_requested": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (numpy seeded; GP draw matern52+const)",
+        "config": {"workload": "full GP regression energy+gradient, n=%d d=8 matern52+const, lik_gaussian "
+                               "sigma 0.05, fixed theta sequence" % n, "n": n, "d": D, "precision": "fp64"},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": thr, "kind": "port",
+                         "sample": "%d whole steps at n=%d after %d untimed (oracle gp_fit + gradient, %d "
+                                   "threads; R unavailable, the oracle restates its path)" % (k, n, w, thr)},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -253,6 +299,9 @@ def run_gpu(args):
     ctx = L.Context(local)
     n = args.n
     x, y = make_data(n, seed=2 + rank * 0)
+    # the one-thread CPU step (minutes) runs in a child process on one host core
+    # while the GPU is measured; the all-core CPU step runs after the GPU work
+    cpu1 = cpu_one_thread_subprocess(x, y) if (not args.no_cpu and world == 1 and rank == 0) else None
     xf = np.asfortranarray(x)
     # x column-major on the device: the memory of a row-major (d, n) array
     xd = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
@@ -370,8 +419,51 @@ def run_gpu(args):
         return dict(t_step=t_step, step_ms=step_ms, lmls=lmls, launches=launches, phases=phases, kernels=kp,
                     clocks=clocks, wall=wall, e2e_s=e2e_s, potrf_ms=float(ms[1]), potrf_calls=max(int(calls[1]), 1))
 
+    # gp_pred at 8192 test points (the prediction half of the configuration), on a model
+    # fitted at the first hyperparameters: mean (fused K(xt, x) alpha) and variance
+    xt = np.random.default_rng(7).uniform(-1, 1, (NPRED, D))
+    xtd = torch.from_numpy(np.ascontiguousarray(xt.T)).cuda()
+    md = torch.empty(NPRED, dtype=torch.float64, device="cuda")
+    vd = torch.empty(NPRED, dtype=torch.float64, device="cuda")
+
+    def time_pred(p, reps=3):
+        nonlocal prec
+        prec = L.PRECISION[p]
+        kk, lk, me, ap, op = specs(theta_sequence(0))
+        h = C.c_void_p()
+        r = L.FitResult()
+        L.check(lib.gpgp_fit_dev(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
+                                 C.c_void_p(xd.data_ptr()), n, D, C.c_void_p(yd.data_ptr()), None, None,
+                                 C.byref(h), C.byref(r)), ctx.h)
+
+        def one():
+            L.check(lib.gpgp_pred_dev(h, C.c_void_p(xtd.data_ptr()), NPRED, 0, C.c_void_p(md.data_ptr()),
+                                      C.c_void_p(vd.data_ptr())), ctx.h)
+        one()  # the first call also forms L^-1 (mixed), kept on the model
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            one()
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / reps
+        lib.gpgp_profile_enable(ctx.h, 1)
+        one()
+        barrier()
+        pm = np.zeros(8)
+        pc = np.zeros(8, dtype=np.int64)
+        lib.gpgp_profile_read(ctx.h, L.ptr(pm), pc.ctypes.data_as(C.c_void_p))
+        lib.gpgp_profile_enable(ctx.h, 0)
+        lib.gpgp_model_free(h)
+        return {"ms_per_call": ms, "points": NPRED, "n": n, "mean_ms": float(pm[6]), "var_ms": float(pm[7]),
+                "fp64_equiv_tflops": float(n) ** 2 * NPRED / (ms / 1e3) / 1e12,
+                "note": "algorithmic flops n^2 m (the triangular solve of the variance); time per call with "
+                        "device inputs and outputs; L^-1 formed by the first call is kept on the model"}
+
     precs = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
     res = {p: measure(p) for p in precs}
+    preds = {p: time_pred(p) for p in precs}
     head = res[precs[0]]
     value = world / head["t_step"]
     h2d = xf.nbytes + yh.nbytes
@@ -381,41 +473,62 @@ def run_gpu(args):
     if rank == 0:
         peaks = measured_peaks()
 
+        # Algorithmic work of the dominant GEMM per step: the Cholesky (n^3 / 3),
+        # the triangular inverse (n^3 / 3) and B^-1 = L^-T L^-1 (n^3 / 3) are the
+        # contractions it carries, n^3 FP64-equivalent flops per energy+gradient step.
+        alg = float(n) ** 3
+
         def roofline(p):
             r = res[p]
+            potrf_tf = (n ** 3 / 3) / (r["potrf_ms"] / max(r["potrf_calls"], 1) / 1e3) / 1e12
             if p == "fp64":
                 fp64 = fp64_peak_gflops(torch) / 1e3
                 k = r["kernels"]["gemm64"]
-                ach = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+                ach = alg / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+                exe = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
                 return {"bound": "fp64", "kernel": "gemm64_kernel (FP64 trailing updates of potrf, "
                                                    "trtri/lauum products)",
                         "achieved": ach, "peak": fp64, "unit": "TFLOP/s", "frac": ach / fp64 if ach else None,
-                        "launches": k["launches"], "avg_launch_ms": k["ms"] / max(k["launches"], 1),
+                        "algorithmic_flops_per_step": alg, "launches": k["launches"],
+                        "avg_launch_ms": k["ms"] / max(k["launches"], 1),
                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 is not in "
                                        "MEASURED_PEAKS.json)",
-                        "potrf_fp64_tflops": (n ** 3 / 3) / (r["potrf_ms"] / max(r["potrf_calls"], 1) / 1e3) / 1e12,
-                        "traffic": None}
+                        "executed_tile_flops": {"achieved": exe, "frac": exe / fp64 if exe else None},
+                        "potrf_fp64_tflops": potrf_tf, "traffic": None}
             k = r["kernels"]["oz_gemm"]
             bf = peaks.get("bf16_tflops_sustained", 1700.0)
-            ach = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
-            return {"bound": "tensor", "kernel": "oz_gemm_kernel<4> (BF16-sliced tcgen05 trailing updates)",
+            ach = alg / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+            exe = k["flops"] / (k["ms"] / 1e3) / 1e12 if k["ms"] > 0 else None
+            nl = max(k["launches"], 1)
+            return {"bound": "tensor", "kernel": "oz_gemm_kernel<4> (BF16-sliced tcgen05 trailing updates, "
+                                                 "triangular inverse, B^-1)",
                     "achieved": ach, "peak": bf, "unit": "TFLOP/s", "frac": ach / bf if ach else None,
-                    "launches": k["launches"], "avg_launch_ms": k["ms"] / max(k["launches"], 1),
+                    "algorithmic": "FP64-equivalent flops: n^3 per step (potrf n^3/3 + trtri n^3/3 + "
+                                   "lauum n^3/3), %.3g per launch on average" % (alg / nl),
+                    "launches": k["launches"], "avg_launch_ms": k["ms"] / nl,
                     "peak_source": "of measured: MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed "
                                    "inside a long step)",
-                    "potrf_fp64_equiv_tflops": (n ** 3 / 3) / (r["potrf_ms"] / max(r["potrf_calls"], 1) / 1e3) / 1e12,
-                    "traffic": None}
+                    "executed_slice_products": {
+                        "achieved": exe, "frac": exe / bf if exe else None,
+                        "note": "BF16 MMA flops of all slice products the launches executed (13 per "
+                                "FP64-equivalent product with 4 slices), incl. zero-padded tiles: a "
+                                "tensor-pipe utilisation, not algorithmic work"},
+                    "potrf_fp64_equiv_tflops": potrf_tf,
+                    "traffic": OZ_TRAFFIC_PER_LAUNCH.get(n), "traffic_unit": "bytes per launch",
+                    "traffic_source": OZ_TRAFFIC_SOURCE if n in OZ_TRAFFIC_PER_LAUNCH else None}
 
         cpu = None
-        if not args.no_cpu and world == 1:
-            xs, ys = make_data(args.cpu_n, seed=2)
-            t0 = time.perf_counter()
-            cpu_energy_grad(xs, ys, theta_sequence(0))
-            tc = time.perf_counter() - t0
-            sc = (N_FULL / args.cpu_n) ** 3
-            cpu = {"value": 1.0 / (tc * sc), "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
-                   "sample": "one oracle fit + numpy gradient at n=%d (R unavailable), time scaled by "
-                             "(16384/%d)^3" % (args.cpu_n, args.cpu_n)}
+        if cpu1 is not None:
+            thr = cpu_threads()
+            one = collect_one_thread(cpu1, timeout=1800)  # finish it before the all-core step
+            tc, kc, _ = cpu_steps(x, y, 0, 1, thr, 1e9)
+            cpu = {"value": 1.0 / tc, "unit": "solves/s", "cores": thr, "kind": "port",
+                   "sample": "one whole step at n=%d (oracle gp_fit + gradient, %d threads; R unavailable, "
+                             "the oracle restates its path)" % (n, thr),
+                   "one_thread": ({"value": 1.0 / one["s_per_step"], "unit": "solves/s", "cores": 1,
+                                   "sample": "one whole step at n=%d, OpenBLAS at 1 thread (run in a child "
+                                             "process while the GPU was measured)" % n}
+                                  if one else None)}
         sm = sorted(head["step_ms"])
         out = {
             "metric": "GP solves/s (energy+gradient, n=16384 full GP)", "value": value, "unit": "solves/s",
@@ -454,6 +567,22 @@ def run_gpu(args):
                                  "phases_ms": f["phases"], "clocks": f["clocks"]}
             out["mixed_over_fp64"] = f["t_step"] / head["t_step"]
             out["lml_rel_err_mixed_vs_fp64"] = max(rel)
+        out["c2_pred"] = preds
+        if not args.headline_only and world == 1:
+            # the other configurations, each on its own workload (smaller stream window
+            # and plain-path samples than their standalone modes, to keep the run short)
+            import copy as _copy
+            sa = _copy.copy(args)
+            sa.steps, sa.warmup, sa.window, sa.plain_budget, sa.c1_reps = 3, 3, 0.5, 20.0, 100
+            del x, y, xd, yd
+            torch.cuda.empty_cache()
+            for key, fn in (("c1", run_c1), ("c3", run_c3), ("c4", run_batched), ("c5", run_served)):
+                t0 = time.perf_counter()
+                try:
+                    out[key] = fn(sa)
+                except Exception as e:  # a sub-benchmark failure must not hide the headline line
+                    out[key] = {"error": repr(e)}
+                out[key]["wall_s"] = time.perf_counter() - t0
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.barrier()
@@ -552,7 +681,7 @@ def run_batched(args):
                          lml=np.array([r["log_evidence"] for r in res]), info=plan.info(),
                          launches=L.launch_count() - l0)
         plan.close()
-    plain = run_plain_fp64(probs, budget_s=60.0)
+    plain = run_plain_fp64(probs, budget_s=args.plain_budget)
     ns = np.array([len(p["y"]) for p in probs], dtype=np.float64)
     diff = np.abs(out["mixed"]["lml"] - out["fp64"]["lml"])
     rel_plain = diff / np.abs(out["fp64"]["lml"])
@@ -585,8 +714,7 @@ def run_batched(args):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "autotune": out["mixed"]["info"], "gpu_launches": int(out["mixed"]["launches"]),
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -646,8 +774,7 @@ def run_c1(args):
             "lml_rel_err_vs_oracle": abs(f["lml"] - ogf.fit["log_evidence"]) / abs(ogf.fit["log_evidence"]),
             "cpu_baseline": {"value": 1e6 / cfit, "unit": "solves/s", "cores": 1, "kind": "port",
                              "sample": "oracle gp_fit at n=200 (median of 50); pred %.0f us" % cpred}}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def make_c3(n=8192, seed=3):
@@ -708,8 +835,7 @@ def run_c3(args):
             "mixed_over_fp64": {k: f[k]["fit_s"] / m[k]["fit_s"] for k in m},
             "lml_rel_err_mixed_vs_fp64": {k: abs(m[k]["lml"] - f[k]["lml"]) / abs(f[k]["lml"]) for k in m},
             "gpu_launches": int(m["laplace"]["launches"])}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -890,8 +1016,7 @@ def run_served(args):
         "batched_requests": m["stats"]["batched_requests"], "bytes_peak": m["stats"]["bytes_peak"],
         "clocks": clk, "gpu_launches": int(m["launches"]),
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main():
@@ -902,7 +1027,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
     ap.add_argument("--n", type=int, default=N_FULL)
-    ap.add_argument("--cpu-n", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="full", choices=["full", "batched", "served", "c1", "c3"])
     ap.add_argument("--c1-reps", type=int, default=200)
@@ -911,17 +1035,20 @@ def main():
     ap.add_argument("--workers", type=int, default=12)
     ap.add_argument("--plain-budget", type=float, default=40.0)
     ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--cpu-budget", type=float, default=300.0,
+                    help="seconds of timed CPU work for the reference arm")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="C2 only (no C1, C3, C4, C5 keys in the line)")
+    ap.add_argument("--cpu-step", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.cpu_step:
+        return run_cpu_step(args)
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "batched":
-        return run_batched(args)
-    if args.workload == "served":
-        return run_served(args)
-    if args.workload == "c1":
-        return run_c1(args)
-    if args.workload == "c3":
-        return run_c3(args)
+    sub = {"batched": run_batched, "served": run_served, "c1": run_c1, "c3": run_c3}
+    if args.workload in sub:
+        print(json.dumps(sub[args.workload](args)), flush=True)
+        return 0
     return run_gpu(args)
 
 

@@ -6,6 +6,12 @@ computes C = C - A B^T for random M x K and N x K operands with the BF16-sliced
 tcgen05 GEMM and with the FP64 GEMM (gpgp_mixed_selftest), and prints the
 relative difference with the GEMM's launch count, time and BF16 MMA rate from
 the library's kernel timers. The first call is a warm-up.
+
+    python -m gplite_gb300.selftest fit N M [fp64|mixed] [repeats]
+
+runs a full GP regression fit, its energy gradient and a prediction with
+variance at M points (see fit_pred): the profiling entry point of the other
+kernels.
 """
 from __future__ import annotations
 
@@ -30,7 +36,41 @@ def run(M, N, K, slices=4, repeats=1):
                 tflops=fl.value / max(ms.value / 1e3, 1e-30) / 1e12)
 
 
+def fit_pred(n, m, precision="fp64", d=8, repeats=1):
+    """A full GP regression (matern52 + const, lik_gaussian 0.05) on n seeded points in
+    [-1, 1]^d: gp_fit, the energy gradient and gp_pred with variance at m points,
+    `repeats` times after one warm-up round. The profiling entry point of the
+    covariance, Cholesky, solve and prediction kernels."""
+    import time
+
+    import numpy as np
+
+    from . import gp as G
+    from .objects import cf_const, cf_matern52, lik_gaussian
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1, 1, (n, d))
+    y = np.sin(2 * x[:, 0]) + x[:, 1] + 0.05 * rng.standard_normal(n)
+    xt = rng.uniform(-1, 1, (m, d))
+    out = []
+    for r in range(repeats + 1):
+        t0 = time.perf_counter()
+        g = G.gp_fit(G.gp_init([cf_matern52(lscale=0.7), cf_const(1.0)], lik_gaussian(sigma=0.05)), x, y,
+                     precision=precision)
+        G.gp_energy_grad(g)
+        p = G.gp_pred(g, xt, var=True)
+        if r:
+            out.append(time.perf_counter() - t0)
+    return dict(lml=g.fit["log_evidence"], mean0=float(p["mean"][0]), s_per_round=sum(out) / len(out))
+
+
 def main(argv):
+    if argv and argv[0] == "fit":
+        n, m = int(argv[1]), int(argv[2])
+        prec = argv[3] if len(argv) > 3 else "fp64"
+        r = fit_pred(n, m, prec, repeats=int(argv[4]) if len(argv) > 4 else 1)
+        print("fit + gradient + pred n %d m %d %s: lml %.12g, %.3f s per round"
+              % (n, m, prec, r["lml"], r["s_per_round"]))
+        return 0
     if len(argv) < 3:
         print(__doc__)
         return 2

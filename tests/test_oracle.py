@@ -204,3 +204,43 @@ def test_energy_gradient_matches_finite_differences_of_energy():
                 R.gp_fit(og, x, y)
                 fd[i] += sgn * R.gp_energy(og) / (2 * h)
         assert np.allclose(g, fd, rtol=2e-6, atol=2e-7), (cfs, g, fd)
+
+
+def test_synthetic_inputs_are_reproducible():
+    """The full-size fixtures rebuild their uniform inputs from numpy's PCG64 raw stream;
+    pin the stream and the conversion (the GPU tests check the same on their machine)."""
+    import sys
+    sys.path.insert(0, GOLD)
+    import synth as S
+    S.check_streams()
+    u = S.uniform(20, (4,), -1.0, 1.0)
+    raw = np.random.PCG64(20).random_raw(4)
+    assert np.array_equal(u, -1.0 + 2.0 * ((raw >> np.uint64(11)).astype(np.float64) * 2.0 ** -53))
+    assert len(S.C4_SIZES) == 32 and min(S.C4_SIZES) == 64 and max(S.C4_SIZES) == 1024
+    assert sorted({(n + 63) // 64 for n in S.C4_SIZES}) == list(range(1, 17))  # every bucket
+
+
+def test_fitc_and_c4_fixtures_reproduce():
+    """The oracle reproduces the FITC (n = 65536) fixture exactly and one C4 problem
+    per size bucket (the n = 16384 and n = 8192 fixtures take minutes; the GPU tests
+    hold the library to them)."""
+    import sys
+    sys.path.insert(0, GOLD)
+    import synth as S
+    g = np.load(os.path.join(GOLD, "fitc_n65536.npz"))
+    x, z, xt = S.fitc_inputs()
+    gp = R.gp_init([R.cf("sexp", lscale=0.7, magn=1.0)], R.lik("gaussian", sigma=0.1), method=R.method_fitc(z))
+    gp = R.gp_fit(gp, x, g["y"].astype(np.float64))
+    assert gp.fit["log_evidence"] == float(g["lml"])
+    assert np.array_equal(gp.fit["fmean"][::64], g["fmean_s64"])
+    c = np.load(os.path.join(GOLD, "c4_sample.npz"))
+    off = 0
+    for i, n in enumerate(S.C4_SIZES):
+        p = S.c4_problem(i, n)
+        y = c["y"][off:off + n].astype(np.float64)
+        off += n
+        if i % 4:
+            continue
+        gp = R.gp_fit(R.gp_init([R.cf(p["kind"], lscale=p["lscale"], magn=1.0)],
+                                R.lik("gaussian", sigma=p["sigma"])), p["x"], y)
+        assert gp.fit["log_evidence"] == c["lml"][i]
