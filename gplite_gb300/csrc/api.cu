@@ -115,6 +115,21 @@ __global__ void loo_laplace_kernel(int64_t n, double jitter, const double *__res
   }
 }
 
+// LOO posteriors from the posterior variance pv at the training inputs
+// (R/gp_loo.R:119-129); lvar holds pv on entry
+__global__ void loo_from_pv_kernel(int64_t n, const double *__restrict__ fhat, const double *__restrict__ z,
+                                   const double *__restrict__ V, double *__restrict__ lmean,
+                                   double *__restrict__ lvar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double Vi = V[i];
+    const double grad = (z[i] - fhat[i]) / Vi;
+    const double lv = 1.0 / (1.0 / lvar[i] - 1.0 / Vi);
+    lvar[i] = lv;
+    lmean[i] = fhat[i] - lv * grad;
+  }
+}
+
 // W_ij = alpha_i alpha_j - s_i s_j Binv_ij on the lower triangle (in place)
 __global__ void grad_w_kernel(int64_t n, const double *__restrict__ alpha,
                               const double *__restrict__ s, double *__restrict__ W) {
@@ -313,6 +328,8 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
     fnew.alloc(st, n);
     double diff = 0.0;
     int it = 0;
+    bool nlc_iter = false;  // the last iteration took the non-log-concave branch
+    double nlc_lml = 0.0;
     for (it = 1; it <= maxiter; ++it) {
       lik_pseudodata_la(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, m->z.p, m->V.p);
       GPGP_CUDA(cudaMemsetAsync(w.flags.p, 0, sizeof(int), st));
@@ -321,41 +338,62 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       int hflags = 0;
       GPGP_CUDA(cudaMemcpyAsync(&hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
       GPGP_CUDA(cudaStreamSynchronize(st));
-      if (hflags) {
-        res->status = GPGP_EUNSUPPORTED;
-        res->log_evidence = -INFINITY;
-        return fail(ctx, GPGP_EUNSUPPORTED,
-                    "non-log-concave branch (some pseudo-variance <= 0, R/laplace.R:40-117) is "
-                    "not implemented");
+      if (hflags & 2) {  // all(V > 0) is NA in R: an error
+        res->status = GPGP_ENAN;
+        res->log_evidence = NAN;
+        return fail(ctx, GPGP_ENAN, "NaN in the Laplace pseudo-data");
       }
       // mixed precision: the Newton iterates only steer the iteration, so their
       // solves go unrefined; the final alpha and f are refined once it stops
       const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
-      int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
-                                      (mixed && maxiter > 1) ? 0 : -1);
-      if (info != 0) {
-        res->status = GPGP_ENOT_PD;
-        res->info = info;
-        res->log_evidence = -INFINITY;
-        return fail(ctx, GPGP_ENOT_PD, "Cholesky factorisation: matrix is not positive definite");
+      if (hflags & 4) {
+        // some pseudo-variance <= 0: the good / bad split (R/laplace.R:40-117), FP64
+        bool improper = false;
+        gpgp_status s2 = nlc_fit_full(m, w.K.p, nullptr, false, m->alpha.p, fnew.p, nullptr, &nlc_lml, &improper);
+        if (s2 != GPGP_OK) {
+          res->status = s2;
+          res->log_evidence = -INFINITY;
+          return s2;
+        }
+        if (improper)  // R returns fmean = fhat_old and -Inf
+          GPGP_CUDA(cudaMemcpyAsync(fnew.p, m->fmean.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        m->improper = improper;
+        nlc_iter = true;
+      } else {
+        int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
+                                        (mixed && maxiter > 1) ? 0 : -1);
+        if (info != 0) {
+          res->status = GPGP_ENOT_PD;
+          res->info = info;
+          res->log_evidence = -INFINITY;
+          return fail(ctx, GPGP_ENOT_PD, "Cholesky factorisation: matrix is not positive definite");
+        }
+        m->nlc.reset();
+        m->improper = false;
+        nlc_iter = false;
       }
       max_abs_diff(st, n, m->fmean.p, fnew.p, red);
       diff = read_scalar(ctx, red + 64);
       const bool last = diff < m->approx.tol || it == maxiter;
-      if (last && mixed && maxiter > 1) refine_alpha(m, w, m->alpha.p, fnew.p, std::max(1, m->opts.refine_iters));
+      if (last && mixed && maxiter > 1 && !nlc_iter)
+        refine_alpha(m, w, m->alpha.p, fnew.p, std::max(1, m->opts.refine_iters));
       GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
       if (diff < m->approx.tol) break;
     }
     if (it > maxiter) it = maxiter;
     res->iters = it;
     if (maxiter > 1 && it == maxiter && !(diff < m->approx.tol)) res->converged = 0;
-    // LML = loglik(f) - 0.5 f^T alpha - 0.5 (C_logdet - V_logdet), C_logdet - V_logdet = 2 sum log L_ii
-    lik_loglik(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, red + 101, red);
-    dot_partial(st, n, m->fmean.p, m->alpha.p, red + 110);  // result at red + 174
-    double ll = read_scalar(ctx, red + 101);
-    double fa = read_scalar(ctx, red + 174);
-    double ld = read_scalar(ctx, logdetL);
-    m->log_evidence = ll - 0.5 * fa - 0.5 * (2.0 * ld);
+    if (nlc_iter) {
+      m->log_evidence = m->improper ? -INFINITY : nlc_lml;
+    } else {
+      // LML = loglik(f) - 0.5 f^T alpha - 0.5 (C_logdet - V_logdet), C_logdet - V_logdet = 2 sum log L_ii
+      lik_loglik(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, red + 101, red);
+      dot_partial(st, n, m->fmean.p, m->alpha.p, red + 110);  // result at red + 174
+      double ll = read_scalar(ctx, red + 101);
+      double fa = read_scalar(ctx, red + 174);
+      double ld = read_scalar(ctx, logdetL);
+      m->log_evidence = ll - 0.5 * fa - 0.5 * (2.0 * ld);
+    }
     res->log_evidence = m->log_evidence;
     res->status = GPGP_OK;
     return GPGP_OK;
@@ -413,11 +451,47 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       return GPGP_OK;
     }
     if (hflags & 4) {
-      res->status = GPGP_EUNSUPPORTED;
-      return fail(ctx, GPGP_EUNSUPPORTED,
-                  "non-log-concave EP branch (some site variance <= 0, R/ep.R:50-138) is not "
-                  "implemented");
+      // some site variance <= 0: the good / bad split (R/ep.R:50-138), FP64
+      bool improper = false;
+      double lml_it = 0.0;
+      gpgp_status s2 = nlc_fit_full(m, w.K.p, logC.p, true, m->alpha.p, fnew.p, m->fvar.p, &lml_it, &improper);
+      if (s2 != GPGP_OK) {
+        res->status = s2;
+        return s2;
+      }
+      if (improper) {
+        // R returns fmean = Inf: the sweep is rejected when an earlier one was
+        // accepted; on the first sweep R goes on without site variances and errors
+        if (!(diff_old < INFINITY)) {
+          res->status = GPGP_ENOT_PD;
+          return fail(ctx, GPGP_ENOT_PD, "EP: improper posterior of the bad sites in the first sweep");
+        }
+        m->improper = true;
+        lml = -INFINITY;
+        damp = damp * m->approx.damping;
+        continue;
+      }
+      m->improper = false;
+      GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      lml = lml_it;
+      max_abs_diff(st, n, fm_old.p, m->fmean.p, red);
+      diff_new = read_scalar(ctx, red + 64);
+      if (diff_new > diff_old) {
+        damp = damp * m->approx.damping;
+        continue;
+      }
+      damp = std::max(damp, m->approx.damping_min);
+      GPGP_CUDA(cudaMemcpyAsync(fm_old.p, m->fmean.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      GPGP_CUDA(cudaMemcpyAsync(fv_old.p, m->fvar.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      GPGP_CUDA(cudaMemcpyAsync(z_old.p, m->z.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      recip_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, P_old.p);
+      GPGP_CHECK_LAUNCH();
+      diff_old = diff_new;
+      if (diff_new < tol) break;
+      continue;
     }
+    m->nlc.reset();
+    m->improper = false;
     int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL);
     if (info != 0) {
       res->status = GPGP_ENOT_PD;
@@ -485,10 +559,10 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   if (lik->kind == GPGP_LIK_GAUSSIAN && approx->kind == GPGP_APPROX_EP)
     return fail(ctx, GPGP_EINVAL,
                 "approx_ep disabled for lik_gaussian: use approx_laplace (R/gp.R:54-56)");
-  if (lik->kind == GPGP_LIK_BETABINOM)
-    return fail(ctx, GPGP_EUNSUPPORTED, "lik_betabinom is not implemented on the device");
-  if (lik->kind == GPGP_LIK_BINOMIAL && !trials)
-    return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial likelihood");
+  if ((lik->kind == GPGP_LIK_BINOMIAL || lik->kind == GPGP_LIK_BETABINOM) && !trials)
+    return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial and beta binomial likelihoods");
+  if (lik->kind == GPGP_LIK_BETABINOM && !(lik->phi > 0))
+    return fail(ctx, GPGP_EINVAL, "lik_betabinom needs phi > 0");
   if (method->kind != GPGP_METHOD_FULL && method->kind != GPGP_METHOD_FITC)
     return fail(ctx, GPGP_EINVAL, "unknown method");
   if (opts->precision != GPGP_PREC_FP64 && opts->precision != GPGP_PREC_MIXED)
@@ -849,6 +923,8 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
                              double *mean, double *var, bool on_device) {
   if (!m || !xt || !mean || mt < 0) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (m->improper)
+    return fail(m->ctx, GPGP_ENOT_FITTED, "the fit has no posterior (log_evidence = -Inf, improper bad-site posterior)");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {
     GPGP_CUDA(cudaSetDevice(ctx->device));
@@ -887,7 +963,15 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       Phase ph(ctx, GPGP_PHASE_PRED_MEAN);
       cov_matvec(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, mout);
     }
-    if (var) {
+    if (var && m->nlc) {
+      // a fit whose last iteration was non-log-concave: (K + V)^-1 through the blocks
+      Phase ph(ctx, GPGP_PHASE_PRED_VAR);
+      DBuf dv;
+      dv.alloc(s, mt);
+      nlc_pred_var(m, Ft.p, mt, gm, dv.p);
+      GPGP_CUDA(cudaMemcpyAsync(var, dv.p, mt * sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    } else if (var) {
       Phase ph(ctx, GPGP_PHASE_PRED_VAR);
       // var = diag(Ktt) - colSums((C_chol^-1 Kt^T)^2), C_chol^-1 = L^-1 diag(s)  (R/gp_pred.R:216-228)
       const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(mt, (int64_t)(1ll << 28) / std::max<int64_t>(n, 1)));
@@ -939,6 +1023,8 @@ gpgp_status gpgp_pred_dev(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
 gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *loo_sum) {
   if (!m || !loos) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (m->improper)
+    return fail(m->ctx, GPGP_ENOT_FITTED, "the fit has no posterior (log_evidence = -Inf, improper bad-site posterior)");
   if (quad_order < 1 || quad_order > 64) return fail(m->ctx, GPGP_EINVAL, "quad_order must be in 1..64");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {
@@ -956,6 +1042,16 @@ gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *lo
       lvar.alloc(s, n);
       gpgp_status st2 = loo_fitc_posteriors(m, lmean.p, lvar.p);
       if (st2 != GPGP_OK) return st2;
+      mp = lmean.p;
+      vp = lvar.p;
+    } else if (m->nlc) {
+      // non-log-concave fit: post_var at the training inputs through the blocks of
+      // (K + V)^-1 (gp_pred_post with train = TRUE, R/gp_loo.R:124)
+      lmean.alloc(s, n);
+      lvar.alloc(s, n);
+      nlc_pred_var(m, m->F.p, n, 0xffffffffu, lvar.p);
+      loo_from_pv_kernel<<<g1(n), 256, 0, s>>>(n, m->fmean.p, m->z.p, m->V.p, lmean.p, lvar.p);
+      GPGP_CHECK_LAUNCH();
       mp = lmean.p;
       vp = lvar.p;
     } else {
@@ -989,6 +1085,8 @@ gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *lo
 gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_sigma) {
   if (!m || !grad_terms) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (m->improper)
+    return fail(m->ctx, GPGP_ENOT_FITTED, "the fit has no posterior (log_evidence = -Inf, improper bad-site posterior)");
   if (m->lik.kind != GPGP_LIK_GAUSSIAN || m->method.kind != GPGP_METHOD_FULL)
     return fail(m->ctx, GPGP_EUNSUPPORTED, "gradient needs lik_gaussian and method_full");
   gpgp_ctx *ctx = m->ctx;

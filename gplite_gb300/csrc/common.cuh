@@ -223,6 +223,12 @@ void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, cons
             int64_t lda, const double *x, double beta, double *y);
 // Sum of logdet partials (fixed order) -> out[0].
 void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out);
+// LU with partial pivoting of a general n x n A (lda), in place; piv[k] is the row
+// swapped with row k at step k; status[0] = k + 1 at an exactly zero pivot.
+void getrf(cudaStream_t s, double *A, int64_t n, int64_t lda, int *piv, int *status);
+// X <- A^-1 X (n x m, ldx) with the factors of getrf.
+void getrs(cudaStream_t s, const double *LU, int64_t n, int64_t lda, const int *piv, double *X, int64_t m,
+           int64_t ldx, const int *status);
 
 // ---------------------------------------------------------------------------
 // mixed precision (mixed.cu / mixed_la.cu): BF16-sliced operands for tcgen05

@@ -930,4 +930,124 @@ void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out) {
   GPGP_CHECK_LAUNCH();
 }
 
+// ---------------------------------------------------------------------------
+// LU with partial pivoting of a small general matrix (the symmetric indefinite
+// Schur complement of the bad sites in the non-log-concave fits, where the
+// reference takes Matrix::lu of K + diag(V), R/laplace.R:113, R/ep.R:128)
+// ---------------------------------------------------------------------------
+// Column k: one CTA picks the pivot (largest |A_ik|, i >= k, first index on
+// ties), swaps rows k and p across all columns and divides the column below the
+// pivot by it; a grid then applies the rank-1 update to the trailing block.
+__global__ void __launch_bounds__(256) lu_pivot_kernel(double *__restrict__ A, int64_t n, int64_t lda,
+                                                       int64_t k, int *__restrict__ piv,
+                                                       int *__restrict__ status) {
+  __shared__ double bv[256];
+  __shared__ int64_t bi[256];
+  if (*(volatile int *)status != 0) return;
+  double best = -1.0;
+  int64_t arg = k;
+  for (int64_t i = k + threadIdx.x; i < n; i += 256) {
+    const double v = fabs(A[i + k * lda]);
+    if (v > best) {
+      best = v;
+      arg = i;
+    }
+  }
+  bv[threadIdx.x] = best;
+  bi[threadIdx.x] = arg;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      const double o = bv[threadIdx.x + st];
+      const int64_t oi = bi[threadIdx.x + st];
+      if (o > bv[threadIdx.x] || (o == bv[threadIdx.x] && oi < bi[threadIdx.x])) {
+        bv[threadIdx.x] = o;
+        bi[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const int64_t p = bi[0];
+  if (!(bv[0] > 0.0)) {  // exactly singular (or NaN)
+    if (threadIdx.x == 0) atomicCAS(status, 0, (int)(k + 1));
+    return;
+  }
+  if (threadIdx.x == 0) piv[k] = (int)p;
+  if (p != k)
+    for (int64_t j = threadIdx.x; j < n; j += 256) {
+      const double t = A[k + j * lda];
+      A[k + j * lda] = A[p + j * lda];
+      A[p + j * lda] = t;
+    }
+  __syncthreads();
+  const double r = 1.0 / A[k + k * lda];
+  for (int64_t i = k + 1 + threadIdx.x; i < n; i += 256) A[i + k * lda] *= r;
+}
+
+__global__ void lu_update_kernel(double *__restrict__ A, int64_t n, int64_t lda, int64_t k,
+                                 const int *__restrict__ status) {
+  if (*(volatile const int *)status != 0) return;
+  const int64_t m = n - k - 1;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m * m;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k + 1 + e % m, j = k + 1 + e / m;
+    A[i + j * lda] -= A[i + k * lda] * A[k + j * lda];
+  }
+}
+
+void getrf(cudaStream_t s, double *A, int64_t n, int64_t lda, int *piv, int *status) {
+  for (int64_t k = 0; k < n; ++k) {
+    lu_pivot_kernel<<<1, 256, 0, s>>>(A, n, lda, k, piv, status);
+    GPGP_CHECK_LAUNCH();
+    const int64_t m = n - k - 1;
+    if (m > 0) {
+      const unsigned g = (unsigned)std::min<int64_t>((m * m + 255) / 256, 4 * 152);
+      lu_update_kernel<<<g, 256, 0, s>>>(A, n, lda, k, status);
+      GPGP_CHECK_LAUNCH();
+    }
+  }
+}
+
+// X <- A^-1 X with the factors of getrf: the row interchanges in order, then the
+// unit lower and the upper substitutions. One warp per right-hand side; the
+// lanes share each row's dot product.
+__global__ void getrs_kernel(const double *__restrict__ LU, int64_t n, int64_t lda, const int *__restrict__ piv,
+                             double *__restrict__ X, int64_t m, int64_t ldx, const int *__restrict__ status) {
+  const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (c >= m || *(volatile const int *)status != 0) return;
+  double *x = X + c * ldx;
+  if (lane == 0)
+    for (int64_t k = 0; k < n; ++k) {
+      const int64_t p = piv[k];
+      if (p != k) {
+        const double t = x[k];
+        x[k] = x[p];
+        x[p] = t;
+      }
+    }
+  __syncwarp();
+  for (int64_t i = 1; i < n; ++i) {  // unit lower
+    double acc = 0.0;
+    for (int64_t j = lane; j < i; j += 32) acc = fma(LU[i + j * lda], x[j], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[i] -= acc;
+    __syncwarp();
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {  // upper
+    double acc = 0.0;
+    for (int64_t j = i + 1 + lane; j < n; j += 32) acc = fma(LU[i + j * lda], x[j], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[i] = (x[i] - acc) / LU[i + i * lda];
+    __syncwarp();
+  }
+}
+
+void getrs(cudaStream_t s, const double *LU, int64_t n, int64_t lda, const int *piv, double *X, int64_t m,
+           int64_t ldx, const int *status) {
+  if (n <= 0 || m <= 0) return;
+  getrs_kernel<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(LU, n, lda, piv, X, m, ldx, status);
+  GPGP_CHECK_LAUNCH();
+}
+
 }  // namespace gpgp

@@ -47,6 +47,8 @@ gpgp_status gpgp_pred_cov(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
                           double *mean, double *cov) {
   if (!m || !xt || !mean || !cov || mt < 1) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
+  if (m->nlc || m->improper)
+    return fail(m->ctx, GPGP_EUNSUPPORTED, "predictive covariance of a non-log-concave fit is not available");
   if (m->fitc) return fail(m->ctx, GPGP_EUNSUPPORTED, "the full predictive covariance of method_fitc");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {

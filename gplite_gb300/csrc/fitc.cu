@@ -138,6 +138,12 @@ __global__ void fitc_d_kernel(int64_t n, const double *__restrict__ Kdiag, doubl
   if (i < n) D[i] = cs ? (Kdiag[i] + jit) - cs[i] : Kdiag[i] + jit;
 }
 
+// A_ii += d_i (n x n, leading dimension n)
+__global__ void add_diag2_kernel(double *__restrict__ A, int64_t n, const double *__restrict__ d) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[i + i * n] += d[i];
+}
+
 __global__ void fill_kernel(int64_t n, double v, double *__restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = v;
@@ -299,6 +305,160 @@ void fitc_fmean(gpgp_model *m, const double *alpha, double *fhat) {
   GPGP_CHECK_LAUNCH();
 }
 
+// The evidence of a non-log-concave FITC iteration (R/laplace.R:151-216,
+// R/ep.R:186-255): the good sites' lemma fit (the recursive laplace_iter / ep_iter),
+// the bad sites' prior given them through the inducing inputs,
+//   K21 = X_bad X_good^T, prior_cov = X_bad X_bad^T + diag(D_bad),
+//   pred_cov = prior_cov - K21 inv_lemma_solve(C_inv_good, K21^T),
+// and the shared bad-site terms (nlc.cu). *failed: a Cholesky inside the reference's
+// tryCatch failed (the fit's evidence is -Inf); *improper: chol(A) failed.
+gpgp_status fitc_nlc_terms(gpgp_model *m, Red &red, double logdet_z, bool ep, const double *logC, double *lml,
+                           double *lpu, bool *improper, bool *failed) {
+  FitcState &f = *m->fitc;
+  gpgp_ctx *ctx = m->ctx;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = m->n, M = f.M;
+  *improper = *failed = false;
+  std::vector<int> hg, hb;
+  IBuf good, bad;
+  split_sites(m, &hg, &hb, &good, &bad);
+  const int64_t ng = (int64_t)hg.size(), nb = (int64_t)hb.size();
+  if (ng == 0) return fail(ctx, GPGP_EUNSUPPORTED, "every pseudo-variance is <= 0: no good sites to condition on");
+  const double *trials = m->has_trials ? m->trials.p : nullptr;
+  const double *offset = m->has_offset ? m->offset.p : nullptr;
+  auto gat = [&](DBuf &dst, const double *src, int64_t ld, int64_t nf, const IBuf &idx, int64_t cnt) {
+    dst.alloc(st, std::max<int64_t>(cnt, 1) * nf);
+    gather_rows(st, src, ld, nf, idx.p, cnt, dst.p);
+  };
+  DBuf Ug, Xg, Xb, Dg, Vg, zg, yg, tg, og, Db, Vb, zb, yb, tb, ob;
+  gat(Ug, f.Kxz.p, n, M, good, ng);
+  gat(Xg, f.X.p, n, M, good, ng);
+  gat(Xb, f.X.p, n, M, bad, nb);
+  gat(Dg, f.D.p, n, 1, good, ng);
+  gat(Vg, m->V.p, n, 1, good, ng);
+  gat(zg, m->z.p, n, 1, good, ng);
+  gat(yg, m->y.p, n, 1, good, ng);
+  gat(Db, f.D.p, n, 1, bad, nb);
+  gat(Vb, m->V.p, n, 1, bad, nb);
+  gat(zb, m->z.p, n, 1, bad, nb);
+  gat(yb, m->y.p, n, 1, bad, nb);
+  if (trials) {
+    gat(tg, trials, n, 1, good, ng);
+    gat(tb, trials, n, 1, bad, nb);
+  }
+  if (offset) {
+    gat(og, offset, n, 1, good, ng);
+    gat(ob, offset, n, 1, bad, nb);
+  }
+  // the good sites' lemma: S = D + V, iDU = U / S, C_m = K_z + U^T S^-1 U
+  DBuf Sg, iDUg, VDU, Cm, Lm, Wm, a1, t, q, fg, lS;
+  Sg.alloc(st, ng);
+  axpy_vec_kernel<<<g1(ng), 256, 0, st>>>(ng, Dg.p, 1.0, Vg.p, Sg.p);
+  GPGP_CHECK_LAUNCH();
+  iDUg.alloc(st, ng * M);
+  div_rows_kernel<<<gs(ng * M), 256, 0, st>>>(ng, M, Ug.p, Sg.p, iDUg.p);
+  GPGP_CHECK_LAUNCH();
+  VDU.alloc(st, M * M);
+  gemm64(st, true, false, M, M, ng, 1.0, Ug.p, ng, iDUg.p, ng, 0.0, VDU.p, M);
+  Cm.alloc(st, M * M);
+  sym_add_kernel<<<gs(M * M), 256, 0, st>>>(M, f.Kz.p, VDU.p, Cm.p);
+  GPGP_CHECK_LAUNCH();
+  Lm.alloc(st, M * M);
+  Wm.alloc(st, ((M + NB - 1) / NB) * NB * NB);
+  GPGP_CUDA(cudaMemcpyAsync(Lm.p, Cm.p, M * M * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  double ldm = 0.0;
+  if (chol_small(ctx, Lm.p, M, Wm.p, &ldm) != 0) {
+    *failed = true;
+    return GPGP_OK;
+  }
+  lS.alloc(st, ng);
+  log_vec2_kernel<<<g1(ng), 256, 0, st>>>(ng, Sg.p, lS.p);
+  GPGP_CHECK_LAUNCH();
+  const double logdet_g = red.sum(lS.p, ng, 4) - 2.0 * logdet_z + 2.0 * ldm;
+  // alpha1 = z / S - iDU C_m^-1 (iDU^T z); f1 = U K_z^-1 (U^T alpha1) + D alpha1
+  a1.alloc(st, ng);
+  t.alloc(st, M);
+  q.alloc(st, ng);
+  fg.alloc(st, ng);
+  gemv64(st, true, ng, M, 1.0, iDUg.p, ng, zg.p, 0.0, t.p);
+  tri_vec(st, Lm.p, M, M, t.p, t.p, false);
+  tri_vec(st, Lm.p, M, M, t.p, t.p, true);
+  gemv64(st, false, ng, M, 1.0, iDUg.p, ng, t.p, 0.0, q.p);
+  div_vec_kernel<<<g1(ng), 256, 0, st>>>(ng, zg.p, Sg.p, a1.p);
+  GPGP_CHECK_LAUNCH();
+  vec_axpby(st, ng, -1.0, q.p, 1.0, a1.p);
+  gemv64(st, true, ng, M, 1.0, Ug.p, ng, a1.p, 0.0, t.p);
+  tri_vec(st, f.Lz.p, M, M, t.p, t.p, false);
+  tri_vec(st, f.Lz.p, M, M, t.p, t.p, true);
+  gemv64(st, false, ng, M, 1.0, Ug.p, ng, t.p, 0.0, q.p);
+  fma_vec_kernel<<<g1(ng), 256, 0, st>>>(ng, q.p, Dg.p, a1.p, fg.p);
+  GPGP_CHECK_LAUNCH();
+  double lml1, lpu1 = 0.0;
+  if (!ep) {
+    lik_loglik(st, m->lk, ng, fg.p, yg.p, trials ? tg.p : nullptr, offset ? og.p : nullptr, red.b.p + 400,
+               red.b.p + 200);
+    const double ll = read_scalar(ctx, red.b.p + 400);
+    const double fa = red.dot(fg.p, a1.p, ng);
+    log_vec2_kernel<<<g1(ng), 256, 0, st>>>(ng, Vg.p, lS.p);
+    GPGP_CHECK_LAUNCH();
+    const double slogV = red.sum(lS.p, ng, 5);
+    lml1 = ll - 0.5 * fa + 0.5 * (slogV - logdet_g);
+    lpu1 = ll - 0.5 * fa;
+  } else {
+    DBuf terms, tg2;
+    terms.alloc(st, n);
+    ep_terms2_kernel<<<g1(n), 256, 0, st>>>(n, logC, m->cav_var.p, m->cav_mean.p, m->z.p, m->V.p, terms.p);
+    GPGP_CHECK_LAUNCH();
+    gat(tg2, terms.p, n, 1, good, ng);
+    lml1 = -0.5 * logdet_g - 0.5 * red.dot(zg.p, a1.p, ng) + red.sum(tg2.p, ng, 6);
+  }
+  // the bad sites' prior given the good ones
+  DBuf K21, pm, pc, Q, Qc;
+  K21.alloc(st, nb * ng);
+  gemm64(st, false, true, nb, ng, M, 1.0, Xb.p, nb, Xg.p, ng, 0.0, K21.p, nb);
+  pm.alloc(st, nb);
+  gemv64(st, false, nb, ng, 1.0, K21.p, nb, a1.p, 0.0, pm.p);
+  // K21 inv_lemma_solve(C_inv, K21^T) = K21 S^-1 K21^T - (K21 iDU) C_m^-1 (K21 iDU)^T
+  Q.alloc(st, nb * M);
+  gemm64(st, false, false, nb, M, ng, 1.0, K21.p, nb, iDUg.p, ng, 0.0, Q.p, nb);
+  Qc.alloc(st, nb * M);
+  tri_rows(st, Lm.p, M, M, Q.p, nb, Qc.p, nb, nb, 0);
+  tri_rows(st, Lm.p, M, M, Qc.p, nb, Qc.p, nb, nb, 1);
+  pc.alloc(st, nb * nb);
+  gemm64(st, false, true, nb, nb, M, 1.0, Xb.p, nb, Xb.p, nb, 0.0, pc.p, nb);  // X_bad X_bad^T
+  {
+    DBuf KS;
+    KS.alloc(st, nb * ng);
+    GPGP_CUDA(cudaMemcpyAsync(KS.p, K21.p, nb * ng * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    DBuf iS;
+    iS.alloc(st, ng);
+    recip2_kernel<<<g1(ng), 256, 0, st>>>(ng, Sg.p, iS.p);
+    GPGP_CHECK_LAUNCH();
+    scale_cols_kernel<<<gs(nb * ng), 256, 0, st>>>(nb, ng, KS.p, iS.p);  // K21 S^-1
+    GPGP_CHECK_LAUNCH();
+    gemm64(st, false, true, nb, nb, ng, -1.0, KS.p, nb, K21.p, nb, 1.0, pc.p, nb);
+  }
+  gemm64(st, false, true, nb, nb, M, 1.0, Q.p, nb, Qc.p, nb, 1.0, pc.p, nb);
+  {
+    DBuf dd;
+    dd.alloc(st, nb);
+    GPGP_CUDA(cudaMemcpyAsync(dd.p, Db.p, nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    add_diag2_kernel<<<g1(nb), 256, 0, st>>>(pc.p, nb, dd.p);
+    GPGP_CHECK_LAUNCH();
+  }
+  double lml2 = 0.0, lpu2 = 0.0;
+  gpgp_status s2 = nlc_bad_terms(m, nb, bad.p, pm.p, pc.p, zb.p, Vb.p, yb.p, trials ? tb.p : nullptr,
+                                 offset ? ob.p : nullptr, ep, logC, &lml2, &lpu2, improper);
+  if (s2 != GPGP_OK) {
+    // chol(pred_cov) failing is an R error inside the reference's tryCatch: -Inf
+    *failed = true;
+    return GPGP_OK;
+  }
+  *lml = lml1 + lml2;
+  *lpu = lpu1 + lpu2;
+  return GPGP_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -390,24 +550,35 @@ gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing
       int hf = 0;
       GPGP_CUDA(cudaMemcpyAsync(&hf, flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
       GPGP_CUDA(cudaStreamSynchronize(st));
-      if (hf) {
-        res->status = GPGP_EUNSUPPORTED;
-        return fail(ctx, GPGP_EUNSUPPORTED,
-                    "non-log-concave FITC branch (R/laplace.R:153-232) is not implemented");
+      if (hf & 2) return minus_inf(GPGP_ENAN);  // NA in all(V > 0): an R error, caught by tryCatch
+      double nlc_lml = 0.0, nlc_lpu = 0.0;
+      if (hf & 4) {
+        // some pseudo-variance <= 0: the good / bad split (R/laplace.R:151-231)
+        bool improper = false, failed = false;
+        gpgp_status s2 = fitc_nlc_terms(m, red, logdet_z, false, nullptr, &nlc_lml, &nlc_lpu, &improper, &failed);
+        if (s2 != GPGP_OK) return s2;
+        // chol(A) failing returns no log_post_unnorm, on which R's loop then errors: -Inf
+        if (failed || improper) return minus_inf(GPGP_ENOT_PD);
       }
       axpy_vec_kernel<<<g1(n), 256, 0, st>>>(n, f.D.p, 1.0, m->V.p, f.S.p);  // S = D + V
       GPGP_CHECK_LAUNCH();
       if (!lemma_get(m, red, logdet_z)) return minus_inf(GPGP_ENOT_PD);
       lemma_solve_vec(m, m->z.p, m->alpha.p);
       fitc_fmean(m, m->alpha.p, fnew.p);
-      lik_loglik(st, m->lk, n, fnew.p, m->y.p, trials, offset, red.b.p + 400, red.b.p + 200);
-      const double ll = read_scalar(ctx, red.b.p + 400);
-      const double fa = red.dot(fnew.p, m->alpha.p, n);
-      log_vec2_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, lV.p);
-      GPGP_CHECK_LAUNCH();
-      const double slogV = red.sum(lV.p, n, 2);
-      lml = ll - 0.5 * fa + 0.5 * (slogV - f.logdet);
-      const double lpu = ll - 0.5 * fa;
+      double lpu;
+      if (hf & 4) {
+        lml = nlc_lml;
+        lpu = nlc_lpu;
+      } else {
+        lik_loglik(st, m->lk, n, fnew.p, m->y.p, trials, offset, red.b.p + 400, red.b.p + 200);
+        const double ll = read_scalar(ctx, red.b.p + 400);
+        const double fa = red.dot(fnew.p, m->alpha.p, n);
+        log_vec2_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, lV.p);
+        GPGP_CHECK_LAUNCH();
+        const double slogV = red.sum(lV.p, n, 2);
+        lml = ll - 0.5 * fa + 0.5 * (slogV - f.logdet);
+        lpu = ll - 0.5 * fa;
+      }
       GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fnew.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
       diff = lpu - old;
       old = lpu;
@@ -472,9 +643,22 @@ gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing
       GPGP_CUDA(cudaMemcpyAsync(m->fmean.p, fm_old.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
       return minus_inf(GPGP_ENAN);
     }
+    double nlc_lml = 0.0;
     if (hf & 4) {
-      res->status = GPGP_EUNSUPPORTED;
-      return fail(ctx, GPGP_EUNSUPPORTED, "non-log-concave FITC EP branch is not implemented");
+      // some site variance <= 0: the good / bad split (R/ep.R:186-272)
+      bool improper = false, failed = false;
+      double lpu_unused = 0.0;
+      gpgp_status s2 = fitc_nlc_terms(m, red, logdet_z, true, logC.p, &nlc_lml, &lpu_unused, &improper, &failed);
+      if (s2 != GPGP_OK) return s2;
+      if (failed) return minus_inf(GPGP_ENOT_PD);
+      if (improper) {
+        // R returns fmean = Inf: the sweep is rejected after an accepted one; on the
+        // first sweep R goes on without site variances and errors (tryCatch: -Inf)
+        if (!(diff_old < INFINITY)) return minus_inf(GPGP_ENOT_PD);
+        lml = -INFINITY;
+        damp = damp * m->approx.damping;
+        continue;
+      }
     }
     axpy_vec_kernel<<<g1(n), 256, 0, st>>>(n, f.D.p, 1.0, m->V.p, f.S.p);
     GPGP_CHECK_LAUNCH();
@@ -511,7 +695,7 @@ gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing
     const double za = red.dot(m->z.p, m->alpha.p, n);
     max_abs_diff(st, n, fm_old.p, m->fmean.p, red.b.p);
     diff_new = read_scalar(ctx, red.b.p + 64);
-    lml = -0.5 * f.logdet - 0.5 * za + sterm;
+    lml = (hf & 4) ? nlc_lml : -0.5 * f.logdet - 0.5 * za + sterm;
     if (diff_new > diff_old) {
       damp = damp * m->approx.damping;
       continue;

@@ -21,6 +21,28 @@ __device__ __forceinline__ double response(const LikDev &L, double f) {
 
 __device__ __forceinline__ double xlogy(double x, double y) { return x == 0.0 ? 0.0 : x * log(y); }
 
+// Digamma psi(x) for x > 0, from its recurrence psi(x) = psi(x + 1) - 1/x (lifting x
+// to >= 12) and the asymptotic series psi(x) = ln x - 1/(2x) - sum_k B_2k / (2k x^2k)
+// (Abramowitz & Stegun 6.3.18) through x^-14; the first omitted term is below
+// 3e-18 at x = 12.
+__device__ double digamma_pos(double x) {
+  double acc = 0.0;
+  while (x < 12.0) {
+    acc -= 1.0 / x;
+    x += 1.0;
+  }
+  const double r = 1.0 / x, r2 = r * r;
+  // B_2k / (2k): 1/12, -1/120, 1/252, -1/240, 1/132, -691/32760, 1/12
+  double p = 1.0 / 12.0;
+  p = fma(p, r2, -691.0 / 32760.0);
+  p = fma(p, r2, 1.0 / 132.0);
+  p = fma(p, r2, -1.0 / 240.0);
+  p = fma(p, r2, 1.0 / 252.0);
+  p = fma(p, r2, -1.0 / 120.0);
+  p = fma(p, r2, 1.0 / 12.0);
+  return acc + (log(x) - 0.5 * r - r2 * p);
+}
+
 // log p(y | f) for one observation; f already includes the offset.
 __device__ __forceinline__ double loglik1(const LikDev &L, double f, double y, double N) {
   switch (L.kind) {
@@ -38,6 +60,14 @@ __device__ __forceinline__ double loglik1(const LikDev &L, double f, double y, d
       const double mu = exp(f);
       return xlogy(y, mu) - mu - lgamma(y + 1.0);
     }
+    case GPGP_LIK_BETABINOM: {  // R/lik.R:332-354
+      const double mu = response(L, f);
+      const double a = mu / L.phi, b = (1.0 - mu) / L.phi;
+      const double term1 = lgamma(N + 1.0) - lgamma(y + 1.0) - lgamma(N - y + 1.0);
+      const double term2 = lgamma(y + a) + lgamma(N - y + b) - lgamma(N + a + b);
+      const double term3 = lgamma(a + b) - lgamma(a) - lgamma(b);
+      return term1 + term2 + term3;
+    }
     default:
       return nan("");
   }
@@ -52,11 +82,17 @@ __device__ __forceinline__ double loglik_d1(const LikDev &L, double f, double y,
   const double mu = response(L, f);
   const double dmu =
       (L.link == GPGP_LINK_PROBIT) ? exp(-0.5 * f * f) * 0.398942280401432677939946059934 : mu * (1.0 - mu);
+  if (L.kind == GPGP_LIK_BETABINOM) {  // R/lik.R:400-425
+    const double a = mu / L.phi, b = (1.0 - mu) / L.phi;
+    const double term2 = (dmu / L.phi) * (digamma_pos(y + a) - digamma_pos(N - y + b));
+    const double term3 = (dmu / L.phi) * (-digamma_pos(a) + digamma_pos(b));
+    return term2 + term3;
+  }
   return dmu * (y / mu - (N - y) / (1.0 - mu));
 }
 
 __device__ __forceinline__ double trials_of(const LikDev &L, const double *trials, int64_t i) {
-  if (L.kind == GPGP_LIK_BINOMIAL) return trials[i];
+  if (L.kind == GPGP_LIK_BINOMIAL || L.kind == GPGP_LIK_BETABINOM) return trials[i];
   return 1.0;
 }
 

@@ -122,6 +122,19 @@ struct FitcState {
   bool have_pred_cache = false;
 };
 
+// Blocks of a method_full fit whose last iteration took the non-log-concave
+// branch (nlc.cu): the good sites' factor and the Schur complement of the bad
+// ones, in place of a factor of B over all sites.
+struct NlcState {
+  int64_t ng = 0, nb = 0;
+  IBuf good, bad;       // site indices (V > 0, V <= 0)
+  DBuf sg, L1, W1;      // 1/sqrt(V_good), lower factor of B_good, its diagonal-block inverses
+  DBuf aux;             // L1^-1 s_good K(good, bad), ng x nb
+  DBuf Slu;             // LU of S = pred_cov + diag(V_bad), nb x nb
+  IBuf piv;
+  DBuf Fg, Fb;          // features of the good / bad training rows, filled on first prediction
+};
+
 }  // namespace gpgp
 
 struct gpgp_model {
@@ -147,6 +160,8 @@ struct gpgp_model {
   bool have_Linv = false;
   gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
   std::unique_ptr<gpgp::FitcState> fitc;
+  std::unique_ptr<gpgp::NlcState> nlc;  // set when the last iteration was non-log-concave
+  bool improper = false;  // the reference's -Inf fit without a posterior (chol(A) failed)
   bool has_trials = false, has_offset = false;
   double log_evidence = 0.0;
   int fitted = 0;
@@ -214,6 +229,18 @@ gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing
 gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double *mean,
                       double *var);
 gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar);
+
+// Non-log-concave branch of a method_full Laplace / EP iteration (nlc.cu).
+gpgp_status nlc_fit_full(gpgp_model *m, const double *K, const double *logC, bool ep, double *alpha, double *fnew,
+                         double *fvar, double *lml, bool *improper);
+// Predictive variances (device, mt) of a fit in m->nlc at test features Ft (mt rows).
+void nlc_pred_var(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double *var);
+// The bad sites' terms of the split given their prior N(pm, pc) (nlc.cu).
+gpgp_status nlc_bad_terms(gpgp_model *m, int64_t nb, const int *bad, const double *pm, const double *pc,
+                          const double *zb, const double *Vb, const double *yb, const double *tb, const double *ob,
+                          bool ep, const double *logC, double *lml2, double *lpu2, bool *improper);
+void gather_rows(cudaStream_t s, const double *F, int64_t ldf, int64_t nf, const int *idx, int64_t m, double *out);
+void split_sites(gpgp_model *m, std::vector<int> *hg, std::vector<int> *hb, IBuf *good, IBuf *bad);
 
 // Batched pipeline for the request server (batched.cu): one plan, one run, no
 // autotune or graph; lml[nprob], mean/var[sum m] packed in problem order.

@@ -259,8 +259,9 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     n, d = x.shape
     if len(y) != n:
         raise ValueError("x and y have different numbers of rows")
-    if gp.lik.kind == "binomial" and trials is None:
-        raise ValueError("trials must be provided for the binomial likelihood.")
+    if gp.lik.kind in ("binomial", "betabinom") and trials is None:
+        raise ValueError("trials must be provided for the %s likelihood." %
+                         ("binomial" if gp.lik.kind == "binomial" else "beta binomial"))
     learn_scales(gp, x)
     lib = L.load()
     ctx = L.default_context(device)

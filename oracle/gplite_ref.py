@@ -397,8 +397,10 @@ def get_loglik(lik, f, y, trials=None, offset=None, sum_=True):
         a = mu / lik.phi
         b = (1 - mu) / lik.phi
         g = sps.gammaln
-        ll = (g(N + 1) - g(y + 1) - g(N - y + 1) + g(y + a) + g(N - y + b) - g(N + a + b)
-              + g(a + b) - g(a) - g(b))
+        term1 = g(N + 1) - g(y + 1) - g(N - y + 1)
+        term2 = g(y + a) + g(N - y + b) - g(N + a + b)
+        term3 = g(a + b) - g(a) - g(b)
+        ll = term1 + term2 + term3  # R/lik.R:344-347
     else:
         raise ValueError(lik.kind)
     ll = np.broadcast_to(ll, f.shape).astype(np.float64)
@@ -497,12 +499,73 @@ def logsumexp_rows(L, w=None):
 # Laplace, full method (R/laplace.R:13-39, 274-297)
 # ----------------------------------------------------------------------------
 
-def laplace_iter_full(lik, K, y, fhat_old, trials=None, offset=None):
-    """laplace_iter.method_full, log-concave branch (R/laplace.R:13-39)."""
-    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset)
+def _sub(a, idx):
+    return None if a is None else np.asarray(a)[idx]
+
+
+def _fwd(L, b):
+    """forwardsolve(L, b)."""
+    return sla.solve_triangular(L, b, lower=True)
+
+
+def _bwd_t(L, b):
+    """backsolve(t(L), b) for a lower L."""
+    return sla.solve_triangular(L.T, b, lower=False)
+
+
+def _bad_site_terms(pred_mean, pred_cov, Vb, zb):
+    """The shared algebra of the non-log-concave branches (R/laplace.R:73-98,
+    R/ep.R:88-113): the prior of the bad sites given the good ones is
+    N(pred_mean, pred_cov); Lk = t(chol(pred_cov)), A = I + Lk^T V^-1 Lk. Returns
+    None when chol(A) fails (R returns log_evidence = -Inf there); chol(pred_cov)
+    failing is an error, as in R."""
+    Lk = sla.cholesky(pred_cov, lower=False).T
+    A = np.eye(len(Vb)) + Lk.T @ ((1 / Vb)[:, None] * Lk)
+    try:
+        A_chol = sla.cholesky(A, lower=False).T
+    except np.linalg.LinAlgError:
+        return None
+
+    def solve_a(v):  # backsolve(t(A_chol), forwardsolve(A_chol, v))
+        return _bwd_t(A_chol, _fwd(A_chol, v))
+    alpha2 = _bwd_t(Lk, solve_a(Lk.T @ (zb / Vb)))
+    aux = _bwd_t(Lk, _fwd(Lk, pred_mean))
+    aux = _bwd_t(Lk, solve_a(Lk.T @ aux))
+    f2hat = pred_cov @ (alpha2 + aux)
+    return dict(Lk=Lk, A_chol=A_chol, solve_a=solve_a, f2hat=f2hat,
+                invC2_V2_logdet=2 * np.log(np.diag(A_chol)).sum())
+
+
+def laplace_iter_full(lik, K, y, fhat_old, trials=None, offset=None, pobs=None):
+    """laplace_iter.method_full (R/laplace.R:13-119): the log-concave branch
+    (B factorisation, :21-38) and, when some pseudo-variance is <= 0, the split
+    p(y) = p(y_good) p(y_bad | y_good) with an LU of K + diag(V) for the final
+    fit (:40-116)."""
+    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset) if pobs is None else pobs
     n = len(z)
     if not np.all(V > 0):
-        raise NotImplementedError("non-log-concave branch (R/laplace.R:40-117)")
+        good = np.nonzero(V > 0)[0]
+        bad = np.nonzero(~(V > 0))[0]
+        if len(bad) > 500:
+            warnings.warn("More than 500 data points with pseudo-variance < 0 (outliers), computation "
+                          "getting slow. Check that the model and hyperparameter values are sensible.")
+        fit1 = laplace_iter_full(lik, K[np.ix_(good, good)], np.asarray(y)[good], None, _sub(trials, good),
+                                 _sub(offset, good), pobs=(z[good], V[good]))
+        K21 = K[np.ix_(bad, good)]
+        K22 = K[np.ix_(bad, bad)]
+        pred_mean = K21 @ fit1["alpha"]
+        aux = _fwd(fit1["C_chol"], K21.T)
+        pred_cov = K22 - aux.T @ aux
+        t = _bad_site_terms(pred_mean, pred_cov, V[bad], z[bad])
+        if t is None:
+            return dict(fmean=fhat_old, log_evidence=-np.inf)
+        df2 = (_fwd(t["Lk"], t["f2hat"] - pred_mean) ** 2).sum()
+        log_lik2 = get_loglik(lik, t["f2hat"], np.asarray(y)[bad], _sub(trials, bad), _sub(offset, bad))
+        lml2 = log_lik2 - 0.5 * df2 + 0.5 * t["invC2_V2_logdet"]
+        C_lu = sla.lu_factor(K + np.diag(V))
+        alpha = sla.lu_solve(C_lu, z)
+        return dict(fmean=K @ alpha, z=z, V=V, C_lu=C_lu, alpha=alpha,
+                    log_evidence=float(fit1["log_evidence"] + lml2))
     sv = np.sqrt(1 / V)
     B = np.eye(n) + sv[:, None] * (K * sv[None, :])
     Lb = sla.cholesky(B, lower=False).T
@@ -576,15 +639,46 @@ def get_pseudodata_ep(lik, post_mean, post_prec, z_old, P_old, y, quad_order=11,
 
 
 def ep_iter_full(lik, K, y, fmean_old, fvar_old, z_old, P_old, quad_order, damping,
-                 trials=None, offset=None):
-    """ep_iter.method_full, log-concave branch (R/ep.R:16-49, 140-145)."""
-    po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
-                           trials, offset)
+                 trials=None, offset=None, po=None):
+    """ep_iter.method_full (R/ep.R:16-145): the log-concave branch (:33-49) and, when
+    some site variance is <= 0, the split p(y_good) p(y_bad | y_good) with an LU of
+    K + diag(V) for the final fit (:50-138)."""
+    if po is None:
+        po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
+                               trials, offset)
     z, V = po["z"], po["var"]
     if np.any(np.isnan(V) | np.isnan(z)):
         return dict(fmean=fmean_old, log_evidence=-np.inf, nan=True)
     if not np.all(V > 0):
-        raise NotImplementedError("non-log-concave branch (R/ep.R:50-138)")
+        good = np.nonzero(V > 0)[0]
+        bad = np.nonzero(~(V > 0))[0]
+        if len(bad) > 500:
+            warnings.warn("More than 500 data points with pseudo-variance < 0 (outliers), computation "
+                          "getting slow. Check that the model and hyperparameter values are sensible.")
+        po1 = dict(z=z[good], var=V[good], log_C=po["log_C"][good], mean_cavity=po["mean_cavity"][good],
+                   var_cavity=po["var_cavity"][good], quad_ok=po["quad_ok"])
+        fit1 = ep_iter_full(lik, K[np.ix_(good, good)], np.asarray(y)[good], None, None, None, None,
+                            quad_order, damping, _sub(trials, good), _sub(offset, good), po=po1)
+        K21 = K[np.ix_(bad, good)]
+        K22 = K[np.ix_(bad, bad)]
+        pred_mean = K21 @ fit1["alpha"]
+        aux = _fwd(fit1["C_chol"], K21.T)
+        pred_cov = K22 - aux.T @ aux
+        Vb, zb = V[bad], z[bad]
+        t = _bad_site_terms(pred_mean, pred_cov, Vb, zb)
+        if t is None:
+            return dict(fmean=np.inf, log_evidence=-np.inf)
+        d = pred_mean - zb
+        df2 = d @ _bwd_t(t["Lk"], t["solve_a"](t["Lk"].T @ (d / Vb)))
+        vc, mc = po["var_cavity"], po["mean_cavity"]
+        lml2 = (-0.5 * df2 + 0.5 * t["invC2_V2_logdet"] + po["log_C"][bad].sum()
+                + 0.5 * np.log((vc[bad] + Vb) / Vb).sum() + 0.5 * ((mc[bad] - zb) ** 2 / (vc[bad] + Vb)).sum())
+        C_lu = sla.lu_factor(K + np.diag(V))
+        alpha = sla.lu_solve(C_lu, z)
+        fvar = V * np.diag(sla.lu_solve(C_lu, K))
+        return dict(fmean=K @ alpha, fvar=fvar, cavity_mean=mc, cavity_var=vc, z=z, P=1 / V, V=V,
+                    C_lu=C_lu, alpha=alpha, log_evidence=float(fit1["log_evidence"] + lml2),
+                    quad_ok=po["quad_ok"])
     n = len(z)
     sv = np.sqrt(1 / V)
     B = np.eye(n) + sv[:, None] * (K * sv[None, :])
@@ -624,6 +718,8 @@ def ep_full(lik, K, y, maxiter=300, tol=1e-4, damping=0.9, damping_min=0.1, quad
             damp = damp * damping
             continue
         damp = max(damp, damping_min)
+        if "fvar" not in fit:  # R goes on with fvar_old = NULL and errors in the next sweep
+            raise ValueError("EP: the first sweep has an improper posterior for the bad sites")
         fmean_old, fvar_old, z_old, P_old = fit["fmean"], fit["fvar"], fit["z"], fit["P"]
         diff_old = diff_new
         if diff_new < tol:
@@ -695,11 +791,45 @@ def fitc_prepare(cfs, x, z, jitter):
     return Kz, Kxz, Kz_chol, K_diag, D
 
 
-def laplace_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fhat_old, trials=None, offset=None):
-    """laplace_iter.method_fitc, log-concave branch (R/laplace.R:122-152)."""
-    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset)
+def _fitc_bad_prior(Kz_chol, Kxz, D, good, bad, fit1):
+    """Prior of the bad sites given the good ones under FITC (R/laplace.R:179-186,
+    R/ep.R:219-226): K21 through the inducing inputs, the bad sites' own FITC prior
+    covariance, and the lemma solve with the good fit's C_inv."""
+    Lb = _fwd(Kz_chol, Kxz[bad].T)
+    K21 = Lb.T @ _fwd(Kz_chol, Kxz[good].T)
+    prior_cov = Lb.T @ Lb + np.diag(D[bad])
+    pred_mean = K21 @ fit1["alpha"]
+    pred_cov = prior_cov - K21 @ inv_lemma_solve(fit1["C_inv"], K21.T)
+    return pred_mean, pred_cov
+
+
+def laplace_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fhat_old, trials=None, offset=None, pobs=None):
+    """laplace_iter.method_fitc (R/laplace.R:122-238): the log-concave branch
+    (:136-150) and, when some pseudo-variance is <= 0, the good / bad split with the
+    lemma of the whole data (S = D + V, no log-determinant) for the final fit (:151-231)."""
+    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset) if pobs is None else pobs
     if not np.all(V > 0):
-        raise NotImplementedError("non-log-concave branch (R/laplace.R:153-232)")
+        good = np.nonzero(V > 0)[0]
+        bad = np.nonzero(~(V > 0))[0]
+        if len(bad) > 500:
+            warnings.warn("More than 500 data points with pseudo-variance < 0 (outliers), computation "
+                          "getting slow. Check that the model and hyperparameter values are sensible.")
+        fit1 = laplace_iter_fitc(lik, Kz, Kz_chol, Kxz[good], D[good], np.asarray(y)[good], None,
+                                 _sub(trials, good), _sub(offset, good), pobs=(z[good], V[good]))
+        pred_mean, pred_cov = _fitc_bad_prior(Kz_chol, Kxz, D, good, bad, fit1)
+        t = _bad_site_terms(pred_mean, pred_cov, V[bad], z[bad])
+        if t is None:
+            return dict(fmean=fhat_old, log_evidence=-np.inf)
+        df2 = (_fwd(t["Lk"], t["f2hat"] - pred_mean) ** 2).sum()
+        log_lik2 = get_loglik(lik, t["f2hat"], np.asarray(y)[bad], _sub(trials, bad), _sub(offset, bad))
+        lpu2 = float(log_lik2 - 0.5 * df2)
+        lml2 = log_lik2 - 0.5 * df2 + 0.5 * t["invC2_V2_logdet"]
+        Ci = inv_lemma_get(Kz, Kxz, D + V, logdet=False)
+        alpha = inv_lemma_solve(Ci, z)
+        fhat = Kxz @ _chol_solve_lower(Kz_chol, Kxz.T @ alpha) + D * alpha
+        return dict(fmean=fhat, z=z, V=V, Kz=Kz, Kxz=Kxz, Kz_chol=Kz_chol, C_inv=Ci, diag=D, alpha=alpha,
+                    log_evidence=float(fit1["log_evidence"] + lml2),
+                    log_post_unnorm=float(fit1["log_post_unnorm"] + lpu2))
     S = D + V
     Ci = inv_lemma_get(Kz, Kxz, S)
     alpha = inv_lemma_solve(Ci, z)
@@ -734,15 +864,45 @@ def laplace_fitc(lik, Kz, Kz_chol, Kxz, D, y, maxiter=100, tol=1e-4, trials=None
 
 
 def ep_iter_fitc(lik, Kz, Kz_chol, Kxz, D, y, fmean_old, fvar_old, z_old, P_old, quad_order, damping,
-                 trials=None, offset=None):
-    """ep_iter.method_fitc, log-concave branch (R/ep.R:148-185, 274-279)."""
-    po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
-                           trials, offset)
+                 trials=None, offset=None, po=None):
+    """ep_iter.method_fitc (R/ep.R:148-279): the log-concave branch (:167-185) and,
+    when some site variance is <= 0, the good / bad split with the lemma of the whole
+    data for the final fit (:186-272)."""
+    if po is None:
+        po = get_pseudodata_ep(lik, fmean_old, 1 / fvar_old, z_old, P_old, y, quad_order, damping,
+                               trials, offset)
     z, V = po["z"], po["var"]
     if np.any(np.isnan(V) | np.isnan(z)):
         return dict(fmean=fmean_old, log_evidence=-np.inf, nan=True)
     if not np.all(V > 0):
-        raise NotImplementedError("non-log-concave branch (R/ep.R:186-272)")
+        good = np.nonzero(V > 0)[0]
+        bad = np.nonzero(~(V > 0))[0]
+        if len(bad) > 500:
+            warnings.warn("More than 500 data points with pseudo-variance < 0 (outliers), computation "
+                          "getting slow. Check that the model and hyperparameter values are sensible.")
+        po1 = dict(z=z[good], var=V[good], log_C=po["log_C"][good], mean_cavity=po["mean_cavity"][good],
+                   var_cavity=po["var_cavity"][good], quad_ok=po["quad_ok"])
+        fit1 = ep_iter_fitc(lik, Kz, Kz_chol, Kxz[good], D[good], np.asarray(y)[good], None, None, None, None,
+                            quad_order, damping, _sub(trials, good), _sub(offset, good), po=po1)
+        pred_mean, pred_cov = _fitc_bad_prior(Kz_chol, Kxz, D, good, bad, fit1)
+        Vb, zb = V[bad], z[bad]
+        t = _bad_site_terms(pred_mean, pred_cov, Vb, zb)
+        if t is None:
+            return dict(fmean=np.inf, log_evidence=-np.inf)
+        d = pred_mean - zb
+        df2 = d @ _bwd_t(t["Lk"], t["solve_a"](t["Lk"].T @ (d / Vb)))
+        vc, mc = po["var_cavity"], po["mean_cavity"]
+        lml2 = (-0.5 * df2 + 0.5 * t["invC2_V2_logdet"] + po["log_C"][bad].sum()
+                + 0.5 * np.log((vc[bad] + Vb) / Vb).sum() + 0.5 * ((mc[bad] - zb) ** 2 / (vc[bad] + Vb)).sum())
+        Ci = inv_lemma_get(Kz, Kxz, D + V, logdet=False)
+        alpha = inv_lemma_solve(Ci, z)
+        inv_Kz_Kzx = _chol_solve_lower(Kz_chol, Kxz.T)
+        aux = inv_lemma_solve(Ci, V, inv_Kz_Kzx, rhs_diag=True)
+        fvar = (Kxz.T * aux).sum(0) + inv_lemma_solve(Ci, V, D, rhs_diag=True, lhs_diag=True, diag_only=True)
+        fmean = Kxz @ _chol_solve_lower(Kz_chol, Kxz.T @ alpha) + D * alpha
+        return dict(fmean=fmean, fvar=fvar, cavity_mean=mc, cavity_var=vc, z=z, P=1 / V, V=V, Kz=Kz,
+                    Kxz=Kxz, Kz_chol=Kz_chol, C_inv=Ci, diag=D, alpha=alpha,
+                    log_evidence=float(fit1["log_evidence"] + lml2), quad_ok=po["quad_ok"])
     S = D + V
     Ci = inv_lemma_get(Kz, Kxz, S)
     alpha = inv_lemma_solve(Ci, z)
@@ -783,6 +943,8 @@ def ep_fitc(lik, Kz, Kz_chol, Kxz, K_diag, D, y, damping=0.9, damping_min=0.1, m
             damp = damp * damping
             continue
         damp = max(damp, damping_min)
+        if "fvar" not in fit:  # R goes on with fvar_old = NULL and errors in the next sweep
+            raise np.linalg.LinAlgError("EP: the first sweep has an improper posterior for the bad sites")
         fmean_old, fvar_old, z_old, P_old = fit["fmean"], fit["fvar"], fit["z"], fit["P"]
         diff_old = diff_new
         if diff_new < tol:
@@ -1056,12 +1218,14 @@ def gp_energy_grad(gp, include_prior=True, threads=1):
 
 
 def gp_pred_post_full(gp, xt, var=False, cfind=None):
-    """gp_pred_post.method_full (R/gp_pred.R:202-232), Cholesky branch."""
+    """gp_pred_post.method_full (R/gp_pred.R:202-232)."""
     Kt = eval_cf(gp.cfs, xt, gp.x, cfind)
     mean = Kt @ gp.fit["alpha"]
     if not var:
         return dict(mean=mean)
     Ktt_diag = eval_cf(gp.cfs, xt, xt, cfind, diag_only=True)
+    if gp.fit.get("C_chol") is None:  # LU of K + diag(V) (non-log-concave fit, R/gp_pred.R:220-223)
+        return dict(mean=mean, var=Ktt_diag - (Kt * sla.lu_solve(gp.fit["C_lu"], Kt.T).T).sum(1))
     aux = sla.solve_triangular(gp.fit["C_chol"], Kt.T, lower=True)
     return dict(mean=mean, var=Ktt_diag - (aux * aux).sum(0))
 

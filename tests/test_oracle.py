@@ -244,3 +244,38 @@ def test_fitc_and_c4_fixtures_reproduce():
         gp = R.gp_fit(R.gp_init([R.cf(p["kind"], lscale=p["lscale"], magn=1.0)],
                                 R.lik("gaussian", sigma=p["sigma"])), p["x"], y)
         assert gp.fit["log_evidence"] == c["lml"][i]
+
+
+def _betabinom_outliers(n=60, seed=2):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-3, 3, n)
+    N = np.full(n, 20.0)
+    y = rng.binomial(20, 1 / (1 + np.exp(-1.5 * x))).astype(float)
+    out = np.argsort(-np.abs(x))[:4]
+    y[out] = np.where(x[out] > 0, 0.0, 20.0)
+    return x, y, N
+
+
+@pytest.mark.parametrize("approx", ["laplace", "ep"])
+def test_nonlogconcave_split_is_consistent(approx):
+    """The oracle's split branch (R/laplace.R:40-117, R/ep.R:50-138) with beta-binomial
+    outliers: some pseudo-variances are <= 0, the final alpha solves
+    (K + diag(V)) alpha = z through the LU, and FITC with every training input as an
+    inducing input (its own split, R/laplace.R:151-231, R/ep.R:186-272) reaches
+    nearly the same evidence."""
+    x, y, N = _betabinom_outliers()
+    ap = (lambda: R.approx_laplace()) if approx == "laplace" else (lambda: R.approx_ep())
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        gp = R.gp_fit(R.gp_init([R.cf("sexp", lscale=1.5, magn=2.0)], R.lik("betabinom", phi=0.3),
+                                approx=ap()), x, y, trials=N)
+        gf = R.gp_fit(R.gp_init([R.cf("sexp", lscale=1.5, magn=2.0)], R.lik("betabinom", phi=0.3),
+                                approx=ap(), method=R.method_fitc(x)), x, y, trials=N)
+    f = gp.fit
+    assert "C_lu" in f and np.any(f["V"] <= 0)
+    K = R.eval_cf(gp.cfs, gp.x, gp.x) + 1e-6 * np.eye(len(y))
+    assert np.allclose((K + np.diag(f["V"])) @ f["alpha"], f["z"], rtol=1e-9, atol=1e-9)
+    assert np.isfinite(f["log_evidence"]) and np.isfinite(gf.fit["log_evidence"])
+    assert abs(gf.fit["log_evidence"] - f["log_evidence"]) < 1e-3 * abs(f["log_evidence"])
+    pr = R.gp_pred(gp, np.linspace(-3, 3, 9), var=True)
+    assert np.all(pr["var"] > 0)
