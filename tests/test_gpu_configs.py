@@ -159,7 +159,8 @@ def test_c4_every_bucket_to_1024(precision):
     """The batched plan on two problems per size bucket (64 .. 1024). Evidence relative to
     max(|LML|, n) (a sum of n-extensive terms; a near-zero evidence would make rounding
     look large); vectors relative to their largest entry, at max(base, 100 x the oracle's
-    one-ulp sensitivity x the roundoff ratio of the precision: 1 for FP64, 2^12 for the
+    one-ulp sensitivity (the largest over four nudges: the LOO variance cancels for
+    small sigma) x the roundoff ratio of the precision: 1 for FP64, 2^12 for the
     40-bit slices of the mixed plan)."""
     g = load("c4_sample.npz")
     probs = [S.c4_problem(i, n) for i, n in enumerate(S.C4_SIZES)]
