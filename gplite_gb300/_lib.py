@@ -130,6 +130,7 @@ SIGNATURES = {
     "gpgp_pred": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_pred_dev": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_loo": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "gpgp_loo_mc": (C.c_int, [_P, C.c_int64, _P, _P, _P]),
     "gpgp_pred_cov": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, C.c_double, _P, _P]),
     "gpgp_kmeans": (C.c_int, [_P, _P, C.c_int64, C.c_int32, C.c_int32, _P, C.c_int32, _P, _P, _P]),
     "gpgp_mvn_draw": (C.c_int, [_P, _P, _P, C.c_int64, _P, C.c_int64, _P]),

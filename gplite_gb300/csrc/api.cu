@@ -1020,12 +1020,18 @@ gpgp_status gpgp_pred_dev(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
   return pred_impl(m, xt, mt, group_mask, mean, var, true);
 }
 
-gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *loo_sum) {
+// gp_loo (R/gp_loo.R:73-109): the LOO posteriors, then Gauss-Hermite quadrature of
+// order quad_order (draws == 0) or Monte Carlo with the caller's standard normals z
+// (n x draws, column-major: fsample = loo_mean + sd z, as R fills it).
+static gpgp_status loo_impl(gpgp_model *m, int32_t quad_order, int64_t draws, const double *z, double *loos,
+                            double *loo_sum) {
   if (!m || !loos) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "invalid argument");
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
   if (m->improper)
     return fail(m->ctx, GPGP_ENOT_FITTED, "the fit has no posterior (log_evidence = -Inf, improper bad-site posterior)");
-  if (quad_order < 1 || quad_order > 64) return fail(m->ctx, GPGP_EINVAL, "quad_order must be in 1..64");
+  if (draws == 0 && (quad_order < 1 || quad_order > 64))
+    return fail(m->ctx, GPGP_EINVAL, "quad_order must be in 1..64");
+  if (draws < 0 || (draws > 0 && !z)) return fail(m->ctx, GPGP_EINVAL, "draws > 0 needs the normals z");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {
     GPGP_CUDA(cudaSetDevice(ctx->device));
@@ -1064,13 +1070,20 @@ gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *lo
       mp = lmean.p;
       vp = lvar.p;
     }
-    std::vector<double> hx, hw;
-    gauss_hermite(quad_order, &hx, &hw);
-    copy_in(s, ghx, hx.data(), quad_order, false);
-    copy_in(s, ghw, hw.data(), quad_order, false);
     out.alloc(s, n);
-    lik_loo_gh(s, m->lk, n, quad_order, ghx.p, ghw.p, mp, vp, m->y.p,
-               m->has_trials ? m->trials.p : nullptr, m->has_offset ? m->offset.p : nullptr, out.p);
+    if (draws > 0) {
+      DBuf dz;
+      copy_in(s, dz, z, (size_t)n * draws, false);
+      lik_loo_mc(s, m->lk, n, draws, dz.p, mp, vp, m->y.p, m->has_trials ? m->trials.p : nullptr,
+                 m->has_offset ? m->offset.p : nullptr, out.p);
+    } else {
+      std::vector<double> hx, hw;
+      gauss_hermite(quad_order, &hx, &hw);
+      copy_in(s, ghx, hx.data(), quad_order, false);
+      copy_in(s, ghw, hw.data(), quad_order, false);
+      lik_loo_gh(s, m->lk, n, quad_order, ghx.p, ghw.p, mp, vp, m->y.p,
+                 m->has_trials ? m->trials.p : nullptr, m->has_offset ? m->offset.p : nullptr, out.p);
+    }
     GPGP_CUDA(cudaMemcpyAsync(loos, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     GPGP_CUDA(cudaStreamSynchronize(s));
     if (loo_sum) {
@@ -1080,6 +1093,15 @@ gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *lo
     }
     return GPGP_OK;
   });
+}
+
+gpgp_status gpgp_loo(gpgp_model *m, int32_t quad_order, double *loos, double *loo_sum) {
+  return loo_impl(m, quad_order, 0, nullptr, loos, loo_sum);
+}
+
+gpgp_status gpgp_loo_mc(gpgp_model *m, int64_t draws, const double *z, double *loos, double *loo_sum) {
+  if (draws < 1) return fail(m ? m->ctx : nullptr, GPGP_EINVAL, "draws must be positive");
+  return loo_impl(m, 0, draws, z, loos, loo_sum);
 }
 
 gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_sigma) {

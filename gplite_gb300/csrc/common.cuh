@@ -317,6 +317,11 @@ void lik_loo_gh(cudaStream_t s, const LikDev &lk, int64_t n, int q, const double
                 const double *ghw, const double *mean, const double *var, const double *y,
                 const double *trials, const double *offset, double *loos);
 
+// LOO densities by Monte Carlo with given standard normals z (n x draws,
+// column-major) (R/gp_loo.R:97-103).
+void lik_loo_mc(cudaStream_t s, const LikDev &lk, int64_t n, int64_t draws, const double *z, const double *mean,
+                const double *var, const double *y, const double *trials, const double *offset, double *loos);
+
 // Elementwise helpers.
 void vec_axpby(cudaStream_t s, int64_t n, double a, const double *x, double b, double *y);
 void vec_mul(cudaStream_t s, int64_t n, const double *a, const double *b, double *out);

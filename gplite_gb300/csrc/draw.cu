@@ -49,7 +49,6 @@ gpgp_status gpgp_pred_cov(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
   if (m->nlc || m->improper)
     return fail(m->ctx, GPGP_EUNSUPPORTED, "predictive covariance of a non-log-concave fit is not available");
-  if (m->fitc) return fail(m->ctx, GPGP_EUNSUPPORTED, "the full predictive covariance of method_fitc");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {
     GPGP_CUDA(cudaSetDevice(ctx->device));
@@ -62,6 +61,15 @@ gpgp_status gpgp_pred_cov(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
     Ft.alloc(s, (size_t)mt * std::max(1, m->dk.nfeat));
     prep_features(s, m->dk, m->prep, dxt.p, mt, mt, Ft.p, mt);
     dmean.alloc(s, mt);
+    if (m->fitc) {  // gp_pred_post.method_fitc(cov = TRUE), R/gp_pred.R:263-276
+      C.alloc(s, (size_t)mt * mt);
+      gpgp_status st = pred_cov_fitc(m, Ft.p, mt, gm, jitter, dmean.p, C.p);
+      if (st != GPGP_OK) return st;
+      GPGP_CUDA(cudaMemcpyAsync(mean, dmean.p, mt * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(cov, C.p, (size_t)mt * mt * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaStreamSynchronize(s));
+      return GPGP_OK;
+    }
     cov_matvec(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, dmean.p);
     // K(xt, xt), both triangles
     C.alloc(s, (size_t)mt * mt);

@@ -793,6 +793,45 @@ gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, 
   return GPGP_OK;
 }
 
+// Full predictive covariance of a FITC fit (gp_pred_post.method_fitc with cov = TRUE,
+// R/gp_pred.R:263-276, test points apart from the training inputs):
+//   prior_cov = A2^T A2 + diag(Dt),  A2 = Lz^-1 K(z, xt) (the rows of X2 = A2^T),
+//   cov = prior_cov - A2^T sol A2 + jitter I,  sol = A1 C^-1 A1^T (the cached Sig1).
+// Mean as in pred_fitc. C is mt x mt column-major (device).
+gpgp_status pred_cov_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double jitter, double *mean,
+                          double *C) {
+  FitcState &f = *m->fitc;
+  cudaStream_t st = m->ctx->stream;
+  const int64_t n = m->n, M = f.M;
+  DBuf Ktz, X2, v1, Dt, cs, T;
+  Ktz.alloc(st, (size_t)mt * M);
+  X2.alloc(st, (size_t)mt * M);
+  v1.alloc(st, M);
+  cov_matrix(st, m->dk, gm, Ft, mt, mt, f.Fz.p, M, M, Ktz.p, mt, COV_FULL, 0, 0, 0.0, nullptr);
+  tri_rows(st, f.Lz.p, M, M, Ktz.p, mt, X2.p, mt, mt, 0);        // X2 = Ktz Lz^-T
+  gemv64(st, true, n, M, 1.0, f.X.p, n, m->alpha.p, 0.0, v1.p);  // Kt_aux1 alpha
+  gemv64(st, false, mt, M, 1.0, X2.p, mt, v1.p, 0.0, mean);
+  // Dt = diag K(xt, xt) - colSums(Kt_aux2^2)
+  Dt.alloc(st, mt);
+  cs.alloc(st, mt);
+  cov_diag(st, m->dk, gm, Ft, mt, Ft, mt, mt, Dt.p);
+  rowdot_nn_kernel<<<g1(mt), 256, 0, st>>>(M, mt, X2.p, X2.p, cs.p);
+  GPGP_CHECK_LAUNCH();
+  vec_axpby(st, mt, -1.0, cs.p, 1.0, Dt.p);
+  gemm64(st, false, true, mt, mt, M, 1.0, X2.p, mt, X2.p, mt, 0.0, C, mt);  // A2^T A2
+  add_diag2_kernel<<<g1(mt), 256, 0, st>>>(C, mt, Dt.p);
+  GPGP_CHECK_LAUNCH();
+  fitc_pred_cache(m);
+  T.alloc(st, (size_t)mt * M);
+  gemm64(st, false, false, mt, M, M, 1.0, X2.p, mt, f.Sig1.p, M, 0.0, T.p, mt);  // A2^T sol
+  gemm64(st, false, true, mt, mt, M, -1.0, T.p, mt, X2.p, mt, 1.0, C, mt);
+  fill_kernel<<<g1(mt), 256, 0, st>>>(mt, jitter, cs.p);
+  GPGP_CHECK_LAUNCH();
+  add_diag2_kernel<<<g1(mt), 256, 0, st>>>(C, mt, cs.p);
+  GPGP_CHECK_LAUNCH();
+  return GPGP_OK;
+}
+
 // Training-point posterior (gp_pred_post.method_fitc with train = TRUE,
 // R/gp_pred.R:262-290) turned into LOO moments (R/gp_loo.R:119-129).
 gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar) {

@@ -272,6 +272,39 @@ void lik_loo_gh(cudaStream_t s, const LikDev &lk, int64_t n, int q, const double
   GPGP_CHECK_LAUNCH();
 }
 
+// Monte Carlo LOO densities (R/gp_loo.R:97-103): per site, logsumexp over the draws of
+// log p(y_i | mean_i + sd_i z_ik) minus log(draws); z is n x draws, column-major.
+// One warp per site; the lanes share the draws, the maxima and sums are combined
+// in a fixed order.
+__global__ void loo_mc_kernel(LikDev L, int64_t n, int64_t draws, const double *__restrict__ z,
+                              const double *__restrict__ mean, const double *__restrict__ var,
+                              const double *__restrict__ y, const double *__restrict__ trials,
+                              const double *__restrict__ offset, double *__restrict__ loos) {
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const double sd = sqrt(var[i]);
+  const double mu = mean[i];
+  const double off = offset ? offset[i] : 0.0;
+  const double N = trials_of(L, trials, i);
+  const double yi = y[i];
+  double mx = -INFINITY;
+  for (int64_t k = lane; k < draws; k += 32) mx = fmax(mx, loglik1(L, (mu + sd * z[i + k * n]) + off, yi, N));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  double acc = 0.0;
+  for (int64_t k = lane; k < draws; k += 32)
+    acc += exp(loglik1(L, (mu + sd * z[i + k * n]) + off, yi, N) - mx);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) loos[i] = (mx + log(acc)) - log((double)draws);
+}
+
+void lik_loo_mc(cudaStream_t s, const LikDev &lk, int64_t n, int64_t draws, const double *z, const double *mean,
+                const double *var, const double *y, const double *trials, const double *offset, double *loos) {
+  if (n == 0) return;
+  loo_mc_kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(lk, n, draws, z, mean, var, y, trials, offset, loos);
+  GPGP_CHECK_LAUNCH();
+}
+
 // ---------------------------------------------------------------------------
 // elementwise helpers
 // ---------------------------------------------------------------------------

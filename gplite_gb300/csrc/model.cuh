@@ -229,6 +229,8 @@ gpgp_status fit_fitc(gpgp_model *m, gpgp_fit_result *res, const double *inducing
 gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double *mean,
                       double *var);
 gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar);
+gpgp_status pred_cov_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double jitter, double *mean,
+                          double *C);
 
 // Non-log-concave branch of a method_full Laplace / EP iteration (nlc.cu).
 gpgp_status nlc_fit_full(gpgp_model *m, const double *K, const double *logC, bool ep, double *alpha, double *fnew,

@@ -496,17 +496,25 @@ def _generate_target(lik, f, rng, trials=None):
 
 
 def gp_pred_cov(gp, xnew, cfind=None, jitter=None):
-    """gp_pred_post(cov = TRUE) / gp_pred_prior(cov = TRUE) for method_full
-    (R/gp_pred.R:140-153, 202-232): mean and the full covariance + jitter I."""
+    """gp_pred_post(cov = TRUE) / gp_pred_prior(cov = TRUE) (R/gp_pred.R:140-184,
+    202-276): mean and the full covariance + jitter I, for method_full and
+    method_fitc."""
     xnew = _as_x(xnew)
     m = xnew.shape[0]
     jit = JITTER_DEFAULT if jitter is None else float(jitter)
     if not _is_fitted(gp):
-        if gp.method.kind == "fitc":
-            raise NotImplementedError("prior covariance of method_fitc")
+        if gp.method.kind == "fitc":  # gp_pred_prior.method_fitc (R/gp_pred.R:158-184)
+            if gp.method.inducing is None:
+                raise RuntimeError("Inducing points not set yet.")
+            z = _as_x(gp.method.inducing)
+            Kz = eval_cf(gp.cfs, z, z) + jit * np.eye(z.shape[0])
+            Ktz = eval_cf(gp.cfs, xnew, z)
+            Lz = np.linalg.cholesky(Kz)
+            from scipy.linalg import solve_triangular
+            aux = solve_triangular(Lz, Ktz.T, lower=True)
+            D = eval_cf(gp.cfs, xnew, xnew, diag_only=True) - (aux * aux).sum(0)
+            return np.zeros(m), aux.T @ aux + np.diag(D) + jit * np.eye(m)
         return np.zeros(m), eval_cf(gp.cfs, xnew, xnew, cfind) + jit * np.eye(m)
-    if gp.method.kind == "fitc":
-        raise NotImplementedError("the full predictive covariance of method_fitc")
     mean = np.empty(m)
     cov = np.empty((m, m), order="F")
     xf = L.fortran(xnew)
@@ -548,11 +556,13 @@ def gp_draw(gp, xnew, draws=None, transform=True, target=False, marginal=False, 
 
 
 def gp_loo(gp, x, y, quadrature=True, quad_order=11, draws=4000, jitter=None, seed=None, **kw):
-    """gp_loo (R/gp_loo.R:73-109) with Gauss-Hermite quadrature, on the fitted data."""
+    """gp_loo (R/gp_loo.R:73-109) on the fitted data: Gauss-Hermite quadrature of order
+    quad_order, or (quadrature = False) Monte Carlo with `draws` samples of each LOO
+    posterior. R draws those normals from its own stream (set.seed(seed)), which cannot
+    be reproduced here; numpy's generator seeded by `seed` draws them instead, in R's
+    order (an n x draws matrix filled column by column)."""
     if not _is_fitted(gp):
         raise RuntimeError("The provied GP model is not fitted. Please call gp_fit (or gp_optim) first.")
-    if not quadrature:
-        raise NotImplementedError("Monte Carlo LOO (quadrature = FALSE) is not implemented")
     x = _as_x(x)
     y = np.asarray(y, dtype=np.float64).ravel()
     if x.shape != gp.x.shape or not np.array_equal(x, gp.x) or not np.array_equal(y, gp.fit["y"]):
@@ -560,7 +570,12 @@ def gp_loo(gp, x, y, quadrature=True, quad_order=11, draws=4000, jitter=None, se
     n = len(y)
     loos = np.empty(n)
     s = C.c_double(0.0)
-    st = L.load().gpgp_loo(gp._model, int(quad_order), L.ptr(loos), C.byref(s))
+    if quadrature:
+        st = L.load().gpgp_loo(gp._model, int(quad_order), L.ptr(loos), C.byref(s))
+    else:
+        draws = int(draws)
+        z = np.asfortranarray(np.random.default_rng(seed).standard_normal((n, draws)))
+        st = L.load().gpgp_loo_mc(gp._model, draws, z.ctypes.data_as(C.c_void_p), L.ptr(loos), C.byref(s))
     L.check(st, None)
     return dict(loo=float(loos.sum()), sd=float(n * (np.std(loos, ddof=1) / math.sqrt(n))), loos=loos)
 

@@ -297,6 +297,12 @@ gpgp_status gpgp_kmeans(gpgp_ctx *ctx, const double *x, int64_t n, int32_t d, in
 /* ---- LOO: replaces loo_posteriors + the quadrature of gp_loo
  *      (R/gp_loo.R:73-133) on the model's own training data. ------------- */
 gpgp_status gpgp_loo(gpgp_model *model, int32_t quad_order, double *loos, double *loo_sum);
+/* Monte Carlo LOO (gp_loo with quadrature = FALSE, R/gp_loo.R:97-103): z holds
+ * n x draws standard normals (column-major, host memory; the reference draws them
+ * with stats::rnorm in the same order), fsample = loo_mean + sqrt(loo_var) z and
+ * loos_i = logsumexp_k log p(y_i | fsample_ik) - log(draws). */
+gpgp_status gpgp_loo_mc(gpgp_model *model, int64_t draws, const double *z, double *loos,
+                        double *loo_sum);
 
 /* ---- batched small GPs: many independent regressions of uneven size --
  * Each problem is gp_fit (lik_gaussian, method_full, one covariance term of

@@ -1314,14 +1314,21 @@ def loo_posteriors(gp, x):
     return fhat - loo_var * grad, loo_var
 
 
-def gp_loo(gp, x, y, quad_order=11, trials=None, offset=None):
-    """gp_loo (R/gp_loo.R:73-109), quadrature branch."""
+def gp_loo(gp, x, y, quad_order=11, trials=None, offset=None, z=None):
+    """gp_loo (R/gp_loo.R:73-109): the quadrature branch, or with z (n x draws standard
+    normals standing in for stats::rnorm's, filled in R's column-major order) the Monte
+    Carlo branch: fsample = loo_mean + sqrt(loo_var) z, loos = logsumexp - log(draws)."""
     if getattr(gp, "fit", None) is None or not gp.fitted:
         raise RuntimeError("The provided GP model is not fitted.")
     m, v = loo_posteriors(gp, x)
-    fg, w = gauss_hermite_points_scaled(m, np.sqrt(v), quad_order)
-    ll = get_loglik(gp.lik, fg, y, trials, offset, sum_=False)
-    loos = logsumexp_rows(ll, w)
+    if z is not None:
+        fs = m[:, None] + np.sqrt(v)[:, None] * z
+        ll = get_loglik(gp.lik, fs, y, trials, offset, sum_=False)
+        loos = logsumexp_rows(ll) - math.log(z.shape[1])
+    else:
+        fg, w = gauss_hermite_points_scaled(m, np.sqrt(v), quad_order)
+        ll = get_loglik(gp.lik, fg, y, trials, offset, sum_=False)
+        loos = logsumexp_rows(ll, w)
     n = len(y)
     return dict(loo=float(loos.sum()), sd=float(n * (np.std(loos, ddof=1) / math.sqrt(n))), loos=loos)
 
