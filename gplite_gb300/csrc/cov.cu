@@ -410,9 +410,13 @@ void cov_diag(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const do
 // ---------------------------------------------------------------------------
 // fused K x v
 // ---------------------------------------------------------------------------
+// Block (x, y) takes rows [x CT, (x+1) CT) of x1 and the y-th of gridDim.y equal
+// ranges of x2 tiles; with one range it writes out, otherwise its partial sums go to
+// out + y n1 and a second kernel adds the ranges in order.
 __global__ void __launch_bounds__(256) cov_matvec_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1, int64_t ld1, int64_t n1,
                                   const double *__restrict__ F2, int64_t ld2, int64_t n2,
-                                  const double *__restrict__ v, double *__restrict__ out) {
+                                  const double *__restrict__ v, double *__restrict__ out,
+                                  int64_t tiles_per_range) {
   extern __shared__ double sm[];
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
@@ -421,11 +425,15 @@ __global__ void __launch_bounds__(256) cov_matvec_kernel(DevKernel dk, uint32_t 
   double *vj = sm + 2 * CT * lds;
   double *red = vj + CT;  // 4 x CT partials
   const int64_t i0 = (int64_t)blockIdx.x * CT;
+  out += (int64_t)blockIdx.y * n1;
   load_feats(Fi, lds, F1, ld1, i0, n1, nf);
   const int r = threadIdx.x % CT;
   const int cb = threadIdx.x / CT;
   double acc = 0.0;
-  for (int64_t j0 = 0; j0 < n2; j0 += CT) {
+  const int64_t jbeg = (int64_t)blockIdx.y * tiles_per_range * CT;
+  const int64_t jlim = jbeg + tiles_per_range * CT;
+  const int64_t jend = jlim < n2 ? jlim : n2;
+  for (int64_t j0 = jbeg; j0 < jend; j0 += CT) {
     __syncthreads();
     load_feats(Fj, lds, F2, ld2, j0, n2, nf);
     if (threadIdx.x < CT) vj[threadIdx.x] = (j0 + threadIdx.x < n2) ? v[j0 + threadIdx.x] : 0.0;
@@ -447,6 +455,16 @@ __global__ void __launch_bounds__(256) cov_matvec_kernel(DevKernel dk, uint32_t 
   }
 }
 
+// out[i] = sum over the ranges r (in order) of part[r n1 + i]
+__global__ void sum_ranges_kernel(const double *__restrict__ part, int64_t nr, int64_t n1,
+                                  double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n1) return;
+  double t = part[i];
+  for (int64_t r = 1; r < nr; ++r) t += part[r * n1 + i];
+  out[i] = t;
+}
+
 void cov_matvec(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
                 int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2,
                 const double *v, double *out) {
@@ -459,9 +477,25 @@ void cov_matvec(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const 
                                    (2 * CT * 65 + 5 * CT) * 8));
     return 1;
   });
-  unsigned nb = (unsigned)((n1 + CT - 1) / CT);
-  cov_matvec_kernel<<<nb, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, v, out);
+  const int64_t T1 = (n1 + CT - 1) / CT, T2 = std::max<int64_t>(1, (n2 + CT - 1) / CT);
+  // enough blocks for two per SM: split the x2 tiles into equal ranges
+  const int64_t want = std::max<int64_t>(1, (2 * device_sms() + T1 - 1) / T1);
+  const int64_t tpr = (T2 + std::min(want, T2) - 1) / std::min(want, T2);
+  const int64_t nrange = (T2 + tpr - 1) / tpr;
+  if (nrange == 1) {
+    cov_matvec_kernel<<<dim3((unsigned)T1, 1), 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, v, out,
+                                                               tpr);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
+  double *part = nullptr;
+  GPGP_CUDA(cudaMallocAsync((void **)&part, (size_t)nrange * n1 * sizeof(double), s));
+  cov_matvec_kernel<<<dim3((unsigned)T1, (unsigned)nrange), 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2,
+                                                                            n2, v, part, tpr);
   GPGP_CHECK_LAUNCH();
+  sum_ranges_kernel<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(part, nrange, n1, out);
+  GPGP_CHECK_LAUNCH();
+  GPGP_CUDA(cudaFreeAsync(part, s));
 }
 
 // ---------------------------------------------------------------------------

@@ -232,13 +232,29 @@ __device__ __forceinline__ double rsqrt_fast(double x) {
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
-// Factor: right-looking over the 64 columns; warp 0 takes the pivots (inverse
-// square root, rsqrt_fast) one column ahead while warps 1-7 apply the rank-1
-// updates, one barrier per column. Inverse W = L^-1 by forward substitution over the
-// rows, all columns at once with four threads per column (partial dot
-// products combined by shuffles); a column only depends on itself, so rows
-// advance with warp synchronisation alone. log L_jj are summed in a fixed
-// tree order.
+// On this part one FP64 warp instruction occupies its sub-partition's FP64 unit
+// for about 64 cycles whether 1 or 32 lanes are active, so the kernel is laid out
+// to issue as few FP64 warp instructions as possible, each with all lanes busy,
+// and to keep the serial pivot chain on a sub-partition of its own:
+//  - factor, right-looking over the 64 columns: warp 0 takes the pivots one
+//    column ahead (column j+1 gets its update from column j, then its inverse
+//    square root, rsqrt_fast) while the update warps apply the rank-1 update of
+//    column j to the trailing triangle c >= j+2. The trailing triangle's entries
+//    are numbered by column, last column first, so that step j's entries are the
+//    first (62-j)(63-j)/2 of one fixed list: every update warp instruction has
+//    all 32 lanes on distinct entries. Warp 4, which shares warp 0's
+//    sub-partition, takes no update work. One barrier per column.
+//  - inverse W = L^-1, right-looking over the rows: at step r every entry
+//    (r', c), r' > r, c <= r, takes acc(r', c) += L(r', r) W(r, c); the entries of
+//    row r + 1 are final after that, and the thread that adds the last term to
+//    (r + 1, c) also writes W(r + 1, c) = -acc rd(r + 1). Entries are again
+//    spread evenly over all lanes; one barrier per row.
+//  - log L_jj summed in a fixed tree order.
+__device__ __forceinline__ int div_small(int e, int d, int magic) {
+  // e / d for e < 4096, 1 <= d <= 64, magic = ceil(2^20 / d): exact on that range
+  return (int)(((unsigned)e * (unsigned)magic) >> 20);
+}
+
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                                          double *__restrict__ Winv,
                                                          double *__restrict__ logdet_part,
@@ -253,13 +269,23 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   __shared__ double Wsm[NB][NB + 1];
   __shared__ double rdiag[NB];
   __shared__ double lg[NB];
+  __shared__ unsigned short pairs[NB * (NB + 1) / 2];  // (r | c << 8), column-major from the last column
   __shared__ int failed;
   if (*(volatile int *)status != 0) return;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   for (int idx = tid; idx < NB * NB; idx += 256) {
-    int r = idx % NB, c = idx / NB;
+    const int r = idx % NB, c = idx / NB;
     S[r][c] = (r < kb && c < kb && r >= c) ? A[r + c * lda] : 0.0;
+    Wsm[r][c] = 0.0;
+  }
+  // entry e: u = 63 - c is the largest u with u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2
+  for (int e = tid; e < NB * (NB + 1) / 2; e += 256) {
+    int u = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+    while (u * (u + 1) / 2 > e) --u;
+    while ((u + 1) * (u + 2) / 2 <= e) ++u;
+    const int c = NB - 1 - u, r = c + (e - u * (u + 1) / 2);
+    pairs[e] = (unsigned short)(r | (c << 8));
   }
   if (tid == 0) failed = 0;
   __syncthreads();
@@ -286,21 +312,21 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   if (warp == 0) pivot(0);
   __syncthreads();
   if (failed) return;
-  // Step j: warp 0 looks ahead (column j+1 takes its update from column j, then
-  // its pivot), while warps 1-7 update columns j+2.. with column j; the serial
-  // pivot chain so overlaps the rank-1 work, with one barrier per column.
+  // update workers: warps 1-3 and 5-7 (warp 4 shares warp 0's sub-partition)
+  const int uw = warp < 4 ? warp - 1 : warp - 2;  // 0..5 for the update warps
+  const int ut = uw * 32 + lane;
   for (int j = 0; j + 1 < kb; ++j) {
     if (warp == 0) {
       const double l = S[j + 1][j];
       for (int r = j + 1 + lane; r < kb; r += 32) S[r][j + 1] -= S[r][j] * l;
       __syncwarp();
       pivot(j + 1);
-    } else {
-      // pairs (r, c), j+2 <= c <= r < kb, over a 16 x 14 thread grid
-      const int t = tid - 32, tr = t & 15, tc = t >> 4;
-      for (int c = j + 2 + tc; c < kb; c += 14) {
-        const double lc = S[c][j];
-        for (int r = c + ((tr - (c - (j + 2)) % 16 + 16) % 16); r < kb; r += 16) S[r][c] -= S[r][j] * lc;
+    } else if (warp != 4) {
+      const int cnt = (62 - j) * (63 - j) / 2;  // entries with c >= j + 2
+      for (int e = ut; e < cnt; e += 192) {
+        const unsigned short pc = pairs[e];
+        const int r = pc & 0xFF, c = pc >> 8;
+        S[r][c] -= S[r][j] * S[c][j];
       }
     }
     __syncthreads();
@@ -308,31 +334,31 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   }
   // write the factor back (lower part of the block)
   for (int idx = tid; idx < kb * kb; idx += 256) {
-    int r = idx % kb, c = idx / kb;
+    const int r = idx % kb, c = idx / kb;
     if (r >= c) A[r + c * lda] = S[r][c];
   }
-  // inverse: column c = tid / 4, part p = tid % 4
-  {
-    const int c = tid >> 2, p = tid & 3;
-    for (int r = 0; r < NB; ++r) {
-      double part = 0.0;
-      if (c < r && r < kb)
-        for (int k = c + p; k < r; k += 4) part = fma(S[r][k], Wsm[k][c], part);
-      part += __shfl_xor_sync(0xffffffffu, part, 1);
-      part += __shfl_xor_sync(0xffffffffu, part, 2);
-      if (p == 0) {
-        double w = 0.0;
-        if (r < kb && c < kb) w = (r == c) ? rdiag[r] : (c < r ? -part * rdiag[r] : 0.0);
-        Wsm[r][c] = w;
-      }
-      __syncwarp();
+  // inverse, right-looking over the rows; Wsm holds the accumulators of rows not yet final
+  if (tid == 0) Wsm[0][0] = rdiag[0];
+  __syncthreads();
+  for (int r = 0; r + 1 < kb; ++r) {
+    const int w = r + 1;                 // columns c = 0..r of each updated row
+    const int cnt = (kb - 1 - r) * w;    // entries (r', c), r < r' < kb
+    const int magic = ((1 << 20) + w - 1) / w;
+    const double rdn = rdiag[r + 1];
+    for (int e = tid; e < cnt; e += 256) {
+      const int q = div_small(e, w, magic);
+      const int c = e - q * w, rr = r + 1 + q;
+      const double acc = fma(S[rr][r], Wsm[r][c], Wsm[rr][c]);
+      Wsm[rr][c] = (rr == r + 1) ? -acc * rdn : acc;
     }
+    if (tid == 0) Wsm[r + 1][r + 1] = rdn;
+    __syncthreads();
   }
   if (tid < NB) lg[tid] = tid < kb ? log(S[tid][tid]) : 0.0;
   __syncthreads();
   for (int idx = tid; idx < NB * NB; idx += 256) {
-    int r = idx % NB, c = idx / NB;
-    Winv[r + c * NB] = Wsm[r][c];
+    const int r = idx % NB, c = idx / NB;
+    Winv[r + c * NB] = (r < kb && c <= r) ? Wsm[r][c] : 0.0;
   }
   for (int st = NB / 2; st > 0; st >>= 1) {
     if (tid < st) lg[tid] += lg[tid + st];

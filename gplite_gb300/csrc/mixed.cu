@@ -173,19 +173,32 @@ __global__ void __launch_bounds__(256) oz_split_kernel(const double *__restrict_
     if (r0 + lane < nrb * OZ_TR) ex[r0 + lane] = e;
   }
   __syncthreads();
-  const int64_t ngroups = nkb * 8, nkc = 2 * nkb;
-  for (int64_t item = threadIdx.x; item < 32 * ngroups; item += 256) {
-    const int rl = trans ? (int)(item / ngroups) : (int)(item % 32);
-    const int64_t g = trans ? item % ngroups : item / 32;
-    const int64_t r = r0 + rl, k0 = g * 8;
+  // The block's 32 rows go through shared memory 64 K at a time, read along the
+  // operand's contiguous direction (rows for trans = 0, K for trans = 1), so that
+  // the slices are written with consecutive lanes on consecutive rows in either
+  // layout (four full 128-byte lines per store).
+  __shared__ double T[32][65];
+  const int64_t nkc = 2 * nkb;
+  const int rl = threadIdx.x & 31, gl = threadIdx.x >> 5;  // row, 8-wide K group of the chunk
+  const int64_t r = r0 + rl;
+  const int e = exs[rl];
+  for (int64_t kb0 = 0; kb0 < nkb * 64; kb0 += 64) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = threadIdx.x + 256 * q;
+      const int ar = trans ? idx / 64 : idx % 32, ak = trans ? idx % 64 : idx / 32;
+      T[ar][ak] = oz_elem(P, ld, trans, r0 + ar, kb0 + ak, rows, K);
+    }
+    __syncthreads();
     if (r >= nrb * OZ_TR) continue;
-    const int e = exs[rl];
+    const int64_t k0 = kb0 + 8 * gl;
     uint32_t packed[S][4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
       int d0[S], d1[S];
-      oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j, rows, K), e, d0);
-      oz_digits<S>(oz_elem(P, ld, trans, r, k0 + j + 1, rows, K), e, d1);
+      oz_digits<S>(T[rl][8 * gl + j], e, d0);
+      oz_digits<S>(T[rl][8 * gl + j + 1], e, d1);
 #pragma unroll
       for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t], t) | (bf16_of_digit(d1[t], t) << 16);
     }
