@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fp64math.cuh"
 #include "model.cuh"
 
 namespace gpgp {
@@ -56,11 +57,11 @@ __device__ __forceinline__ double bat_kernel(int kind, double lscale, double m2,
     const double df = xi[k * si] - xj[k * sj];
     r2 += df * df;
   }
-  if (kind == GPGP_CF_SEXP) return m2 * exp(-0.5 * r2 * (1.0 / (lscale * lscale)));
+  if (kind == GPGP_CF_SEXP) return m2 * exp_fast(-0.5 * r2 * (1.0 / (lscale * lscale)));
   const double c = (kind == GPGP_CF_MATERN32 ? sqrt(3.0) : sqrt(5.0)) / lscale;
-  const double a = c * sqrt(r2);
-  if (kind == GPGP_CF_MATERN32) return m2 * (1.0 + a) * exp(-a);
-  return m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp(-a);
+  const double a = c * sqrt_fast(r2);
+  if (kind == GPGP_CF_MATERN32) return m2 * (1.0 + a) * exp_fast(-a);
+  return m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp_fast(-a);
 }
 
 // B = I + s (K + jitter I) s on the lower triangle; identity on the padding.

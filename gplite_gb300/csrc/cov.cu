@@ -10,6 +10,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "fp64math.cuh"
 
 namespace gpgp {
 
@@ -256,10 +257,10 @@ __device__ __forceinline__ double term_value(const DevTerm &T, const double *fi,
         double df = fi[c] - fj[c];
         r2 += df * df;
       }
-      if (T.kind == GPGP_CF_SEXP) return T.m2 * exp(-0.5 * r2 * T.c1);
-      double a = T.c1 * sqrt(r2);
-      if (T.kind == GPGP_CF_MATERN32) return T.m2 * (1.0 + a) * exp(-a);
-      return T.m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp(-a);
+      if (T.kind == GPGP_CF_SEXP) return T.m2 * exp_fast(-0.5 * r2 * T.c1);
+      double a = T.c1 * sqrt_fast(r2);
+      if (T.kind == GPGP_CF_MATERN32) return T.m2 * (1.0 + a) * exp_fast(-a);
+      return T.m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp_fast(-a);
     }
   }
 }
@@ -562,12 +563,12 @@ __device__ __forceinline__ double term_value_grad(const DevTerm &T, const double
       }
       double dk_dr2;
       if (T.kind == GPGP_CF_SEXP) {
-        k = T.m2 * exp(-0.5 * r2 * T.c1);
+        k = T.m2 * exp_fast(-0.5 * r2 * T.c1);
         dv[0] = k * r2 * T.c1;
         dk_dr2 = -0.5 * T.c1 * k;
       } else {
-        const double a = T.c1 * sqrt(r2);
-        const double e = exp(-a);
+        const double a = T.c1 * sqrt_fast(r2);
+        const double e = exp_fast(-a);
         if (T.kind == GPGP_CF_MATERN32) {
           k = T.m2 * (1.0 + a) * e;
           dv[0] = T.m2 * a * a * e;
@@ -594,12 +595,31 @@ __device__ __forceinline__ double term_value_grad(const DevTerm &T, const double
   }
 }
 
+// parameter slots that term_value_grad can set for a term (bit p: slot p)
+__device__ __forceinline__ int term_param_mask(const DevTerm &T) {
+  switch (T.kind) {
+    case GPGP_CF_CONST:
+      return 2;
+    case GPGP_CF_LIN:
+      return 2 | (T.periodic ? 16 : 0);
+    case GPGP_CF_NN:
+      return 14;
+    default:
+      return 3 | (T.periodic ? 16 : 0);
+  }
+}
+
 constexpr int GT = 64;
 
+// NT > 0: a kernel of exactly NT terms, loops unrolled so that the accumulators
+// stay in registers; NT == 0: any number of terms (dk.nterms).
+template <int NT>
 __global__ void __launch_bounds__(256) cov_grad_kernel(DevKernel dk, const double *__restrict__ F, int64_t ldf, int64_t n,
                                 const double *__restrict__ W, int64_t ldw,
                                 double *__restrict__ part) {
   extern __shared__ double sm[];
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
   double *Fi = sm;
@@ -611,33 +631,45 @@ __global__ void __launch_bounds__(256) cov_grad_kernel(DevKernel dk, const doubl
   load_feats(Fi, lds, F, ldf, i0, n, nf);
   load_feats(Fj, lds, F, ldf, j0, n, nf);
   __syncthreads();
-  const int np = dk.nterms * GPGP_TERM_NPARAM;
-  double acc[GPGP_MAX_TERMS * GPGP_TERM_NPARAM];
-  for (int p = 0; p < np; ++p) acc[p] = 0.0;
+  const int np = nterms * GPGP_TERM_NPARAM;
+  double acc[MT * GPGP_TERM_NPARAM];
+#pragma unroll
+  for (int p = 0; p < MT * GPGP_TERM_NPARAM; ++p) acc[p] = 0.0;
+  int pmask[MT];
+#pragma unroll
+  for (int t = 0; t < MT; ++t) pmask[t] = t < nterms ? term_param_mask(dk.t[t]) : 0;
   const int r = threadIdx.x % GT;
   const int cb = threadIdx.x / GT;
   const int64_t i = i0 + r;
-  double kv[GPGP_MAX_TERMS];
-  double dv[GPGP_MAX_TERMS][GPGP_TERM_NPARAM];
+  double kv[MT];
+  double dv[MT][GPGP_TERM_NPARAM];
 #pragma unroll 1
   for (int q = 0; q < GT / 4; ++q) {
     const int c = cb + 4 * q;
     const int64_t j = j0 + c;
     if (i >= n || j >= n || j > i) continue;
     const double w = W[i + j * ldw] * (i == j ? 1.0 : 2.0);
-    for (int t = 0; t < dk.nterms; ++t)
-      kv[t] = term_value_grad(dk.t[t], Fi + r * lds + dk.t[t].off, Fj + c * lds + dk.t[t].off,
-                              dv[t]);
-    for (int t = 0; t < dk.nterms; ++t) {
+#pragma unroll
+    for (int t = 0; t < MT; ++t)
+      if (t < nterms)
+        kv[t] = term_value_grad(dk.t[t], Fi + r * lds + dk.t[t].off, Fj + c * lds + dk.t[t].off, dv[t]);
+#pragma unroll
+    for (int t = 0; t < MT; ++t) {
+      if (t >= nterms) break;
       double others = 1.0;
-      for (int u = 0; u < dk.nterms; ++u)
-        if (u != t && dk.t[u].group == dk.t[t].group) others *= kv[u];
+#pragma unroll
+      for (int u = 0; u < MT; ++u)
+        if (u < nterms && u != t && dk.t[u].group == dk.t[t].group) others *= kv[u];
       const double f = w * others;
-      for (int p = 0; p < GPGP_TERM_NPARAM; ++p) acc[t * GPGP_TERM_NPARAM + p] += f * dv[t][p];
+#pragma unroll
+      for (int p = 0; p < GPGP_TERM_NPARAM; ++p)
+        if (pmask[t] & (1 << p)) acc[t * GPGP_TERM_NPARAM + p] = fma(f, dv[t][p], acc[t * GPGP_TERM_NPARAM + p]);
     }
   }
   // block reduction per parameter, fixed order
-  for (int p = 0; p < np; ++p) {
+#pragma unroll
+  for (int p = 0; p < MT * GPGP_TERM_NPARAM; ++p) {
+    if (p >= np) break;
     red[threadIdx.x] = acc[p];
     __syncthreads();
     for (int st = 128; st > 0; st >>= 1) {
@@ -678,13 +710,28 @@ gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double 
   size_t smem = (size_t)(2 * GT * lds + 256) * sizeof(double);
   static PerDevice attr;
   per_device(attr, [] {
-    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (2 * GT * 65 + 256) * 8));
+    const int mx = (2 * GT * 65 + 256) * 8;
+    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_grad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     return 1;
   });
   int64_t T = (n + GT - 1) / GT;
   int64_t nt = T * (T + 1) / 2;
-  cov_grad_kernel<<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+  switch (dk.nterms) {
+    case 1:
+      cov_grad_kernel<1><<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+      break;
+    case 2:
+      cov_grad_kernel<2><<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+      break;
+    case 3:
+      cov_grad_kernel<3><<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+      break;
+    default:
+      cov_grad_kernel<0><<<(unsigned)nt, 256, smem, s>>>(dk, F, ldf, n, W, ldw, part);
+  }
   GPGP_CHECK_LAUNCH();
   reduce_partials_kernel<<<1, 256, 0, s>>>(part, nt, dk.nterms * GPGP_TERM_NPARAM, g);
   GPGP_CHECK_LAUNCH();

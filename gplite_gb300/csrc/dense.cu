@@ -16,6 +16,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fp64math.cuh"
 
 namespace gpgp {
 
@@ -207,48 +208,31 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
                  tri_mode);
 }
 
-__device__ __noinline__ double rsqrt_slow(double x) { return 1.0 / sqrt(x); }
-
-// 1/sqrt(x) for a positive finite x. The FP32 estimate rsqrtf(x) comes from a
-// float built out of x's bits with integer operations (and goes back the same
-// way), so no FP64 conversion or compare sits on the pivot chain; the estimate
-// y0 (relative error ~2^-22) is refined by the binomial series
-//   (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 + O(e^3),  e = 1 - x y0^2,
-// four dependent FP64 operations whose neglected terms are ~2^-66. Arguments
-// outside the float range take sqrt and division out of line.
-__device__ __forceinline__ double rsqrt_fast(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int E = (int)(b >> 52);
-  if (E < 1023 - 125 || E > 1023 + 125) return rsqrt_slow(x);
-  const float xf = __uint_as_float(((uint32_t)(E - 1023 + 127) << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
-  const uint32_t yb = __float_as_uint(rsqrtf(xf));
-  const double y0 = __longlong_as_double(
-      (long long)(((unsigned long long)(((yb >> 23) & 0xFFu) - 127u + 1023u) << 52) |
-                  ((unsigned long long)(yb & 0x7FFFFFu) << 29)));
-  const double e = fma(-(x * y0), y0, 1.0);
-  return fma(y0 * e, fma(e, 0.375, 0.5), y0);
-}
-
 // ---------------------------------------------------------------------------
 // diagonal block: factor + invert in shared memory (one CTA)
 // ---------------------------------------------------------------------------
-// On this part one FP64 warp instruction occupies its sub-partition's FP64 unit
-// for about 64 cycles whether 1 or 32 lanes are active, so the kernel is laid out
-// to issue as few FP64 warp instructions as possible, each with all lanes busy,
-// and to keep the serial pivot chain on a sub-partition of its own:
-//  - factor, right-looking over the 64 columns: warp 0 takes the pivots one
-//    column ahead (column j+1 gets its update from column j, then its inverse
-//    square root, rsqrt_fast) while the update warps apply the rank-1 update of
-//    column j to the trailing triangle c >= j+2. The trailing triangle's entries
-//    are numbered by column, last column first, so that step j's entries are the
-//    first (62-j)(63-j)/2 of one fixed list: every update warp instruction has
-//    all 32 lanes on distinct entries. Warp 4, which shares warp 0's
-//    sub-partition, takes no update work. One barrier per column.
-//  - inverse W = L^-1, right-looking over the rows: at step r every entry
-//    (r', c), r' > r, c <= r, takes acc(r', c) += L(r', r) W(r, c); the entries of
-//    row r + 1 are final after that, and the thread that adds the last term to
-//    (r + 1, c) also writes W(r + 1, c) = -acc rd(r + 1). Entries are again
-//    spread evenly over all lanes; one barrier per row.
+// On this part the FP64 pipe retires about 2 lane operations per clock per SM,
+// and a warp instruction occupies it whether 1 or 32 lanes are active, so the
+// kernel issues as few FP64 warp instructions as it can, each with all lanes on
+// distinct entries, and runs the factor and the inverse in one loop with one
+// barrier per column:
+//  - factor, right-looking: warp 0 takes the pivots one column ahead (column
+//    j+1 gets its update from column j, then its inverse square root,
+//    rsqrt_fast) while the update warps apply the rank-1 update of column j to
+//    the trailing triangle c >= j+2. The trailing triangle's entries are
+//    numbered by column, last column first, so that step j's entries are the
+//    first (62-j)(63-j)/2 of one fixed list. Warp 4, which shares warp 0's
+//    sub-partition, takes no update work.
+//  - inverse: W = L^-1 = D^-1 V with D = diag(L) and V the unit lower triangular
+//    inverse of the column-scaled factor L D^-1:
+//      V(i, c) = -sum_{k=c..i-1} (L(i, k) / L(k, k)) V(k, c),  V(c, c) = 1.
+//    The k = c term is written by the pivot of column c (V(i, c) starts as
+//    -L(i, c) / L(c, c)); the terms k > c are added right-looking, step k adding
+//    V(i, k) V(k, c) to every (i > k, c < k) while V(i, k) still holds only its
+//    first term. Step k needs column k of L and rows <= k of V final, so it runs
+//    beside the factor's step k + 1 in the same loop iteration. Every inverse
+//    entry costs one FMA; the row scaling by 1 / L(i, i) happens once, on the
+//    way out.
 //  - log L_jj summed in a fixed tree order.
 __device__ __forceinline__ int div_small(int e, int d, int magic) {
   // e / d for e < 4096, 1 <= d <= 64, magic = ceil(2^20 / d): exact on that range
@@ -266,7 +250,7 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   logdet_part += blockIdx.x * sL;
   status += blockIdx.x;
   __shared__ double S[NB][NB + 1];
-  __shared__ double Wsm[NB][NB + 1];
+  __shared__ double V[NB][NB + 1];
   __shared__ double rdiag[NB];
   __shared__ double lg[NB];
   __shared__ unsigned short pairs[NB * (NB + 1) / 2];  // (r | c << 8), column-major from the last column
@@ -277,7 +261,7 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int r = idx % NB, c = idx / NB;
     S[r][c] = (r < kb && c < kb && r >= c) ? A[r + c * lda] : 0.0;
-    Wsm[r][c] = 0.0;
+    V[r][c] = 0.0;
   }
   // entry e: u = 63 - c is the largest u with u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2
   for (int e = tid; e < NB * (NB + 1) / 2; e += 256) {
@@ -289,7 +273,8 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   }
   if (tid == 0) failed = 0;
   __syncthreads();
-  // pivot of column j by warp 0: L_jj and the scaled column below it
+  // pivot of column j by warp 0: L_jj, the scaled column below it and the first
+  // term of column j of V
   auto pivot = [&](int j) {
     const double dj = S[j][j];
     // not positive (sign bit or zero) or not finite, tested on the bits
@@ -303,7 +288,11 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
     }
     const double rp = rsqrt_fast(dj);
     const double piv = dj * rp;
-    for (int r = j + 1 + lane; r < kb; r += 32) S[r][j] *= rp;
+    for (int r = j + 1 + lane; r < kb; r += 32) {
+      const double l = S[r][j] * rp;
+      S[r][j] = l;
+      V[r][j] = -(l * rp);
+    }
     if (lane == 0) {
       S[j][j] = piv;
       rdiag[j] = rp;
@@ -315,18 +304,39 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   // update workers: warps 1-3 and 5-7 (warp 4 shares warp 0's sub-partition)
   const int uw = warp < 4 ? warp - 1 : warp - 2;  // 0..5 for the update warps
   const int ut = uw * 32 + lane;
-  for (int j = 0; j + 1 < kb; ++j) {
+  for (int j = 0; j < kb; ++j) {
     if (warp == 0) {
-      const double l = S[j + 1][j];
-      for (int r = j + 1 + lane; r < kb; r += 32) S[r][j + 1] -= S[r][j] * l;
-      __syncwarp();
-      pivot(j + 1);
+      if (j + 1 < kb) {
+        const double l = S[j + 1][j];
+        for (int r = j + 1 + lane; r < kb; r += 32) S[r][j + 1] -= S[r][j] * l;
+        __syncwarp();
+        pivot(j + 1);
+      }
     } else if (warp != 4) {
-      const int cnt = (62 - j) * (63 - j) / 2;  // entries with c >= j + 2
-      for (int e = ut; e < cnt; e += 192) {
-        const unsigned short pc = pairs[e];
-        const int r = pc & 0xFF, c = pc >> 8;
-        S[r][c] -= S[r][j] * S[c][j];
+      // factor step j: entries (r, c), c >= j + 2, of the fixed list
+      const int cf = j < NB - 2 ? (62 - j) * (63 - j) / 2 : 0;
+      // inverse step k = j - 1: entries (i, c), k < i < kb, c < k, row-major by i
+      const int k = j - 1;
+      const int ci = k >= 1 ? (kb - 1 - k) * k : 0;
+      const int magic = k >= 1 ? ((1 << 20) + k - 1) / k : 0;
+      for (int e = ut; e < cf + ci; e += 192) {
+        double *dst;
+        double a, b;
+        if (e < cf) {
+          const unsigned short pc = pairs[e];
+          const int r = pc & 0xFF, c = pc >> 8;
+          dst = &S[r][c];
+          a = -S[r][j];
+          b = S[c][j];
+        } else {
+          const int e2 = e - cf;
+          const int q = div_small(e2, k, magic);
+          const int c = e2 - q * k, i = k + 1 + q;
+          dst = &V[i][c];
+          a = V[i][k];
+          b = V[k][c];
+        }
+        *dst = fma(a, b, *dst);
       }
     }
     __syncthreads();
@@ -337,28 +347,14 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
     const int r = idx % kb, c = idx / kb;
     if (r >= c) A[r + c * lda] = S[r][c];
   }
-  // inverse, right-looking over the rows; Wsm holds the accumulators of rows not yet final
-  if (tid == 0) Wsm[0][0] = rdiag[0];
-  __syncthreads();
-  for (int r = 0; r + 1 < kb; ++r) {
-    const int w = r + 1;                 // columns c = 0..r of each updated row
-    const int cnt = (kb - 1 - r) * w;    // entries (r', c), r < r' < kb
-    const int magic = ((1 << 20) + w - 1) / w;
-    const double rdn = rdiag[r + 1];
-    for (int e = tid; e < cnt; e += 256) {
-      const int q = div_small(e, w, magic);
-      const int c = e - q * w, rr = r + 1 + q;
-      const double acc = fma(S[rr][r], Wsm[r][c], Wsm[rr][c]);
-      Wsm[rr][c] = (rr == r + 1) ? -acc * rdn : acc;
-    }
-    if (tid == 0) Wsm[r + 1][r + 1] = rdn;
-    __syncthreads();
-  }
   if (tid < NB) lg[tid] = tid < kb ? log(S[tid][tid]) : 0.0;
   __syncthreads();
+  // W = D^-1 V
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int r = idx % NB, c = idx / NB;
-    Winv[r + c * NB] = (r < kb && c <= r) ? Wsm[r][c] : 0.0;
+    double wv = 0.0;
+    if (r < kb && c <= r) wv = (r == c) ? rdiag[r] : rdiag[r] * V[r][c];
+    Winv[r + c * NB] = wv;
   }
   for (int st = NB / 2; st > 0; st >>= 1) {
     if (tid < st) lg[tid] += lg[tid + st];
