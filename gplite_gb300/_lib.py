@@ -23,11 +23,12 @@ OK, ENOT_PD, ENAN, EMAXITER, EUNSUPPORTED, EOOM, ETIMEOUT, ECUDA, EINVAL, ENOT_F
 CF_KIND = {"const": 0, "lin": 1, "sexp": 2, "matern32": 3, "matern52": 4, "nn": 5}
 LIK_KIND = {"gaussian": 0, "bernoulli": 1, "binomial": 2, "poisson": 3, "betabinom": 4}
 LINK = {"identity": 0, "logit": 1, "probit": 2, "log": 3}
-METHOD = {"full": 0, "fitc": 1}
+METHOD = {"full": 0, "fitc": 1, "rf": 2, "rbf": 3}
 APPROX = {"laplace": 0, "ep": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
 PHASES = ["cov", "potrf", "solve", "trtri", "lauum", "grad", "pred_mean", "pred_var"]
-FIELD = {"alpha": 0, "fmean": 1, "z": 2, "V": 3, "fvar": 4, "cavity_mean": 5, "cavity_var": 6}
+FIELD = {"alpha": 0, "fmean": 1, "z": 2, "V": 3, "fvar": 4, "cavity_mean": 5, "cavity_var": 6, "wmean": 7,
+         "wcov": 8}
 
 
 class CfTerm(C.Structure):
@@ -47,7 +48,8 @@ class Lik(C.Structure):
 
 
 class Method(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("num_inducing", C.c_int32), ("inducing", C.c_void_p)]
+    _fields_ = [("kind", C.c_int32), ("num_inducing", C.c_int32), ("inducing", C.c_void_p),
+                ("num_basis", C.c_int32 * MAX_TERMS), ("draws", C.c_void_p * MAX_TERMS)]
 
 
 class Approx(C.Structure):
@@ -134,6 +136,9 @@ SIGNATURES = {
     "gpgp_pred_cov": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, C.c_double, _P, _P]),
     "gpgp_kmeans": (C.c_int, [_P, _P, C.c_int64, C.c_int32, C.c_int32, _P, C.c_int32, _P, _P, _P]),
     "gpgp_mvn_draw": (C.c_int, [_P, _P, _P, C.c_int64, _P, C.c_int64, _P]),
+    "gpgp_rf_prior": (C.c_int, [_P, C.POINTER(Kernel), C.POINTER(Method), _P, C.c_int64, C.c_int32, C.c_uint32,
+                                _P, _P, C.c_int64, _P]),
+    "gpgp_rf_draw": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, C.c_int64, _P]),
     "gpgp_batch_create": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.POINTER(_P)]),
     "gpgp_batch_upload": (C.c_int, [_P, _P]),
     "gpgp_batch_run": (C.c_int, [_P]),

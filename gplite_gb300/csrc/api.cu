@@ -563,7 +563,7 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
     return fail(ctx, GPGP_EINVAL, "trials must be provided for the binomial and beta binomial likelihoods");
   if (lik->kind == GPGP_LIK_BETABINOM && !(lik->phi > 0))
     return fail(ctx, GPGP_EINVAL, "lik_betabinom needs phi > 0");
-  if (method->kind != GPGP_METHOD_FULL && method->kind != GPGP_METHOD_FITC)
+  if (method->kind < GPGP_METHOD_FULL || method->kind > GPGP_METHOD_RBF)
     return fail(ctx, GPGP_EINVAL, "unknown method");
   if (opts->precision != GPGP_PREC_FP64 && opts->precision != GPGP_PREC_MIXED)
     return fail(ctx, GPGP_EINVAL, "unknown precision");
@@ -613,10 +613,23 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   }
   m->F.alloc(s, (size_t)n * std::max(1, m->dk.nfeat));
   prep_features(s, m->dk, m->prep, m->x.p, n, n, m->F.p, n);
-  if (method->kind == GPGP_METHOD_FITC)
+  if (method->kind == GPGP_METHOD_RF || method->kind == GPGP_METHOD_RBF) {
+    // feature map of the reference's rf_featmap / rbf_featmap with the caller's draws
+    m->rf.reset(new RfState());
+    std::vector<double> hd;
+    st = build_rf_spec(k, method, m->dk, &m->rf->spec, &hd, &err);
+    if (st != GPGP_OK) return fail(ctx, st, err);
+    m->rf->dr.alloc(s, std::max<size_t>(1, hd.size()));
+    if (!hd.empty())
+      GPGP_CUDA(cudaMemcpyAsync(m->rf->dr.p, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    // the caller's draws arrays may go once this call returns
+    GPGP_CUDA(cudaStreamSynchronize(s));
+    st = fit_rf(m.get(), result);
+  } else if (method->kind == GPGP_METHOD_FITC) {
     st = fit_fitc(m.get(), result, method->inducing, on_device);
-  else
+  } else {
     st = fit_full(m.get(), result);
+  }
   if (st != GPGP_OK) {
     GPGP_CUDA(cudaStreamSynchronize(s));
     return st;
@@ -718,7 +731,9 @@ gpgp_status gpgp_profile_enable(gpgp_ctx *ctx, int32_t on) {
       ctx->prof_calls[i] = 0;
     }
     ctx->kt.reset();
+    if (on < 0 || on > 2) return fail(ctx, GPGP_EINVAL, "gpgp_profile_enable: on must be 0, 1 or 2");
     ctx->prof = on != 0;
+    ctx->prof_kernels = on == 1;
     return GPGP_OK;
   });
 }
@@ -900,6 +915,17 @@ gpgp_status gpgp_model_get(gpgp_model *m, int32_t field, double *out) {
   if (!m || !out) return GPGP_EINVAL;
   return guarded(m->ctx, [&]() -> gpgp_status {
     const double *src = nullptr;
+    size_t count = m->n;
+    if (field == GPGP_FIELD_WMEAN || field == GPGP_FIELD_WCOV) {
+      if (!m->rf || !m->fitted) return fail(m->ctx, GPGP_EINVAL, "field not available for this model");
+      const size_t D = m->rf->spec.D;
+      src = field == GPGP_FIELD_WMEAN ? m->rf->wmean.p : m->rf->wcov.p;
+      count = field == GPGP_FIELD_WMEAN ? D : D * D;
+      GPGP_CUDA(cudaSetDevice(m->ctx->device));
+      GPGP_CUDA(cudaMemcpyAsync(out, src, count * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+      GPGP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+      return GPGP_OK;
+    }
     switch (field) {
       case GPGP_FIELD_ALPHA: src = m->alpha.p; break;
       case GPGP_FIELD_FMEAN: src = m->fmean.p; break;
@@ -941,12 +967,13 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       dmean.alloc(s, mt);
       mout = dmean.p;
     }
-    if (m->fitc) {
+    if (m->fitc || m->rf) {
       DBuf dv;
       if (var) dv.alloc(s, mt);
       {
         Phase ph(ctx, GPGP_PHASE_PRED_VAR);
-        gpgp_status st2 = pred_fitc(m, Ft.p, mt, gm, mout, var ? dv.p : nullptr);
+        gpgp_status st2 = m->rf ? pred_rf(m, Ft.p, mt, gm, mout, var ? dv.p : nullptr)
+                                : pred_fitc(m, Ft.p, mt, gm, mout, var ? dv.p : nullptr);
         if (st2 != GPGP_OK) return st2;
       }
       if (var)
@@ -1048,6 +1075,15 @@ static gpgp_status loo_impl(gpgp_model *m, int32_t quad_order, int64_t draws, co
       lvar.alloc(s, n);
       gpgp_status st2 = loo_fitc_posteriors(m, lmean.p, lvar.p);
       if (st2 != GPGP_OK) return st2;
+      mp = lmean.p;
+      vp = lvar.p;
+    } else if (m->rf) {
+      // post_var = diag(Z wcov Z^T) at the training inputs (R/gp_loo.R:124, R/gp_pred.R:298-314)
+      lmean.alloc(s, n);
+      lvar.alloc(s, n);
+      rf_train_var(m, lvar.p);
+      loo_from_pv_kernel<<<g1(n), 256, 0, s>>>(n, m->fmean.p, m->z.p, m->V.p, lmean.p, lvar.p);
+      GPGP_CHECK_LAUNCH();
       mp = lmean.p;
       vp = lvar.p;
     } else if (m->nlc) {

@@ -49,6 +49,10 @@ gpgp_status gpgp_pred_cov(gpgp_model *m, const double *xt, int64_t mt, uint32_t 
   if (!m->fitted) return fail(m->ctx, GPGP_ENOT_FITTED, "model is not fitted");
   if (m->nlc || m->improper)
     return fail(m->ctx, GPGP_EUNSUPPORTED, "predictive covariance of a non-log-concave fit is not available");
+  if (m->rf)
+    return fail(m->ctx, GPGP_EUNSUPPORTED,
+                "method_rf / method_rbf have no predictive covariance (gp_pred_post.method_rf has no cov); "
+                "draw in weight space with gpgp_rf_draw");
   gpgp_ctx *ctx = m->ctx;
   return guarded(ctx, [&]() -> gpgp_status {
     GPGP_CUDA(cudaSetDevice(ctx->device));

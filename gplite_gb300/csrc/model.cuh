@@ -17,6 +17,7 @@ struct gpgp_ctx {
   double *h_pinned = nullptr;  // host pinned scalars
   // live profiling: (phase, start event, stop event) per recorded interval
   bool prof = false;
+  bool prof_kernels = false;  // per-launch timers as well (single-stream Cholesky)
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
   double prof_ms[GPGP_NPHASE] = {0};
   int64_t prof_calls[GPGP_NPHASE] = {0};
@@ -135,6 +136,37 @@ struct NlcState {
   DBuf Fg, Fb;          // features of the good / bad training rows, filled on first prediction
 };
 
+// One term of a random-feature map (rf.cu).
+enum RfKind { RF_CONST = 0, RF_LIN = 1, RF_SEXP = 2, RF_NN = 3, RBF_SEXP = 4 };
+struct RfTerm {
+  int kind;      // RfKind
+  int group;     // the cf (group) whose features this term multiplies into
+  int off;       // first input column of the term in the feature matrix F
+  int q;         // input columns of the term
+  int nb;        // features of the group
+  int64_t doff;  // offset of the term's draws in the packed draws array
+  double magn, lscale, sigma0, sigma;
+};
+struct RfSpec {
+  int nterms = 0, ngroups = 0, D = 0;
+  int gcol0[GPGP_MAX_TERMS + 1];  // first column of each group in the feature matrix; [ngroups] = D
+  RfTerm t[GPGP_MAX_TERMS];
+};
+// Host side: the feature map of (kernel, method) from the method's draws; packs
+// the draws into *draws. Errors as the reference's feature-map constructors.
+gpgp_status build_rf_spec(const gpgp_kernel *k, const gpgp_method *me, const DevKernel &dk, RfSpec *sp,
+                          std::vector<double> *draws, std::string *err);
+
+// Resident quantities of a method_rf / method_rbf fit (R/laplace.R:241-262).
+struct RfState {
+  RfSpec spec;
+  DBuf dr;               // packed draws
+  DBuf Z;                // features of the training inputs, n x D
+  DBuf L, Wblk;          // factor of Z^T diag(1/V) Z + I and its diagonal-block inverses
+  DBuf W;                // L^-1 (strict upper zero)
+  DBuf wmean, wcov;      // weight posterior
+};
+
 }  // namespace gpgp
 
 struct gpgp_model {
@@ -161,6 +193,7 @@ struct gpgp_model {
   gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
   std::unique_ptr<gpgp::FitcState> fitc;
   std::unique_ptr<gpgp::NlcState> nlc;  // set when the last iteration was non-log-concave
+  std::unique_ptr<gpgp::RfState> rf;    // method_rf / method_rbf
   bool improper = false;  // the reference's -Inf fit without a posterior (chol(A) failed)
   bool has_trials = false, has_offset = false;
   double log_evidence = 0.0;
@@ -181,7 +214,7 @@ inline gpgp_status fail(gpgp_ctx *ctx, gpgp_status st, const std::string &msg) {
 // binds the context's kernel timer to this thread for one API call
 struct KTBind {
   KernelTimer *prev;
-  explicit KTBind(gpgp_ctx *ctx) : prev(tl_kt) { tl_kt = (ctx && ctx->prof) ? &ctx->kt : nullptr; }
+  explicit KTBind(gpgp_ctx *ctx) : prev(tl_kt) { tl_kt = (ctx && ctx->prof && ctx->prof_kernels) ? &ctx->kt : nullptr; }
   ~KTBind() { tl_kt = prev; }
 };
 
@@ -231,6 +264,12 @@ gpgp_status pred_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, 
 gpgp_status loo_fitc_posteriors(gpgp_model *m, double *lmean, double *lvar);
 gpgp_status pred_cov_fitc(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double jitter, double *mean,
                           double *C);
+
+// method_rf / method_rbf (rf.cu): fit, predictive mean / variance at test features
+// Ft (mt rows), posterior variances at the training inputs (LOO).
+gpgp_status fit_rf(gpgp_model *m, gpgp_fit_result *res);
+gpgp_status pred_rf(gpgp_model *m, const double *Ft, int64_t mt, uint32_t gm, double *mean, double *var);
+void rf_train_var(gpgp_model *m, double *var);
 
 // Non-log-concave branch of a method_full Laplace / EP iteration (nlc.cu).
 gpgp_status nlc_fit_full(gpgp_model *m, const double *K, const double *logC, bool ep, double *alpha, double *fnew,

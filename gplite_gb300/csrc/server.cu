@@ -428,6 +428,8 @@ gpgp_status gpgp_server_submit(gpgp_server *s, const gpgp_request *q, int64_t *i
     r->k = *q->kernel;
     r->lik = *q->lik;
     if (q->method) {
+      // the server keeps copies of full and FITC requests only (no random-feature draws)
+      if (q->method->kind != GPGP_METHOD_FULL && q->method->kind != GPGP_METHOD_FITC) return GPGP_EUNSUPPORTED;
       r->meth = *q->method;
     } else {
       r->meth.kind = GPGP_METHOD_FULL;

@@ -19,6 +19,8 @@ from . import _lib as L
 from .objects import (GRAD_SLOT, Cf, approx_ep, approx_laplace, cf_sexp, lik_gaussian,
                       method_full)
 
+RF_METHODS = ("rf", "rbf")
+
 JITTER_DEFAULT = 1e-6  # get_jitter (R/gp.R:276-281)
 
 
@@ -63,7 +65,96 @@ def gp_init(cfs=None, lik=None, method=None, approx=None) -> GP:
                          "gives exact results")
     if isinstance(cfs, Cf):
         cfs = [cfs]
+    if method.kind in RF_METHODS:
+        method.num_basis = check_num_basis(cfs, method.num_basis)  # R/gp.R:64-66
     return GP(list(cfs), lik, method, approx)
+
+
+def check_num_basis(cfs, num_basis, num_inputs=None):
+    """check_num_basis (R/gp.R:211-233): one count per covariance function; cf_const takes
+    1 feature and cf_lin its number of inputs (None while that is unknown, R's NA)."""
+    if num_basis is None:
+        return None
+    nb = [None if v is None else int(v) for v in np.atleast_1d(np.asarray(num_basis, dtype=object))]
+    if len(nb) == 1:
+        nb = nb * len(cfs)
+    if len(nb) != len(cfs):
+        raise ValueError("The length of num_basis must match to the number of covariance functions.")
+    for k, c in enumerate(cfs):
+        if c.kind == "const":
+            nb[k] = 1
+        elif c.kind == "lin":
+            nb[k] = len(c.vars) if c.vars is not None else num_inputs
+    return nb
+
+
+def _rf_term_inputs(c, d):
+    """Input columns a term's feature map reads: its vars (all d when unset), twice
+    that under cf_periodic (sin and cos, R/cf.R:659-674)."""
+    nv = len(c.vars) if c.vars is not None else d
+    return 2 * nv if c.kind == "periodic" else nv
+
+
+def _rf_draws(gp, d, x=None):
+    """The random draws of the feature maps (rf_featmap / rbf_featmap, R/cf.R:571-817), one
+    array per device term (None for cf_const / cf_lin) in the layout include/gpgp.h gives.
+    Every covariance function (and every factor of a product) starts from the method's seed,
+    as the reference calls set.seed(seed) in each feature-map constructor; numpy's generator
+    stands in for R's stream (the same shapes and distributions, other numbers). rbf centres
+    are training inputs sampled without replacement (R's sample(n, num_feat))."""
+    me = gp.method
+    nb = check_num_basis(gp.cfs, me.num_basis, d)
+    out = []
+    for g, c in _flat_terms(gp):
+        base = c.base if c.kind == "periodic" else c
+        q = _rf_term_inputs(c, d)
+        rng = np.random.default_rng(me.seed)
+        if base.kind in ("const", "lin"):
+            out.append(None)
+            continue
+        if base.kind in ("matern32", "matern52"):
+            raise ValueError("Random Fourier features for Matern kernels not implemented yet." if me.kind == "rf"
+                             else "RBF features are not available for Matern kernels")
+        if me.kind == "rf":
+            if base.kind == "sexp":
+                if nb[g] % 2 == 1:
+                    raise ValueError("number of features must be an even number.")
+                out.append(rng.standard_normal((nb[g] // 2) * q))  # matrix(rnorm(m q), nrow = q)
+            else:  # nn: w (q x m), then w0 (m)
+                w = rng.standard_normal(nb[g] * q)
+                out.append(np.concatenate([w, rng.standard_normal(nb[g])]))
+        else:
+            if base.kind != "sexp":
+                raise ValueError("RBF features are not available for cf_%s" % base.kind)
+            if x is None:
+                raise RuntimeError("Cannot compute RBF feature map when the x matrix is not known.")
+            xs = x if c.vars is None else x[:, c.vars]
+            if c.kind == "periodic":
+                w = 2 * math.pi / c.period
+                xs = np.hstack([np.sin(w * xs), np.cos(w * xs)])
+            if nb[g] > xs.shape[0]:
+                raise ValueError("cannot take a sample larger than the population when 'replace = FALSE'")
+            ind = rng.choice(xs.shape[0], nb[g], replace=False)
+            out.append(np.ascontiguousarray(xs[ind]).ravel())  # column j of q x nb = centre j
+    return nb, out
+
+
+def _method_struct(gp, d, x=None):
+    """The C method struct; for rf / rbf also the arrays its pointers refer to (kept by
+    the caller for the duration of the call)."""
+    me = L.Method()
+    me.kind = L.METHOD[gp.method.kind]
+    keep = []
+    if gp.method.kind in RF_METHODS:
+        nb, draws = _rf_draws(gp, d, x)
+        for g, v in enumerate(nb):
+            me.num_basis[g] = int(v)
+        for t, a in enumerate(draws):
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                keep.append(a)
+                me.draws[t] = a.ctypes.data
+    return me, keep
 
 
 # ----------------------------------------------------------------------------
@@ -267,8 +358,11 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     ctx = L.default_context(device)
     k = kernel_struct(gp.cfs, d)
     lk = _lik_struct(gp.lik)
-    me = L.Method()
-    me.kind = L.METHOD[gp.method.kind]
+    me, keep = _method_struct(gp, d, x)
+    if gp.method.kind in RF_METHODS:
+        gp.method.num_basis = check_num_basis(gp.cfs, gp.method.num_basis, d)  # R/gp_fit.R:128
+        if gp.approx.kind == "ep":
+            raise ValueError("approx_ep is not available for method_%s" % gp.method.kind)
     ind = None
     if gp.method.kind == "fitc":
         if gp.method.inducing is None:
@@ -325,9 +419,16 @@ def gp_energy(gp, include_prior=True):
 
 
 def model_field(gp, name):
-    """Copy a resident vector of the fit (alpha, fmean, z, V, fvar, cavity_mean, cavity_var)."""
+    """Copy a resident vector of the fit (alpha, fmean, z, V, fvar, cavity_mean, cavity_var;
+    wmean and wcov of a method_rf / method_rbf fit)."""
     if not _is_fitted(gp):
         raise RuntimeError("The GP must be fitted. Call gp_fit first.")
+    if name in ("wmean", "wcov"):
+        D = int(sum(gp.method.num_basis)) if gp.method.kind in RF_METHODS else 0
+        out = np.empty(D if name == "wmean" else (D, D), order="F")
+        st = L.load().gpgp_model_get(gp._model, L.FIELD[name], out.ctypes.data_as(C.c_void_p))
+        L.check(st, None)
+        return out
     out = np.empty(gp.fit["n"])
     st = L.load().gpgp_model_get(gp._model, L.FIELD[name], L.ptr(out))
     L.check(st, None)
@@ -369,6 +470,35 @@ def gp_energy_grad(gp, include_prior=True):
 # ----------------------------------------------------------------------------
 # prediction (R/gp_pred.R:88-156)
 # ----------------------------------------------------------------------------
+
+def _rf_selected(gp, cfind, d):
+    """Features of the selected covariance functions (get_weight_inds, R/gp.R:235-245)."""
+    nb = check_num_basis(gp.cfs, gp.method.num_basis, d)
+    sel = range(len(gp.cfs)) if cfind is None else [int(k) for k in np.atleast_1d(cfind)]
+    return int(sum(nb[k] for k in sel))
+
+
+def _rf_prior(gp, xnew, cfind, var=False, z=None):
+    """Prior variance and / or prior draws zt z of a method_rf / method_rbf model without
+    a fit (gp_pred_prior / gp_draw_prior.method_rf, R/gp_pred.R:186-200, R/gp_draw.R:87-103),
+    on the device. method_rbf needs the training inputs, which an unfitted model lacks."""
+    if gp.method.kind == "rbf" and gp.x is None:
+        raise RuntimeError("Cannot compute RBF feature map when the x matrix is not known.")
+    m, d = xnew.shape
+    k = kernel_struct(gp.cfs, d)
+    me, keep = _method_struct(gp, d, gp.x)
+    ctx = L.default_context()
+    v = np.empty(m) if var else None
+    draws = 0 if z is None else z.shape[1]
+    sample = None if z is None else np.empty((m, draws), order="F")
+    xf = L.fortran(xnew)
+    st = L.load().gpgp_rf_prior(ctx.h, C.byref(k), C.byref(me), L.ptr(xf), m, d, _group_mask(gp, cfind),
+                                L.ptr(v), None if z is None else z.ctypes.data_as(C.c_void_p), draws,
+                                None if sample is None else sample.ctypes.data_as(C.c_void_p))
+    L.check(st, ctx.h)
+    del keep
+    return v, sample
+
 
 def _group_mask(gp, cfind):
     if cfind is None:
@@ -414,7 +544,10 @@ def gp_pred(gp, xnew, var=False, quantiles=None, transform=False, cfind=None, ji
     if not _is_fitted(gp):
         # gp_pred_prior.method_full / method_fitc (R/gp_pred.R:142-184)
         pred = dict(mean=np.zeros(m))
-        if var:
+        if var and gp.method.kind in RF_METHODS:
+            # gp_pred_prior.method_rf (R/gp_pred.R:186-200): diag(zt zt^T)
+            pred["var"] = _rf_prior(gp, xnew, cfind, var=True)[0]
+        elif var:
             if gp.method.kind == "fitc" and gp.method.inducing is None:
                 raise RuntimeError("Inducing points not set yet.")
             if gp.method.kind == "fitc":
@@ -535,6 +668,19 @@ def gp_draw(gp, xnew, draws=None, transform=True, target=False, marginal=False, 
     m = xnew.shape[0]
     draws = 1 if draws is None else int(draws)
     rng = np.random.default_rng(seed)
+    if gp.method.kind in RF_METHODS:
+        # weight space (gp_draw_prior / gp_draw_analytic.method_rf, R/gp_draw.R:87-169):
+        # w = wmean + t(chol(wcov)) z (prior: w = z), sample = zt w
+        ks = _rf_selected(gp, cfind, xnew.shape[1])
+        z = np.asfortranarray(rng.standard_normal((ks, draws)))
+        if _is_fitted(gp):
+            sample = np.empty((m, draws), order="F")
+            st = L.load().gpgp_rf_draw(gp._model, L.ptr(L.fortran(xnew)), m, _group_mask(gp, cfind),
+                                       z.ctypes.data_as(C.c_void_p), draws, sample.ctypes.data_as(C.c_void_p))
+            L.check(st, None)
+        else:
+            sample = _rf_prior(gp, xnew, cfind, z=z)[1]
+        return _draw_out(gp, sample, offset, target, transform, rng, trials)
     z = np.asfortranarray(rng.standard_normal((m, draws)))
     if marginal and _is_fitted(gp):
         pred = gp_pred(gp, xnew, var=True, cfind=cfind)
@@ -546,6 +692,11 @@ def gp_draw(gp, xnew, draws=None, transform=True, target=False, marginal=False, 
         st = L.load().gpgp_mvn_draw(ctx.h, L.ptr(np.ascontiguousarray(mean)), cov.ctypes.data_as(C.c_void_p), m,
                                     z.ctypes.data_as(C.c_void_p), draws, sample.ctypes.data_as(C.c_void_p))
         L.check(st, ctx.h)
+    return _draw_out(gp, sample, offset, target, transform, rng, trials)
+
+
+def _draw_out(gp, sample, offset, target, transform, rng, trials):
+    """add_offset, then generate_target or get_response (R/gp_draw.R:66-71)."""
     if offset is not None:
         sample = sample + np.asarray(offset, dtype=np.float64).reshape(-1, 1)
     if target:

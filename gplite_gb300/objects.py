@@ -384,6 +384,18 @@ def method_fitc(inducing=None, num_inducing=100, bin_along=None, bin_count=10, s
                      bin_count=min(bin_count, num_inducing), seed=seed)
 
 
+def method_rf(num_basis=400, seed=12345):
+    """method_rf (R/method.R:129-133): random features (a linearised GP with num_basis
+    features per covariance function, drawn from the seed)."""
+    return MethodObj("rf", num_basis=num_basis, seed=seed)
+
+
+def method_rbf(num_basis=400, seed=12345):
+    """method_rbf (R/method.R:135-139): radial basis features centred at num_basis
+    training inputs drawn from the seed."""
+    return MethodObj("rbf", num_basis=num_basis, seed=seed)
+
+
 class ApproxObj:
     def __init__(self, kind, **kw):
         self.kind = kind

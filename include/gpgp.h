@@ -108,15 +108,35 @@ typedef struct gpgp_lik {
   double phi;   /* lik_betabinom over-dispersion */
 } gpgp_lik;
 
-typedef enum gpgp_method_kind { GPGP_METHOD_FULL = 0, GPGP_METHOD_FITC = 1 } gpgp_method_kind;
+typedef enum gpgp_method_kind {
+  GPGP_METHOD_FULL = 0,
+  GPGP_METHOD_FITC = 1,
+  GPGP_METHOD_RF = 2, /* random features (R/method.R:129-133) */
+  GPGP_METHOD_RBF = 3 /* radial basis features at training inputs (R/method.R:135-139) */
+} gpgp_method_kind;
 
-/* Method (R/method.R:105-125). For FITC the inducing inputs are given
+/* Method (R/method.R:105-139). For FITC the inducing inputs are given
  * explicitly (M-by-d column-major, host memory for gpgp_fit, device memory
- * for gpgp_fit_dev). */
+ * for gpgp_fit_dev).
+ * For method_rf / method_rbf the random draws of the reference's feature maps
+ * (rf_featmap / rbf_featmap, R/cf.R:532-817) are given explicitly, in host
+ * memory, per term (terms as in gpgp_kernel), with q the term's input count
+ * (nvars, or 2 nvars for cf_periodic) and nb = num_basis of its group:
+ *   rf, cf_sexp: q x nb/2 standard normals (column-major; R's `w` before the
+ *                scaling by 1/lscale), features [cos(h), sin(h)], h = x w;
+ *   rf, cf_nn:   q x nb standard normals, then nb more (R's `w` and `w0`
+ *                before their scaling by sigma and sigma0 sigma);
+ *   rbf, cf_sexp: q x nb centres (column j = centre j, in the term's input
+ *                space: the raw training inputs of its columns, or their
+ *                sin/cos transform under cf_periodic);
+ *   cf_const, cf_lin: none (NULL); their groups take 1 and nvars features.
+ * cf_matern32/52 have no feature map (an error in the reference too). */
 typedef struct gpgp_method {
   int32_t kind;
   int32_t num_inducing;
   const double *inducing;
+  int32_t num_basis[GPGP_MAX_TERMS];    /* features per group (rf / rbf) */
+  const double *draws[GPGP_MAX_TERMS];  /* per term (rf / rbf), see above */
 } gpgp_method;
 
 typedef enum gpgp_approx_kind { GPGP_APPROX_LAPLACE = 0, GPGP_APPROX_EP = 1 } gpgp_approx_kind;
@@ -175,7 +195,10 @@ void *gpgp_stream(gpgp_ctx *ctx);
 
 /* ---- live profiling: CUDA events recorded on the context's stream around
  *      each phase of the hot path; read back as total milliseconds and
- *      call counts per phase. Enabling resets the accumulators. ----------- */
+ *      call counts per phase. Enabling resets the accumulators. on = 1 also
+ *      times every dense-contraction launch alone (below), which makes the
+ *      mixed Cholesky run on one stream; on = 2 times the phases only and
+ *      keeps the lookahead schedule. on = 0 stops profiling. -------------- */
 typedef enum gpgp_phase {
   GPGP_PHASE_COV = 0,      /* covariance matrix generation */
   GPGP_PHASE_POTRF = 1,    /* blocked Cholesky */
@@ -259,7 +282,9 @@ typedef enum gpgp_model_field {
   GPGP_FIELD_V = 3,
   GPGP_FIELD_FVAR = 4,        /* EP posterior marginal variances */
   GPGP_FIELD_CAVITY_MEAN = 5, /* EP */
-  GPGP_FIELD_CAVITY_VAR = 6   /* EP */
+  GPGP_FIELD_CAVITY_VAR = 6,  /* EP */
+  GPGP_FIELD_WMEAN = 7,       /* rf / rbf: posterior mean of the weights (D = sum of num_basis) */
+  GPGP_FIELD_WCOV = 8         /* rf / rbf: posterior covariance of the weights (D x D) */
 } gpgp_model_field;
 gpgp_status gpgp_model_get(gpgp_model *model, int32_t field, double *out);
 
@@ -284,6 +309,25 @@ gpgp_status gpgp_pred_cov(gpgp_model *model, const double *xt, int64_t m, uint32
  *      of R's chol in the reference). ---- */
 gpgp_status gpgp_mvn_draw(gpgp_ctx *ctx, const double *mean, const double *cov, int64_t d,
                           const double *z, int64_t draws, double *out);
+
+/* ---- random-feature methods without a fit: gp_pred_prior.method_rf
+ *      (R/gp_pred.R:186-200) and gp_draw_prior.method_rf (R/gp_draw.R:87-103).
+ *      The features zt (m x D_sel, the selected groups' columns) of xt
+ *      (m x d, host memory) are formed on the device from method's draws;
+ *      var (m, or NULL) = diag(zt zt^T); sample (m x draws, or NULL when
+ *      z is NULL) = zt z for caller-drawn standard normals z (D_sel x draws,
+ *      column-major). gpgp_pred / gpgp_loo / gpgp_model_get serve fitted
+ *      rf / rbf models; gpgp_model_grad and gpgp_pred_cov return
+ *      GPGP_EUNSUPPORTED for them, as the reference has neither. ---------- */
+gpgp_status gpgp_rf_prior(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_method *method,
+                          const double *xt, int64_t m, int32_t d, uint32_t group_mask, double *var,
+                          const double *z, int64_t draws, double *sample);
+/* ---- posterior draws of a fitted rf / rbf model in weight space:
+ *      gp_draw_analytic.method_rf (R/gp_draw.R:145-169),
+ *      sample = zt (wmean + t(chol(wcov)) z) over the selected groups, z
+ *      D_sel x draws standard normals (host, column-major), sample m x draws. */
+gpgp_status gpgp_rf_draw(gpgp_model *model, const double *xt, int64_t m, uint32_t group_mask,
+                         const double *z, int64_t draws, double *sample);
 
 /* ---- k-means of the inducing inputs: stats::kmeans in get_inducing
  *      (R/gp_fit.R:192-236). Lloyd's algorithm from the caller's initial

@@ -958,6 +958,235 @@ def ep_fitc(lik, Kz, Kz_chol, Kxz, K_diag, D, y, damping=0.9, damping_min=0.1, m
 
 
 # ----------------------------------------------------------------------------
+# random features: method_rf / method_rbf (R/method.R:129-139, R/cf.R:532-817,
+# R/laplace.R:241-266, 327-355, R/gp_pred.R:186-200, 298-318, R/gp_draw.R:87-169).
+# R draws the frequencies / centres after set.seed(seed) in every feature-map
+# constructor; numpy's default_rng(seed), restarted for every covariance function
+# (and every factor of a product), stands in for that stream here: the same
+# shapes, order and distributions, other numbers.
+# ----------------------------------------------------------------------------
+
+def check_num_basis(cfs, num_basis, num_inputs=None):
+    """check_num_basis (R/gp.R:211-233)."""
+    if num_basis is None:
+        return None
+    nb = list(np.atleast_1d(np.asarray(num_basis, dtype=object)))
+    if len(nb) == 1:
+        nb = nb * len(cfs)
+    if len(nb) != len(cfs):
+        raise ValueError("The length of num_basis must match to the number of covariance functions.")
+    for k, c in enumerate(cfs):
+        if c.kind == "const":
+            nb[k] = 1
+        elif c.kind == "lin":
+            nb[k] = len(c.vars) if c.vars is not None else num_inputs
+    return nb
+
+
+def _n_inputs(cf, num_inputs):
+    return len(cf.vars) if cf.vars is not None else num_inputs
+
+
+def rf_featmap(cf, num_feat, num_inputs, seed):
+    """rf_featmap.cf_* (R/cf.R:553-695)."""
+    if cf.kind == "const":
+        return lambda x: cf.magn * np.ones((as_matrix(x).shape[0], 1))
+    if cf.kind == "lin":
+        return lambda x: cf.magn * prepare_inputmat(cf, x)
+    if cf.kind in ("matern32", "matern52"):
+        raise ValueError("Random Fourier features for Matern kernels not implemented yet.")
+    if cf.kind == "sexp":
+        q = _n_inputs(cf, num_inputs)
+        if num_feat % 2 == 1:
+            raise ValueError("number of features must be an even number.")
+        m = num_feat // 2
+        scale = 1 / cf.lscale
+        w = np.random.default_rng(seed).standard_normal(m * q).reshape(m, q).T * scale
+
+        def fm(x):
+            h = prepare_inputmat(cf, x) @ w
+            return cf.magn * math.sqrt(1 / m) * np.hstack([np.cos(h), np.sin(h)])
+        return fm
+    if cf.kind == "nn":
+        q = _n_inputs(cf, num_inputs)
+        m = num_feat
+        rng = np.random.default_rng(seed)
+        w = rng.standard_normal(m * q).reshape(m, q).T * cf.sigma
+        w0 = rng.standard_normal(m).reshape(1, m) * cf.sigma0 * cf.sigma
+        w_aug = np.vstack([w0, w])
+
+        def fm(x):
+            x = prepare_inputmat(cf, x)
+            x_aug = np.hstack([np.ones((x.shape[0], 1)), x])
+            return cf.magn / math.sqrt(m) * sps.erf(x_aug @ w_aug)
+        return fm
+    if cf.kind == "periodic":
+        q = _n_inputs(cf, num_inputs)
+        base = rf_featmap(cf.base, num_feat, 2 * q, seed)
+
+        def fm(x):
+            x = prepare_inputmat(cf, x)
+            w = 2 * math.pi / cf.period
+            return base(np.hstack([np.sin(w * x), np.cos(w * x)]))
+        return fm
+    if cf.kind == "prod":
+        if any(c.kind in ("const", "lin") for c in cf.cfs):
+            raise ValueError("Random features for product kernel containing constant or linear kernel "
+                             "not implemented yet.")
+        maps = [rf_featmap(c, num_feat, num_inputs, seed) for c in cf.cfs]
+
+        def fm(x):
+            z = 1
+            for mp in maps:
+                z = z * mp(x)
+            return z
+        return fm
+    raise ValueError(cf.kind)
+
+
+def rbf_featmap(cf, num_feat, num_inputs, x, seed):
+    """rbf_featmap.cf_* (R/cf.R:722-817). Centres are training inputs sampled without
+    replacement (R's sample(n, num_feat)) from the columns the term uses."""
+    if cf.kind in ("const", "lin"):
+        return rf_featmap(cf, num_feat, num_inputs, seed)
+    if cf.kind == "sexp":
+        if x is None:
+            raise ValueError("Cannot get RBF featuremap if inputs are not given.")
+        xs = as_matrix(x)
+        if cf.vars is not None:
+            xs = xs[:, list(cf.vars)]
+        ind = np.random.default_rng(seed).choice(xs.shape[0], num_feat, replace=False)
+        centers = xs[ind]
+
+        def fm(xx):
+            xx = prepare_inputmat(cf, xx)
+            z = np.empty((xx.shape[0], num_feat))
+            for j in range(num_feat):
+                z[:, j] = np.exp(-((xx - centers[j]) ** 2).sum(1) / cf.lscale ** 2)
+            return cf.magn * math.sqrt(1 / num_feat) * z
+        return fm
+    if cf.kind == "periodic":
+        q = _n_inputs(cf, num_inputs)
+        xs = as_matrix(x)
+        if cf.vars is not None:
+            xs = xs[:, list(cf.vars)]
+        w = 2 * math.pi / cf.period
+        base = rbf_featmap(cf.base, num_feat, 2 * q, np.hstack([np.sin(w * xs), np.cos(w * xs)]), seed)
+
+        def fm(xx):
+            xx = prepare_inputmat(cf, xx)
+            return base(np.hstack([np.sin(w * xx), np.cos(w * xx)]))
+        return fm
+    if cf.kind == "prod":
+        if any(c.kind in ("const", "lin") for c in cf.cfs):
+            raise ValueError("RBF features for product kernel containing constant or linear kernel "
+                             "not implemented yet.")
+        maps = [rbf_featmap(c, num_feat, num_inputs, x, seed) for c in cf.cfs]
+
+        def fm(xx):
+            z = 1
+            for mp in maps:
+                z = z * mp(xx)
+            return z
+        return fm
+    raise ValueError("no RBF feature map for cf_%s" % cf.kind)
+
+
+def get_featuremap(gp, num_inputs):
+    """get_featuremap.gp + rf_featmap.list / rbf_featmap.list (R/gp.R:171-189,
+    R/cf.R:534-551, 703-720): the features of the selected cfs, side by side."""
+    me = gp.method
+    nb = check_num_basis(gp.cfs, me.num_basis, num_inputs)
+    if me.kind == "rf":
+        maps = [rf_featmap(c, nb[k], num_inputs, me.seed) for k, c in enumerate(gp.cfs)]
+    else:
+        if getattr(gp, "x", None) is None:
+            raise ValueError("Cannot compute RBF feature map when the x matrix is not known.")
+        maps = [rbf_featmap(c, nb[k], num_inputs, gp.x, me.seed) for k, c in enumerate(gp.cfs)]
+
+    def featuremap(x, cfind=None):
+        idx = range(len(maps)) if cfind is None else cfind
+        return np.hstack([maps[k](x) for k in idx])
+    return featuremap
+
+
+def get_weight_inds(gp, cfind=None):
+    """get_weight_inds (R/gp.R:235-245), 0-based."""
+    ends = np.concatenate([[0], np.cumsum(gp.method.num_basis)]).astype(int)
+    idx = range(len(gp.cfs)) if cfind is None else cfind
+    return np.concatenate([np.arange(ends[k], ends[k + 1]) for k in idx])
+
+
+def laplace_iter_rf(lik, Z, y, fhat_old, trials=None, offset=None):
+    """laplace_iter.method_rf (R/laplace.R:241-262)."""
+    z, V = get_pseudodata_la(lik, fhat_old, y, trials, offset)
+    n = len(z)
+    d = Z.shape[1]
+    H = Z.T @ (Z / V[:, None])
+    L = np.linalg.cholesky(H + np.eye(d))
+    what = _bwd_t(L, _fwd(L, Z.T @ (z / V)))
+    wcov = sla.solve_triangular(L, sla.solve_triangular(L, np.eye(d), lower=True), lower=True, trans="T")
+    wcov_logdet = -2 * np.sum(np.log(np.diag(L)))
+    fhat_new = Z @ what
+    log_prior = -0.5 * d * math.log(2 * math.pi) - 0.5 * np.sum(what ** 2)
+    log_lik = get_loglik(lik, fhat_new, y, trials, offset)
+    log_evidence = 0.5 * n * math.log(2 * math.pi) + 0.5 * wcov_logdet + log_prior + log_lik
+    return dict(fmean=fhat_new, wmean=what, wcov=wcov, z=z, V=V, log_evidence=log_evidence)
+
+
+def laplace_rf(lik, Z, y, maxiter=100, tol=1e-4, trials=None, offset=None):
+    """laplace.method_rf (R/laplace.R:327-351)."""
+    n = len(y)
+    fhat = np.zeros(n)
+    if lik.kind == "gaussian":
+        maxiter = 1
+    for it in range(1, maxiter + 1):
+        fit = laplace_iter_rf(lik, Z, y, fhat, trials, offset)
+        fhat_new = Z @ fit["wmean"]
+        diff = np.max(np.abs(fhat - fhat_new))
+        fhat = fhat_new
+        if diff < tol:
+            break
+    if maxiter > 1 and it == maxiter:
+        warnings.warn("Maximum number of iterations in Laplace reached, max delta f = %g" % diff)
+    fit["iters"] = it
+    return fit
+
+
+def gp_pred_post_rf(gp, xt, var=False, cfind=None):
+    """gp_pred_post.method_rf (R/gp_pred.R:298-314)."""
+    zt = get_featuremap(gp, xt.shape[1])(xt, cfind)
+    inds = get_weight_inds(gp, cfind)
+    pred = dict(mean=zt @ gp.fit["wmean"][inds])
+    if var:
+        wcov = gp.fit["wcov"][np.ix_(inds, inds)]
+        pred["var"] = np.einsum("ij,jk,ik->i", zt, wcov, zt)
+    return pred
+
+
+def gp_draw_rf(gp, xt, z, cfind=None):
+    """gp_draw_prior / gp_draw_analytic.method_rf (R/gp_draw.R:87-103, 145-163) with the
+    standard normals z (features x draws) given: zt w, w = z (prior) or
+    wmean + t(chol(wcov)) z (posterior, mvnrnd R/gp_draw.R:182-188)."""
+    xt = as_matrix(xt)
+    zt = get_featuremap(gp, xt.shape[1])(xt, cfind)
+    if getattr(gp, "fit", None) is None:
+        return zt @ z
+    inds = get_weight_inds(gp, cfind)
+    wmean = gp.fit["wmean"][inds]
+    wcov = gp.fit["wcov"][np.ix_(inds, inds)]
+    return zt @ (wmean[:, None] + np.linalg.cholesky(wcov) @ z)
+
+
+def method_rf(num_basis=400, seed=12345):
+    return SimpleNamespace(kind="rf", num_basis=num_basis, seed=seed)
+
+
+def method_rbf(num_basis=400, seed=12345):
+    return SimpleNamespace(kind="rbf", num_basis=num_basis, seed=seed)
+
+
+# ----------------------------------------------------------------------------
 # gp_fit / gp_energy / gp_pred / gp_loo (R/gp_fit.R:54-188, R/gp.R:138-147,
 # R/gp_pred.R:88-296, R/gp_loo.R:73-133)
 # ----------------------------------------------------------------------------
@@ -992,6 +1221,14 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, threads=1):
                               maxiter=ap.maxiter, quad_order=ap.quad_order, trials=trials, offset=offset)
         except np.linalg.LinAlgError:
             fit = dict(log_evidence=-np.inf)
+    elif me.kind in ("rf", "rbf"):
+        # fit_laplace.method_rf / method_rbf (R/gp_fit.R:125-141)
+        if ap.kind != "laplace":
+            raise ValueError("approx_ep is not available for method_%s" % me.kind)
+        gp.x = x
+        featuremap = get_featuremap(gp, x.shape[1])
+        me.num_basis = check_num_basis(gp.cfs, me.num_basis, x.shape[1])
+        fit = laplace_rf(gp.lik, featuremap(x), y, ap.maxiter, ap.tol, trials, offset)
     else:
         raise ValueError(me.kind)
     gp.x = x
@@ -1273,13 +1510,18 @@ def gp_pred(gp, xnew, var=False, quantiles=None, transform=False, cfind=None, qu
     if getattr(gp, "fit", None) is None:
         mean = np.zeros(xnew.shape[0])
         pred = dict(mean=mean)
-        if var:
+        if var and gp.method.kind in ("rf", "rbf"):
+            zt = get_featuremap(gp, xnew.shape[1])(xnew, cfind)  # R/gp_pred.R:186-200
+            pred["var"] = (zt * zt).sum(1)
+        elif var:
             pred["var"] = eval_cf(gp.cfs, xnew, xnew, cfind, diag_only=True)
     else:
         if not gp.fitted:
             raise RuntimeError("The GP object seems to contain a posterior fit, but is not refitted")
         if gp.method.kind == "full":
             pred = gp_pred_post_full(gp, xnew, var, cfind)
+        elif gp.method.kind in ("rf", "rbf"):
+            pred = gp_pred_post_rf(gp, xnew, var, cfind)
         else:
             pred = gp_pred_post_fitc(gp, xnew, var, False, cfind)
     pred["mean"] = add_offset(pred["mean"], offset)
@@ -1308,6 +1550,8 @@ def loo_posteriors(gp, x):
     grad = (z - fhat) / V
     if gp.method.kind == "full":
         pv = gp_pred_post_full(gp, as_matrix(x), var=True)["var"]
+    elif gp.method.kind in ("rf", "rbf"):
+        pv = gp_pred_post_rf(gp, as_matrix(x), var=True)["var"]
     else:
         pv = gp_pred_post_fitc(gp, as_matrix(x), var=True, train=True)["var"]
     loo_var = 1 / (1 / pv - 1 / V)
@@ -1403,5 +1647,8 @@ def gp_init(cfs, lik_, method=None, approx=None):
     approx = approx or approx_laplace()
     if approx.kind == "ep" and lik_.kind == "gaussian":
         raise ValueError("approx_ep disabled for lik_gaussian")
-    return SimpleNamespace(cfs=list(cfs), lik=lik_, method=method or method_full(), approx=approx,
+    method = method or method_full()
+    if method.kind in ("rf", "rbf"):
+        method.num_basis = check_num_basis(cfs, method.num_basis)  # R/gp.R:64-66
+    return SimpleNamespace(cfs=list(cfs), lik=lik_, method=method, approx=approx,
                            fitted=False, fit=None, x=None)

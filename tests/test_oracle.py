@@ -279,3 +279,38 @@ def test_nonlogconcave_split_is_consistent(approx):
     assert abs(gf.fit["log_evidence"] - f["log_evidence"]) < 1e-3 * abs(f["log_evidence"])
     pr = R.gp_pred(gp, np.linspace(-3, 3, 9), var=True)
     assert np.all(pr["var"] > 0)
+
+
+@pytest.mark.parametrize("kind", ["sexp", "nn", "periodic"])
+def test_rf_featmap_approximates_the_kernel(kind):
+    """The random-feature maps (rf_featmap, R/cf.R:571-674) are Monte Carlo
+    approximations of their kernels: z(x)^T z(x') -> k(x, x') as the number of
+    features grows (error ~ 1/sqrt(num_feat)). (The reference's product map,
+    R/cf.R:676-695, multiplies the factors' features elementwise with every factor
+    drawn from the same seed, which is not such an approximation; it is restated as
+    it stands and checked against the device only.)"""
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1.5, 1.5, (60, 2))
+    cf = {"sexp": lambda: R.cf("sexp", lscale=0.7, magn=1.3),
+          "nn": lambda: R.cf("nn", sigma0=0.8, sigma=1.4, magn=0.9),
+          "periodic": lambda: R.cf_periodic(period=2.0)}[kind]()
+    K = R.eval_cf([cf], x, x)
+    errs = []
+    for nf in (400, 40000):
+        Z = R.rf_featmap(cf, nf, 2, seed=3)(x)
+        errs.append(np.max(np.abs(Z @ Z.T - K)) / np.max(np.abs(K)))
+    assert errs[1] < 0.05 and errs[1] < errs[0]
+
+
+def test_rf_laplace_matches_exact_linear_model():
+    """laplace_iter.method_rf with lik_gaussian is the exact Bayesian linear model in
+    the features: wmean = (Z^T Z / s2 + I)^-1 Z^T y / s2 and wcov its inverse precision."""
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-2, 2, (80, 1))
+    y = np.sin(2 * x[:, 0]) + 0.1 * rng.standard_normal(80)
+    gp = R.gp_init([R.cf("sexp", lscale=0.5)], R.lik("gaussian", sigma=0.3), method=R.method_rf(num_basis=30))
+    gp = R.gp_fit(gp, x, y)
+    Z = R.get_featuremap(gp, 1)(x)
+    P = Z.T @ Z / 0.09 + np.eye(30)
+    assert np.allclose(gp.fit["wmean"], np.linalg.solve(P, Z.T @ y / 0.09), rtol=1e-10, atol=1e-12)
+    assert np.allclose(gp.fit["wcov"], np.linalg.inv(P), rtol=1e-9, atol=1e-13)
