@@ -234,6 +234,11 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
 //    entry costs one FMA; the row scaling by 1 / L(i, i) happens once, on the
 //    way out.
 //  - log L_jj summed in a fixed tree order.
+// -x by flipping the sign bit (an integer instruction, not an FP64 one)
+__device__ __forceinline__ double neg_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
 __device__ __forceinline__ int div_small(int e, int d, int magic) {
   // e / d for e < 4096, 1 <= d <= 64, magic = ceil(2^20 / d): exact on that range
   return (int)(((unsigned)e * (unsigned)magic) >> 20);
@@ -260,7 +265,8 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   const int lane = tid & 31, warp = tid >> 5;
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int r = idx % NB, c = idx / NB;
-    S[r][c] = (r < kb && c < kb && r >= c) ? A[r + c * lda] : 0.0;
+    // held negated until its column is pivoted (see the update loop)
+    S[r][c] = (r < kb && c < kb && r >= c) ? neg_bits(A[r + c * lda]) : 0.0;
     V[r][c] = 0.0;
   }
   // entry e: u = 63 - c is the largest u with u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2
@@ -273,10 +279,16 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   }
   if (tid == 0) failed = 0;
   __syncthreads();
-  // pivot of column j by warp 0: L_jj, the scaled column below it and the first
-  // term of column j of V
-  auto pivot = [&](int j) {
-    const double dj = S[j][j];
+  // Warp 0 keeps the current scaled column in registers: lane l owns rows l and
+  // l + 32, and lreg[u] holds L(l + 32 u, j) once column j is pivoted. Rows below
+  // 32 drop out after column 31, so their FP64 work is skipped from then on (a
+  // warp instruction costs the same with one lane or 32).
+  double lreg[2] = {0.0, 0.0};
+  // pivot of column j by warp 0 from t[u] = -S(l + 32 u, j) after all updates:
+  // L_jj, the scaled column below it (stored positive, and kept in lreg) and the
+  // first term of column j of V
+  auto pivot = [&](int j, const double (&t)[2]) {
+    const double dj = neg_bits(__shfl_sync(0xffffffffu, j < 32 ? t[0] : t[1], j & 31));
     // not positive (sign bit or zero) or not finite, tested on the bits
     const long long djb = __double_as_longlong(dj);
     if (djb <= 0ll || (djb >> 52) >= 0x7FFll) {
@@ -287,18 +299,29 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
       return;
     }
     const double rp = rsqrt_fast(dj);
-    const double piv = dj * rp;
-    for (int r = j + 1 + lane; r < kb; r += 32) {
-      const double l = S[r][j] * rp;
-      S[r][j] = l;
-      V[r][j] = -(l * rp);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 || j < 31) {
+        const int r = lane + 32 * u;
+        if (r > j && r < kb) {
+          const double l = -(t[u] * rp);
+          S[r][j] = l;
+          V[r][j] = -(l * rp);
+          lreg[u] = l;
+        }
+      }
     }
-    if (lane == 0) {
-      S[j][j] = piv;
+    if (lane == (j & 31)) {
+      S[j][j] = dj * rp;
       rdiag[j] = rp;
     }
   };
-  if (warp == 0) pivot(0);
+  if (warp == 0) {
+    double t0[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) t0[u] = (lane + 32 * u < kb) ? S[lane + 32 * u][0] : 0.0;
+    pivot(0, t0);
+  }
   __syncthreads();
   if (failed) return;
   // update workers: warps 1-3 and 5-7 (warp 4 shares warp 0's sub-partition)
@@ -307,36 +330,45 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   for (int j = 0; j < kb; ++j) {
     if (warp == 0) {
       if (j + 1 < kb) {
-        const double l = S[j + 1][j];
-        for (int r = j + 1 + lane; r < kb; r += 32) S[r][j + 1] -= S[r][j] * l;
-        __syncwarp();
-        pivot(j + 1);
+        // column j + 1 takes its last update, from column j, then its pivot
+        const double l = __shfl_sync(0xffffffffu, (j + 1) < 32 ? lreg[0] : lreg[1], (j + 1) & 31);
+        double t[2] = {0.0, 0.0};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (u == 1 || j < 31) {
+            const int r = lane + 32 * u;
+            if (r > j && r < kb) t[u] = fma(lreg[u], l, S[r][j + 1]);
+          }
+        }
+        pivot(j + 1, t);
       }
     } else if (warp != 4) {
-      // factor step j: entries (r, c), c >= j + 2, of the fixed list
+      // factor step j: entries (r, c), c >= j + 2, of the fixed list; inverse step
+      // k = j - 1: entries (i, c), k < i < kb, c < k, row-major by i. Both are
+      // dst += a b with a, b >= sign-free operands (the trailing matrix is held
+      // negated), so that each entry is exactly one FP64 instruction.
       const int cf = j < NB - 2 ? (62 - j) * (63 - j) / 2 : 0;
-      // inverse step k = j - 1: entries (i, c), k < i < kb, c < k, row-major by i
       const int k = j - 1;
       const int ci = k >= 1 ? (kb - 1 - k) * k : 0;
       const int magic = k >= 1 ? ((1 << 20) + k - 1) / k : 0;
       for (int e = ut; e < cf + ci; e += 192) {
+        const double *pa, *pb;
         double *dst;
-        double a, b;
         if (e < cf) {
           const unsigned short pc = pairs[e];
           const int r = pc & 0xFF, c = pc >> 8;
           dst = &S[r][c];
-          a = -S[r][j];
-          b = S[c][j];
+          pa = &S[r][j];
+          pb = &S[c][j];
         } else {
           const int e2 = e - cf;
           const int q = div_small(e2, k, magic);
           const int c = e2 - q * k, i = k + 1 + q;
           dst = &V[i][c];
-          a = V[i][k];
-          b = V[k][c];
+          pa = &V[i][k];
+          pb = &V[k][c];
         }
-        *dst = fma(a, b, *dst);
+        *dst = fma(*pa, *pb, *dst);
       }
     }
     __syncthreads();

@@ -4,7 +4,9 @@ R/laplace.R:241-266, 327-355, R/gp_pred.R:186-200, 298-318, R/gp_draw.R:87-169).
 
 Both sides draw the frequencies / centres from numpy's generator seeded with the
 method's seed, in the reference's shapes and order, so the feature maps agree.
-Tolerances: 1e-10 relative on the evidence; 1e-9 of the largest entry for latent
+Tolerances: 1e-10 relative on the evidence, relative to max(|evidence|, n) (the
+reference's expression adds n/2 log(2 pi) to terms of similar size, so the evidence
+can be much smaller than its terms); 1e-9 of the largest entry for latent
 means, weights, predictions and draws (the features pass through cos / sin / erf /
 exp, whose device and libm values differ by an ulp, and the Gram matrix sums n of
 them)."""
@@ -68,7 +70,7 @@ def test_rf_fit_pred_loo_draw_match_oracle(cf, lik):
     xt = np.random.default_rng(9).uniform(-2.5, 2.5, (37, 2))
     gp, og = fit_both(CFS[cf](), lik, G.method_rf(num_basis=24), x, y)
     assert gp.fit["iters"] == og.fit["iters"]
-    assert abs(gp.fit["log_evidence"] - og.fit["log_evidence"]) <= 1e-10 * abs(og.fit["log_evidence"])
+    assert abs(gp.fit["log_evidence"] - og.fit["log_evidence"]) <= 1e-10 * max(abs(og.fit["log_evidence"]), len(y))
     assert relmax(G.model_field(gp, "fmean"), og.fit["fmean"]) < 1e-9
     assert relmax(G.model_field(gp, "wmean"), og.fit["wmean"]) < 1e-9
     assert relmax(G.model_field(gp, "wcov"), og.fit["wcov"]) < 1e-9
@@ -90,7 +92,7 @@ def test_rbf_fit_pred_match_oracle(cf):
     xt = np.random.default_rng(9).uniform(-2.5, 2.5, (29, 2))
     gp, og = fit_both(CFS[cf](), "poisson", G.method_rbf(num_basis=20), x, y)
     assert gp.fit["iters"] == og.fit["iters"]
-    assert abs(gp.fit["log_evidence"] - og.fit["log_evidence"]) <= 1e-10 * abs(og.fit["log_evidence"])
+    assert abs(gp.fit["log_evidence"] - og.fit["log_evidence"]) <= 1e-10 * max(abs(og.fit["log_evidence"]), len(y))
     p, po = G.gp_pred(gp, xt, var=True), R.gp_pred(og, xt, var=True)
     assert relmax(p["mean"], po["mean"]) < 1e-9 and relmax(p["var"], po["var"]) < 1e-9
     assert relmax(G.gp_loo(gp, x, y)["loos"], R.gp_loo(og, x, y)["loos"]) < 1e-9
