@@ -328,11 +328,9 @@ def run_gpu(args):
         kk, lk, me, ap, op = specs(theta_sequence(k))
         h = C.c_void_p()
         res = L.FitResult()
-        st = lib.gpgp_fit_dev(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
-                              C.c_void_p(xd.data_ptr()), n, D, C.c_void_p(yd.data_ptr()), None, None,
-                              C.byref(h), C.byref(res))
-        L.check(st, ctx.h)
-        st = lib.gpgp_model_grad(h, L.ptr(gt), C.byref(gs))
+        st = lib.gpgp_fit_grad_dev(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
+                                   C.c_void_p(xd.data_ptr()), n, D, C.c_void_p(yd.data_ptr()), None, None,
+                                   C.byref(h), C.byref(res), L.ptr(gt), C.byref(gs))
         L.check(st, ctx.h)
         lib.gpgp_model_free(h)
         return res.log_evidence
@@ -343,10 +341,9 @@ def run_gpu(args):
         kk, lk, me, ap, op = specs(theta_sequence(k))
         h = C.c_void_p()
         res = L.FitResult()
-        st = lib.gpgp_fit(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
-                          L.ptr(xf), n, D, L.ptr(yh), None, None, C.byref(h), C.byref(res))
-        L.check(st, ctx.h)
-        st = lib.gpgp_model_grad(h, L.ptr(gt), C.byref(gs))
+        st = lib.gpgp_fit_grad(ctx.h, C.byref(kk), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op),
+                               L.ptr(xf), n, D, L.ptr(yh), None, None, C.byref(h), C.byref(res), L.ptr(gt),
+                               C.byref(gs))
         L.check(st, ctx.h)
         lib.gpgp_model_free(h)
         return res.log_evidence

@@ -128,6 +128,12 @@ SIGNATURES = {
                                C.POINTER(FitResult)]),
     "gpgp_model_free": (C.c_int, [_P]),
     "gpgp_model_grad": (C.c_int, [_P, _P, _P]),
+    "gpgp_fit_grad": (C.c_int, [_P, C.POINTER(Kernel), C.POINTER(Lik), C.POINTER(Method), C.POINTER(Approx),
+                                C.POINTER(FitOpts), _P, C.c_int64, C.c_int32, _P, _P, _P, C.POINTER(_P),
+                                C.POINTER(FitResult), _P, _P]),
+    "gpgp_fit_grad_dev": (C.c_int, [_P, C.POINTER(Kernel), C.POINTER(Lik), C.POINTER(Method), C.POINTER(Approx),
+                                    C.POINTER(FitOpts), _P, C.c_int64, C.c_int32, _P, _P, _P, C.POINTER(_P),
+                                    C.POINTER(FitResult), _P, _P]),
     "gpgp_model_get": (C.c_int, [_P, C.c_int32, _P]),
     "gpgp_pred": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),
     "gpgp_pred_dev": (C.c_int, [_P, _P, C.c_int64, C.c_uint32, _P, _P]),

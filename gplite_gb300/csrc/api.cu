@@ -183,24 +183,41 @@ __global__ void refine_residual_kernel(int64_t n, const double *__restrict__ rhs
 // FP64 iterative refinement in B-space on the current factor: r = s z - B u with
 // B u = u + s (K alpha); u += B^-1 r; alpha = s u; fnew = K alpha. w.rhs holds s z
 // and w.u the current solution.
-void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters) {
+// B^-1 b = L^-T (L^-1 b): by the flag-ordered triangular solves with L, or, once
+// W = L^-1 is formed (m->Linv, use_w), by two triangular matrix-vector products.
+void solve_B(gpgp_model *m, Work &w, const double *b, double *tmp, double *x, bool use_w) {
   cudaStream_t st = m->ctx->stream;
   const int64_t n = m->n;
+  if (use_w) {
+    trmv_lower(st, false, n, m->Linv.p, n, b, tmp);
+    trmv_lower(st, true, n, m->Linv.p, n, tmp, x);
+    return;
+  }
   unsigned *bar = (unsigned *)w.flags.p + 2;
+  trsv_flow(st, m->L.p, n, n, m->Winv.p, b, tmp, false, w.status.p, bar, m->errflag.p);
+  trsv_flow(st, m->L.p, n, n, m->Winv.p, tmp, x, true, w.status.p, bar, m->errflag.p);
+}
+
+void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters, bool use_w = false) {
+  cudaStream_t st = m->ctx->stream;
+  const int64_t n = m->n;
   for (int it = 0; it < iters; ++it) {
     refine_residual_kernel<<<g1(n), 256, 0, st>>>(n, w.rhs.p, w.u.p, m->s.p, fnew, w.t1.p);
     GPGP_CHECK_LAUNCH();
-    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
-    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.t1.p, true, w.status.p, bar, m->errflag.p);
+    solve_B(m, w, w.t1.p, w.t2.p, w.t1.p, use_w);  // t1 <- B^-1 t1 (t1 -> t2 -> t1)
     vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
   }
 }
 
-// refine < 0: the model's own refinement count (mixed precision only)
+// refine < 0: the model's own refinement count (mixed precision only). hflags
+// (optional): w.flags[0] read back with the factorisation status in the same
+// synchronisation; a set site flag (NaN or V <= 0) makes the result void, and no
+// FP64 retry is made for it.
 int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
-                         double *fnew, double *logdetL, bool force_fp64 = false, int refine = -1) {
+                         double *fnew, double *logdetL, bool force_fp64 = false, int refine = -1,
+                         int *hflags = nullptr) {
   gpgp_ctx *ctx = m->ctx;
   cudaStream_t st = ctx->stream;
   const int64_t n = m->n;
@@ -215,26 +232,36 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     else
       potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
   }
+  // When the energy gradient follows (mixed precision), W = L^-1, which it needs,
+  // is formed now and the solves use it: two matrix-vector products in place of
+  // the flag-ordered triangular solves, whose 64-row steps are serial.
+  const bool use_w = mixed && m->want_linv;
+  if (use_w) {
+    Phase ph(ctx, GPGP_PHASE_TRTRI);
+    if (m->Linv.n != (size_t)n * n) m->Linv.alloc(st, (size_t)n * n);
+    trtri_mixed(st, m->L.p, n, n, m->Winv.p, m->Linv.p, n, m->errflag.p);
+  }
   {
     Phase ph(ctx, GPGP_PHASE_SOLVE);
     // u = B^-1 (s z) with B = L L^T; alpha = s u
     gauss_alpha_prep<<<g1(n), 256, 0, st>>>(n, m->s.p, zvec, w.t1.p);
     GPGP_CHECK_LAUNCH();
     GPGP_CUDA(cudaMemcpyAsync(w.rhs.p, w.t1.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    unsigned *bar = (unsigned *)w.flags.p + 2;
-    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t1.p, w.t2.p, false, w.status.p, bar, m->errflag.p);
-    trsv_flow(st, m->L.p, n, n, m->Winv.p, w.t2.p, w.u.p, true, w.status.p, bar, m->errflag.p);
+    solve_B(m, w, w.t1.p, w.t2.p, w.u.p, use_w);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
     gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
-    if (mixed) refine_alpha(m, w, alpha, fnew, refine < 0 ? std::max(1, m->opts.refine_iters) : refine);
+    if (mixed)
+      refine_alpha(m, w, alpha, fnew, refine < 0 ? std::max(1, m->opts.refine_iters) : refine, use_w);
   }
   const int64_t nblk = (n + NB - 1) / NB;
   sum_vec(st, w.logdet_part.p, nblk, logdetL);
   int hstatus = 0;
   GPGP_CUDA(cudaMemcpyAsync(&hstatus, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (hflags) GPGP_CUDA(cudaMemcpyAsync(hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   GPGP_CUDA(cudaStreamSynchronize(st));
   m->have_binv_diag = false;
-  m->have_Linv = false;
+  m->have_Linv = use_w && hstatus == 0;
+  if (hflags && (*hflags & 6)) return 0;
   if (hstatus != 0 && mixed) {
     // The sliced trailing updates carry an error of ~2^-33 of the largest entries
     // of B; when B's entries are large (big Laplace weights W) and a pivot is
@@ -242,7 +269,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     // definite in FP64. Redo this factorisation on the FP64 pipe, whose
     // verdict is the reference's.
     ++m->fp64_fallbacks;
-    return factor_and_solve(m, w, zvec, alpha, fnew, logdetL, true, refine);
+    return factor_and_solve(m, w, zvec, alpha, fnew, logdetL, true, refine, hflags);
   }
   return hstatus;
 }
@@ -335,17 +362,20 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       GPGP_CUDA(cudaMemsetAsync(w.flags.p, 0, sizeof(int), st));
       check_positive_kernel<<<g1(n), 256, 0, st>>>(n, m->V.p, w.flags.p);
       GPGP_CHECK_LAUNCH();
+      // mixed precision: the Newton iterates only steer the iteration, so their
+      // solves go unrefined; the final alpha and f are refined once it stops
+      const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
+      // The log-concave factorisation is queued before the site flags are read:
+      // the flags come back with its status in one synchronisation, and a set
+      // flag discards it.
       int hflags = 0;
-      GPGP_CUDA(cudaMemcpyAsync(&hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-      GPGP_CUDA(cudaStreamSynchronize(st));
+      const int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
+                                            (mixed && maxiter > 1) ? 0 : -1, &hflags);
       if (hflags & 2) {  // all(V > 0) is NA in R: an error
         res->status = GPGP_ENAN;
         res->log_evidence = NAN;
         return fail(ctx, GPGP_ENAN, "NaN in the Laplace pseudo-data");
       }
-      // mixed precision: the Newton iterates only steer the iteration, so their
-      // solves go unrefined; the final alpha and f are refined once it stops
-      const bool mixed = m->opts.precision == GPGP_PREC_MIXED;
       if (hflags & 4) {
         // some pseudo-variance <= 0: the good / bad split (R/laplace.R:40-117), FP64
         bool improper = false;
@@ -360,8 +390,6 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
         m->improper = improper;
         nlc_iter = true;
       } else {
-        int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
-                                        (mixed && maxiter > 1) ? 0 : -1);
         if (info != 0) {
           res->status = GPGP_ENOT_PD;
           res->info = info;
@@ -372,8 +400,10 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
         m->improper = false;
         nlc_iter = false;
       }
-      max_abs_diff(st, n, m->fmean.p, fnew.p, red);
-      diff = read_scalar(ctx, red + 64);
+      if (maxiter > 1) {  // one iteration (lik_gaussian): the step size is not used
+        max_abs_diff(st, n, m->fmean.p, fnew.p, red);
+        diff = read_scalar(ctx, red + 64);
+      }
       const bool last = diff < m->approx.tol || it == maxiter;
       if (last && mixed && maxiter > 1 && !nlc_iter)
         refine_alpha(m, w, m->alpha.p, fnew.p, std::max(1, m->opts.refine_iters));
@@ -389,9 +419,11 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       // LML = loglik(f) - 0.5 f^T alpha - 0.5 (C_logdet - V_logdet), C_logdet - V_logdet = 2 sum log L_ii
       lik_loglik(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, red + 101, red);
       dot_partial(st, n, m->fmean.p, m->alpha.p, red + 110);  // result at red + 174
-      double ll = read_scalar(ctx, red + 101);
-      double fa = read_scalar(ctx, red + 174);
-      double ld = read_scalar(ctx, logdetL);
+      // red[100] (log det L), red[101] and red[174] in one copy
+      double hr[75];
+      GPGP_CUDA(cudaMemcpyAsync(hr, red + 100, sizeof(hr), cudaMemcpyDeviceToHost, st));
+      GPGP_CUDA(cudaStreamSynchronize(st));
+      const double ll = hr[1], fa = hr[74], ld = hr[0];
       m->log_evidence = ll - 0.5 * fa - 0.5 * (2.0 * ld);
     }
     res->log_evidence = m->log_evidence;
@@ -550,7 +582,7 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
                        const gpgp_method *method, const gpgp_approx *approx,
                        const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
                        const double *y, const double *trials, const double *offset,
-                       gpgp_model **model, gpgp_fit_result *result, bool on_device) {
+                       gpgp_model **model, gpgp_fit_result *result, bool on_device, bool want_grad = false) {
   if (!ctx || !k || !lik || !method || !approx || !opts || !x || !y || !model || !result)
     return fail(ctx, GPGP_EINVAL, "null argument");
   if (n < 1 || d < 1) return fail(ctx, GPGP_EINVAL, "n and d must be positive");
@@ -628,6 +660,7 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   } else if (method->kind == GPGP_METHOD_FITC) {
     st = fit_fitc(m.get(), result, method->inducing, on_device);
   } else {
+    m->want_linv = want_grad && lik->kind == GPGP_LIK_GAUSSIAN && opts->precision == GPGP_PREC_MIXED;
     st = fit_full(m.get(), result);
   }
   if (st != GPGP_OK) {
@@ -859,9 +892,10 @@ static gpgp_status fit_with_fallback(gpgp_ctx *ctx, const gpgp_kernel *k, const 
                                      const gpgp_method *method, const gpgp_approx *approx,
                                      const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
                                      const double *y, const double *trials, const double *offset,
-                                     gpgp_model **model, gpgp_fit_result *result, bool on_device) {
+                                     gpgp_model **model, gpgp_fit_result *result, bool on_device,
+                                     bool want_grad = false) {
   gpgp_status st = fit_common(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model,
-                              result, on_device);
+                              result, on_device, want_grad);
   const bool mixed = opts && opts->precision == GPGP_PREC_MIXED;
   if (result) result->precision_used = opts ? opts->precision : GPGP_PREC_FP64;
   if (!mixed || !lik || lik->kind == GPGP_LIK_GAUSSIAN) return st;
@@ -878,6 +912,43 @@ static gpgp_status fit_with_fallback(gpgp_ctx *ctx, const gpgp_kernel *k, const 
   st = fit_common(ctx, k, lik, method, approx, &o64, x, n, d, y, trials, offset, model, result, on_device);
   result->precision_used = GPGP_PREC_FP64;
   return st;
+}
+
+// gp_fit and the energy gradient in one call; see include/gpgp.h.
+static gpgp_status fit_grad_impl(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
+                                 const gpgp_method *method, const gpgp_approx *approx,
+                                 const gpgp_fit_opts *opts, const double *x, int64_t n, int32_t d,
+                                 const double *y, const double *trials, const double *offset, gpgp_model **model,
+                                 gpgp_fit_result *result, double *grad_terms, double *grad_lik_sigma,
+                                 bool on_device) {
+  if (!grad_terms) return fail(ctx, GPGP_EINVAL, "grad_terms is null");
+  if (lik && method && (lik->kind != GPGP_LIK_GAUSSIAN || method->kind != GPGP_METHOD_FULL))
+    return fail(ctx, GPGP_EUNSUPPORTED, "gradient needs lik_gaussian and method_full");
+  gpgp_status st = guarded(ctx, [&]() {
+    if (ctx) GPGP_CUDA(cudaSetDevice(ctx->device));
+    return fit_with_fallback(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model, result,
+                             on_device, true);
+  });
+  if (st != GPGP_OK) return st;
+  return gpgp_model_grad(*model, grad_terms, grad_lik_sigma);
+}
+
+gpgp_status gpgp_fit_grad(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik, const gpgp_method *method,
+                          const gpgp_approx *approx, const gpgp_fit_opts *opts, const double *x, int64_t n,
+                          int32_t d, const double *y, const double *trials, const double *offset,
+                          gpgp_model **model, gpgp_fit_result *result, double *grad_terms,
+                          double *grad_lik_sigma) {
+  return fit_grad_impl(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model, result, grad_terms,
+                       grad_lik_sigma, false);
+}
+
+gpgp_status gpgp_fit_grad_dev(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik, const gpgp_method *method,
+                              const gpgp_approx *approx, const gpgp_fit_opts *opts, const double *x, int64_t n,
+                              int32_t d, const double *y, const double *trials, const double *offset,
+                              gpgp_model **model, gpgp_fit_result *result, double *grad_terms,
+                              double *grad_lik_sigma) {
+  return fit_grad_impl(ctx, k, lik, method, approx, opts, x, n, d, y, trials, offset, model, result, grad_terms,
+                       grad_lik_sigma, true);
 }
 
 gpgp_status gpgp_fit(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,

@@ -221,6 +221,9 @@ void col_sumsq(cudaStream_t s, const double *B, int64_t n, int64_t m, int64_t ld
 // y = A x with symmetric A given by its full storage (n x n).
 void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, const double *A,
             int64_t lda, const double *x, double beta, double *y);
+// y = W x (trans false) or W^T x (trans true) for a lower-triangular W whose strict
+// upper part is zero (n x n, ldw).
+void trmv_lower(cudaStream_t s, bool trans, int64_t n, const double *W, int64_t ldw, const double *x, double *y);
 // Sum of logdet partials (fixed order) -> out[0].
 void sum_vec(cudaStream_t s, const double *v, int64_t n, double *out);
 // LU with partial pivoting of a general n x n A (lda), in place; piv[k] is the row

@@ -941,6 +941,51 @@ __global__ void gemv_reduce_kernel(int64_t M, int nchunk, const double *__restri
   y[r] = (beta == 0.0) ? alpha * s : alpha * s + beta * y[r];
 }
 
+// Lower-triangular W (n x n, strict upper zero): y = W x (column chunks above a row
+// block are skipped) or y = W^T x (a column's warp starts at its diagonal's
+// 32-row group). Half the FP64 work of a full gemv, which bounds it on this part.
+__global__ void trmv_n_kernel(int64_t n, const double *__restrict__ W, int64_t ldw, const double *__restrict__ x,
+                              double *__restrict__ part) {
+  const int64_t r = (int64_t)blockIdx.x * GV_ROWS + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * GV_COLS;
+  const int64_t rmax = (int64_t)blockIdx.x * GV_ROWS + GV_ROWS;  // columns >= rmax are zero for this block
+  int64_t c1 = (c0 + GV_COLS < n) ? c0 + GV_COLS : n;
+  if (c1 > rmax) c1 = rmax;
+  if (r >= n) return;
+  double s = 0.0;
+  for (int64_t c = c0; c < c1; ++c) s = fma(W[r + c * ldw], x[c], s);
+  part[r + blockIdx.y * n] = s;
+}
+
+__global__ void trmv_t_kernel(int64_t n, const double *__restrict__ W, int64_t ldw, const double *__restrict__ x,
+                              double *__restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= n) return;
+  double s = 0.0;
+  for (int64_t r = (c & ~(int64_t)31) + lane; r < n; r += 32) s = fma(W[r + c * ldw], x[r], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) y[c] = s;
+}
+
+void trmv_lower(cudaStream_t s, bool trans, int64_t n, const double *W, int64_t ldw, const double *x, double *y) {
+  if (n <= 0) return;
+  if (trans) {
+    trmv_t_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, W, ldw, x, y);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
+  const int nchunk = (int)std::max<int64_t>(1, (n + GV_COLS - 1) / GV_COLS);
+  double *part = nullptr;
+  GPGP_CUDA(cudaMallocAsync((void **)&part, (size_t)n * nchunk * sizeof(double), s));
+  dim3 grid((unsigned)((n + GV_ROWS - 1) / GV_ROWS), (unsigned)nchunk);
+  trmv_n_kernel<<<grid, GV_ROWS, 0, s>>>(n, W, ldw, x, part);
+  GPGP_CHECK_LAUNCH();
+  gemv_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nchunk, part, 1.0, 0.0, y);
+  GPGP_CHECK_LAUNCH();
+  GPGP_CUDA(cudaFreeAsync(part, s));
+}
+
 void gemv64(cudaStream_t s, bool trans, int64_t M, int64_t N, double alpha, const double *A,
             int64_t lda, const double *x, double beta, double *y) {
   if (trans) {

@@ -190,6 +190,7 @@ struct gpgp_model {
   bool have_binv_diag = false;
   gpgp::DBuf Linv;                     // W = L^-1, kept resident once computed
   bool have_Linv = false;
+  bool want_linv = false;              // the gradient follows the fit: form L^-1 right after the factor (mixed)
   gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
   std::unique_ptr<gpgp::FitcState> fitc;
   std::unique_ptr<gpgp::NlcState> nlc;  // set when the last iteration was non-log-concave

@@ -273,6 +273,23 @@ gpgp_status gpgp_model_free(gpgp_model *model);
  * full method. This is tr((alpha alpha^T - C^-1) dC/dtheta)/2; the reference
  * has no gradient (it optimises with Nelder-Mead, R/gp_optim.R:94). */
 gpgp_status gpgp_model_grad(gpgp_model *model, double *grad_terms, double *grad_lik_sigma);
+/* gpgp_fit (gpgp_fit_dev) followed by gpgp_model_grad, in one call: the step of
+ * a gradient-based gp_optim. Same arguments and outputs as the two calls (the
+ * model is returned fitted). Knowing that the gradient follows, a mixed-precision
+ * fit forms the triangular inverse L^-1 the gradient needs right after the
+ * factorisation and solves for alpha with it (two matrix-vector products per
+ * solve) instead of with the blocked triangular solves. lik_gaussian and
+ * method_full only (GPGP_EUNSUPPORTED otherwise, as gpgp_model_grad). */
+gpgp_status gpgp_fit_grad(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik, const gpgp_method *method,
+                          const gpgp_approx *approx, const gpgp_fit_opts *opts, const double *x, int64_t n,
+                          int32_t d, const double *y, const double *trials, const double *offset,
+                          gpgp_model **model, gpgp_fit_result *result, double *grad_terms,
+                          double *grad_lik_sigma);
+gpgp_status gpgp_fit_grad_dev(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik, const gpgp_method *method,
+                              const gpgp_approx *approx, const gpgp_fit_opts *opts, const double *x, int64_t n,
+                              int32_t d, const double *y, const double *trials, const double *offset,
+                              gpgp_model **model, gpgp_fit_result *result, double *grad_terms,
+                              double *grad_lik_sigma);
 
 /* Copy a resident model vector out to host memory (length n unless noted). */
 typedef enum gpgp_model_field {

@@ -153,3 +153,56 @@ def test_mixed_gradient_and_inverse_match_fp64(n):
     prior_var = 1.0 ** 2 + 0.7 ** 2
     assert np.max(np.abs(pm["var"] - p64["var"])) < 1e-7 * prior_var
     assert relmax(pm["mean"], p64["mean"]) < 1e-8
+
+
+def _fit_grad_abi(gp, x, y, prec, fused):
+    """gpgp_fit_grad, or gpgp_fit then gpgp_model_grad, through the C ABI."""
+    from gplite_gb300 import gp as GP
+    lib = L.load()
+    ctx = L.default_context()
+    n, d = x.shape
+    GP.learn_scales(gp, x)
+    k = GP.kernel_struct(gp.cfs, d)
+    lk = GP._lik_struct(gp.lik)
+    me, keep = GP._method_struct(gp, d, x)
+    ap = GP._approx_struct(gp)
+    op = L.FitOpts()
+    op.jitter, op.precision, op.refine_iters = 1e-6, L.PRECISION[prec], 2
+    xf, yy = L.fortran(x), np.ascontiguousarray(y)
+    h = C.c_void_p()
+    res = L.FitResult()
+    gt = np.zeros(len(GP._flat_terms(gp)) * L.TERM_NPARAM)
+    gs = C.c_double(0.0)
+    if fused:
+        st = lib.gpgp_fit_grad(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf),
+                               n, d, L.ptr(yy), None, None, C.byref(h), C.byref(res), L.ptr(gt), C.byref(gs))
+        L.check(st, ctx.h)
+    else:
+        L.check(lib.gpgp_fit(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf),
+                             n, d, L.ptr(yy), None, None, C.byref(h), C.byref(res)), ctx.h)
+        L.check(lib.gpgp_model_grad(h, L.ptr(gt), C.byref(gs)), ctx.h)
+    lib.gpgp_model_free(h)
+    return res.log_evidence, np.append(gt, gs.value)
+
+
+@pytest.mark.parametrize("n", [700, 2248])
+def test_fit_grad_entry_point(n):
+    """gpgp_fit_grad = gpgp_fit + gpgp_model_grad. In FP64 the two are the same
+    computation; under mixed precision the fused call solves for alpha with W = L^-1
+    (formed right after the factor) and its results agree with the separate calls
+    (1e-10 on the evidence) and with FP64 within the mixed path's bound (1e-8)."""
+    rng = np.random.default_rng(n + 1)
+    x = rng.uniform(-1, 1, (n, 3))
+    y = np.sin(3 * x[:, 0]) + x[:, 1] + 0.05 * rng.standard_normal(n)
+
+    def gp():
+        return G.gp_init([G.cf_matern52(lscale=0.6, magn=1.0), G.cf_const(magn=0.7)], G.lik_gaussian(sigma=0.05))
+    l64f, g64f = _fit_grad_abi(gp(), x, y, "fp64", True)
+    l64, g64 = _fit_grad_abi(gp(), x, y, "fp64", False)
+    assert l64f == l64 and np.array_equal(g64f, g64)
+    lmf, gmf = _fit_grad_abi(gp(), x, y, "mixed", True)
+    lm, gm = _fit_grad_abi(gp(), x, y, "mixed", False)
+    assert abs(lmf - lm) <= 1e-10 * abs(lm)
+    assert abs(lmf - l64) <= 1e-8 * abs(l64)  # the mixed path's stated bound (about 1.5e-9 here)
+    assert relmax(gmf, gm) < 1e-9
+    assert relmax(gmf, g64) < 1e-7
