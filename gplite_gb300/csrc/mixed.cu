@@ -214,6 +214,109 @@ __global__ void __launch_bounds__(256) oz_split_kernel(const double *__restrict_
   }
 }
 
+// Two-pass split for operands with too few 32-row groups to fill the GPU: pass 1
+// takes the biased exponent field E of every element of 32 rows x 256 K and
+// atomically maximises it per row (E is monotonic in |x|, so the row's largest E
+// is that of its largest element; 0 and 2047 mark zero / subnormal and
+// non-finite rows as in the one-pass kernel); pass 2 writes the slices of one
+// 64-wide K block of 32 rows per CTA.
+constexpr int OZ_EK = 256;  // K per pass-1 CTA
+
+__global__ void __launch_bounds__(256) oz_rowexp_kernel(const double *__restrict__ P, int64_t ld, int trans,
+                                                        int64_t rows, int64_t K, int *__restrict__ Emax,
+                                                        int64_t sP, int64_t sM) {
+  P += blockIdx.z * sP;
+  Emax += blockIdx.z * sM;
+  __shared__ int part[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  const int64_t k0 = (int64_t)blockIdx.y * OZ_EK;
+  const int64_t k1 = k0 + OZ_EK < K ? k0 + OZ_EK : K;
+  if (!trans) {
+    const int64_t r = r0 + lane;
+    int mx = 0;
+    if (r < rows)
+      for (int64_t k = k0 + warp; k < k1; k += 8) {
+        const int E = (int)(((unsigned long long)__double_as_longlong(P[r + k * ld]) >> 52) & 0x7FF);
+        mx = E > mx ? E : mx;
+      }
+    part[warp][lane] = mx;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int rl = warp * 4 + q;
+      const int64_t r = r0 + rl;
+      int mx = 0;
+      if (r < rows)
+        for (int64_t k = k0 + lane; k < k1; k += 32) {
+          const int E = (int)(((unsigned long long)__double_as_longlong(P[k + r * ld]) >> 52) & 0x7FF);
+          mx = E > mx ? E : mx;
+        }
+      for (int o = 16; o > 0; o >>= 1) {
+        const int t = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = t > mx ? t : mx;
+      }
+      if (lane == 0) part[0][rl] = mx;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int mx = part[0][lane];
+    if (!trans)
+#pragma unroll
+      for (int w = 1; w < 8; ++w) mx = part[w][lane] > mx ? part[w][lane] : mx;
+    if (r0 + lane < rows && mx > 0) atomicMax(Emax + r0 + lane, mx);
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) oz_slice_kernel(const double *__restrict__ P, int64_t ld, int trans,
+                                                       int64_t rows, int64_t K, int64_t nrb, int64_t nkb,
+                                                       const int *__restrict__ Emax, int *__restrict__ ex,
+                                                       uint16_t *__restrict__ sl, int64_t sP, int64_t sE,
+                                                       int64_t sS, int64_t sM) {
+  P += blockIdx.z * sP;
+  ex += blockIdx.z * sE;
+  sl += blockIdx.z * sS;
+  Emax += blockIdx.z * sM;
+  __shared__ double T[32][65];
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  const int rl = threadIdx.x & 31, gl = threadIdx.x >> 5;
+  const int64_t r = r0 + rl;
+  const int E = r < rows ? Emax[r] : 0;
+  const int e = (E == 0 || E == 2047) ? 0 : E - 1022;
+  if (blockIdx.y == 0 && gl == 0 && r < nrb * OZ_TR) ex[r] = e;
+  const int64_t kb0 = (int64_t)blockIdx.y * 64;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int idx = threadIdx.x + 256 * q;
+    const int ar = trans ? idx / 64 : idx % 32, ak = trans ? idx % 64 : idx / 32;
+    T[ar][ak] = oz_elem(P, ld, trans, r0 + ar, kb0 + ak, rows, K);
+  }
+  __syncthreads();
+  if (r >= nrb * OZ_TR) return;
+  const int64_t k0 = kb0 + 8 * gl;
+  uint32_t packed[S][4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    int d0[S], d1[S];
+    oz_digits<S>(T[rl][8 * gl + j], e, d0);
+    oz_digits<S>(T[rl][8 * gl + j + 1], e, d1);
+#pragma unroll
+    for (int t = 0; t < S; ++t) packed[t][j / 2] = bf16_of_digit(d0[t], t) | (bf16_of_digit(d1[t], t) << 16);
+  }
+  const int64_t nkc = 2 * nkb;
+  const int64_t rb = r / OZ_TR, rr = r % OZ_TR;
+  const int64_t kc = k0 / OZ_TK, kk = k0 % OZ_TK;
+  const int64_t within = (rr / 8) * 256 + (kk / 8) * 64 + (rr % 8) * 8;
+#pragma unroll
+  for (int t = 0; t < S; ++t) {
+    const int64_t tile = ((int64_t)t * nkc + kc) * nrb + rb;
+    *reinterpret_cast<uint4 *>(sl + tile * OZ_TILE + within) =
+        make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
+  }
+}
+
 // 64-row tiles of a split operand: one more than the rows need, rounded up to
 // an even count, so that a 128-row A tile starting at any 64-row offset inside
 // the operand stays inside the buffer.
@@ -233,7 +336,27 @@ void oz_split_batched(cudaStream_t s, const double *P, int64_t ld, int64_t sP, i
   const int64_t rows_pad = nrb * OZ_TR;
   const int64_t sE = out->bstride_ex, sS = out->bstride_sl;
   KTScope kts(GPGP_KPROF_OZ_SPLIT, s, 0.0);
-  dim3 g((unsigned)(rows_pad / 32), (unsigned)batch);
+  const int64_t groups = rows_pad / 32;
+  if (groups * batch < 2 * (int64_t)device_sms() && nkb >= 2 && batch <= 65535) {
+    // too few row groups for one CTA each to fill the GPU: two passes over a 2-D grid
+    int *Emax = nullptr;
+    GPGP_CUDA(cudaMallocAsync((void **)&Emax, (size_t)rows_pad * batch * sizeof(int), s));
+    GPGP_CUDA(cudaMemsetAsync(Emax, 0, (size_t)rows_pad * batch * sizeof(int), s));
+    dim3 g1((unsigned)groups, (unsigned)((K + OZ_EK - 1) / OZ_EK), (unsigned)batch);
+    oz_rowexp_kernel<<<g1, 256, 0, s>>>(P, ld, trans, rows, K, Emax, sP, rows_pad);
+    GPGP_CHECK_LAUNCH();
+    dim3 g2((unsigned)groups, (unsigned)nkb, (unsigned)batch);
+    if (out->S == 5)
+      oz_slice_kernel<5><<<g2, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, Emax, out->ex, out->sl, sP, sE, sS,
+                                            rows_pad);
+    else
+      oz_slice_kernel<4><<<g2, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, Emax, out->ex, out->sl, sP, sE, sS,
+                                            rows_pad);
+    GPGP_CHECK_LAUNCH();
+    GPGP_CUDA(cudaFreeAsync(Emax, s));
+    return;
+  }
+  dim3 g((unsigned)groups, (unsigned)batch);
   if (out->S == 5)
     oz_split_kernel<5><<<g, 256, 0, s>>>(P, ld, trans, rows, K, nrb, nkb, out->ex, out->sl, sP, sE, sS);
   else
