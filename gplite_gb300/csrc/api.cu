@@ -207,7 +207,7 @@ void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters
     solve_B(m, w, w.t1.p, w.t2.p, w.t1.p, use_w);  // t1 <- B^-1 t1 (t1 -> t2 -> t1)
     vec_axpby(st, n, 1.0, w.t1.p, 1.0, w.u.p);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
-    gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+    gemv64(st, true, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);  // K symmetric: K alpha = K^T alpha
   }
 }
 
@@ -230,7 +230,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     if (mixed)
       potrf_mixed(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p, m->errflag.p, &ctx->side);
     else
-      potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p);
+      potrf(st, m->L.p, n, n, m->Winv.p, w.logdet_part.p, w.status.p, 1);
   }
   // When the energy gradient follows (mixed precision), W = L^-1, which it needs,
   // is formed now and the solves use it: two matrix-vector products in place of
@@ -249,7 +249,7 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
     GPGP_CUDA(cudaMemcpyAsync(w.rhs.p, w.t1.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     solve_B(m, w, w.t1.p, w.t2.p, w.u.p, use_w);
     vec_mul(st, n, m->s.p, w.u.p, alpha);
-    gemv64(st, false, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);
+    gemv64(st, true, n, n, 1.0, w.K.p, n, alpha, 0.0, fnew);  // K symmetric: K alpha = K^T alpha
     if (mixed)
       refine_alpha(m, w, alpha, fnew, refine < 0 ? std::max(1, m->opts.refine_iters) : refine, use_w);
   }

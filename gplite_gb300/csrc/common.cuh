@@ -186,9 +186,12 @@ void potrf_batched(cudaStream_t s, double *A, int64_t n, int64_t lda, int64_t sA
 // place. Winv receives the inverses of the NB x NB diagonal factors
 // (nblocks * NB * NB); logdet_part the per-block sums of log L_jj; status[0]
 // the first failing pivot (1-based, 0 = OK). Later kernels of the same
-// sequence see a non-zero status and return without work.
+// sequence see a non-zero status and return without work. panel_mode 0: the
+// rows below each diagonal block by substitution (backward stable for an
+// ill-conditioned block, e.g. FITC's K_z); 1: by the block's inverse, spread
+// over many CTAs (for well-conditioned matrices such as B = I + S K S).
 void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
-           int *status);
+           int *status, int panel_mode = 0);
 
 // Triangular solves with the blocked factor (lower L, diagonal inverses Winv).
 // b is consumed as workspace; x receives the solution (x != b).

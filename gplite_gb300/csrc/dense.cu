@@ -172,6 +172,30 @@ static void gemm64_dispatch(cudaStream_t s, bool ta, bool tb, dim3 grid, int64_t
     launch_gemm64<true, true>(s, grid, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lo, tri_mode, sA, sB, sC, kchunk);
 }
 
+// Small products (few 64 x 64 tiles, short K): one thread per element of C, so
+// that the FP64 work spreads over many SMs instead of a few tile CTAs (an FP64
+// warp instruction holds its sub-partition for 64 cycles on this part).
+__global__ void gemm64_small_kernel(int64_t M, int64_t N, int64_t K, double alpha, const double *__restrict__ A,
+                                    int64_t lda, int ta, const double *__restrict__ B, int64_t ldb, int tb,
+                                    double beta, double *__restrict__ C, int64_t ldc, int lower) {
+  const int64_t i = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+  const int64_t j = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= M || j >= N || (lower && j > i)) return;
+  double s0 = 0.0, s1 = 0.0;
+  int64_t k = 0;
+  for (; k + 1 < K; k += 2) {
+    const double a0 = ta ? A[k + i * lda] : A[i + k * lda];
+    const double a1 = ta ? A[k + 1 + i * lda] : A[i + (k + 1) * lda];
+    const double b0 = tb ? B[j + k * ldb] : B[k + j * ldb];
+    const double b1 = tb ? B[j + (k + 1) * ldb] : B[k + 1 + j * ldb];
+    s0 = fma(a0, b0, s0);
+    s1 = fma(a1, b1, s1);
+  }
+  if (k < K) s0 = fma(ta ? A[k + i * lda] : A[i + k * lda], tb ? B[j + k * ldb] : B[k + j * ldb], s0);
+  const double v = alpha * (s0 + s1);
+  C[i + j * ldc] = (beta == 0.0) ? v : v + beta * C[i + j * ldc];
+}
+
 void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
                     const double *A, int64_t lda, int64_t sA, const double *B, int64_t ldb, int64_t sB,
                     double beta, double *C, int64_t ldc, int64_t sC, int64_t batch, bool lower_only,
@@ -204,6 +228,15 @@ void gemm64_batched(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int6
 void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
             const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
             int64_t ldc, bool lower_only, int tri_mode) {
+  // (the batched entry keeps the tile kernel for every batch size, so that a
+  // problem's result does not depend on how many others share its launch)
+  if (M > 0 && N > 0 && tri_mode == 0 && K <= 256 && ((M + GBM - 1) / GBM) * ((N + GBN - 1) / GBN) < 152) {
+    dim3 g((unsigned)((M + 31) / 32), (unsigned)((N + 7) / 8));
+    gemm64_small_kernel<<<g, 256, 0, s>>>(M, N, K, alpha, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, beta, C, ldc,
+                                          lower_only ? 1 : 0);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
   gemm64_batched(s, ta, tb, M, N, K, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, lower_only,
                  tri_mode);
 }
@@ -431,8 +464,38 @@ __global__ void __launch_bounds__(128) potrf_panel_kernel(double *__restrict__ A
     if (c < kb) A21[r + c * lda] = x[c];
 }
 
+// panel by the diagonal block's inverse: L21 = A21 W11^T, L21(r, c) = sum_{k <= c}
+// A21(r, k) W11(c, k). A CTA takes 4 rows (one element per thread), staged in
+// shared memory with W11, so the FP64 work spreads over m / 4 CTAs. For the
+// well-conditioned diagonal blocks of B = I + S K S the error is that of the
+// substitution to within the block's condition number.
+__global__ void __launch_bounds__(256) potrf_panel_inv_kernel(double *__restrict__ A21, int64_t m, int kb,
+                                                              int64_t lda, const double *__restrict__ W,
+                                                              const int *__restrict__ status) {
+  __shared__ double Ws[NB][NB + 1];
+  __shared__ double As[4][NB + 1];
+  if (*(volatile const int *)status != 0) return;
+  const int64_t r0 = (int64_t)blockIdx.x * 4;
+  for (int idx = threadIdx.x; idx < NB * NB; idx += 256) Ws[idx % NB][idx / NB] = W[idx];
+  {
+    const int rr = threadIdx.x & 3, c = threadIdx.x >> 2;
+    As[rr][c] = (r0 + rr < m && c < kb) ? A21[r0 + rr + c * lda] : 0.0;
+  }
+  __syncthreads();
+  const int rr = threadIdx.x & 3, c = threadIdx.x >> 2;
+  if (r0 + rr >= m || c >= kb) return;
+  double s0 = 0.0, s1 = 0.0;
+  int k = 0;
+  for (; k + 1 <= c; k += 2) {
+    s0 = fma(As[rr][k], Ws[c][k], s0);
+    s1 = fma(As[rr][k + 1], Ws[c][k + 1], s1);
+  }
+  if (k <= c) s0 = fma(As[rr][k], Ws[c][k], s0);
+  A21[r0 + rr + c * lda] = s0 + s1;
+}
+
 void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
-           int *status) {
+           int *status, int panel_mode) {
   for (int64_t k0 = 0, blk = 0; k0 < n; k0 += NB, ++blk) {
     const int kb = (int)std::min<int64_t>(NB, n - k0);
     double *Akk = A + k0 + k0 * lda;
@@ -445,7 +508,10 @@ void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, doub
     const int64_t m = n - k0 - kb;
     if (m > 0) {
       double *A21 = A + (k0 + kb) + k0 * lda;
-      potrf_panel_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(A21, m, kb, lda, Akk, status, 0);
+      if (panel_mode == 1)
+        potrf_panel_inv_kernel<<<(unsigned)((m + 3) / 4), 256, 0, s>>>(A21, m, kb, lda, W, status);
+      else
+        potrf_panel_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(A21, m, kb, lda, Akk, status, 0);
       GPGP_CHECK_LAUNCH();
       double *A22 = A + (k0 + kb) + (k0 + kb) * lda;
       gemm64(s, false, true, m, m, kb, -1.0, A21, lda, A21, lda, 1.0, A22, lda, true, 0);
