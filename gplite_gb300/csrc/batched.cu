@@ -412,7 +412,7 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
       double *Akk = k.Bm.p + k0 + k0 * nb;
       {
         KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
-        potrf_diag_kernel<<<(unsigned)P, 256, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB, k.ldp.p + blk,
+        potrf_diag_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB, k.ldp.p + blk,
                                                        k.status.p, k0, nb * nb, nb * NB, nbl);
       }
       GPGP_CHECK_LAUNCH();

@@ -165,6 +165,7 @@ int64_t cov_grad_partials(int64_t n);
 // dense FP64 linear algebra (column-major)
 // ---------------------------------------------------------------------------
 constexpr int NB = 64;  // block size of the blocked factorisations
+constexpr int DIAG_THREADS = 512;  // threads of the diagonal-block kernel (potrf_diag_kernel)
 
 // C = alpha * op(A) op(B) + beta * C. lower_only: only tiles on/below the
 // diagonal of C are computed (SYRK-style). tri_k: A and B are triangular so

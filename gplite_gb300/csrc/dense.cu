@@ -254,8 +254,9 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
 //    rsqrt_fast) while the update warps apply the rank-1 update of column j to
 //    the trailing triangle c >= j+2. The trailing triangle's entries are
 //    numbered by column, last column first, so that step j's entries are the
-//    first (62-j)(63-j)/2 of one fixed list. Warp 4, which shares warp 0's
-//    sub-partition, takes no update work.
+//    first (62-j)(63-j)/2 of one fixed list. The warps that share warp 0's
+//    sub-partition take no update work; the other twelve (three per
+//    sub-partition, enough to cover the FP64 latency) share it evenly.
 //  - inverse: W = L^-1 = D^-1 V with D = diag(L) and V the unit lower triangular
 //    inverse of the column-scaled factor L D^-1:
 //      V(i, c) = -sum_{k=c..i-1} (L(i, k) / L(k, k)) V(k, c),  V(c, c) = 1.
@@ -277,7 +278,7 @@ __device__ __forceinline__ int div_small(int e, int d, int magic) {
   return (int)(((unsigned)e * (unsigned)magic) >> 20);
 }
 
-__global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
+__global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                                          double *__restrict__ Winv,
                                                          double *__restrict__ logdet_part,
                                                          int *__restrict__ status, int64_t k0,
@@ -296,14 +297,14 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   if (*(volatile int *)status != 0) return;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < NB * NB; idx += 256) {
+  for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
     const int r = idx % NB, c = idx / NB;
     // held negated until its column is pivoted (see the update loop)
     S[r][c] = (r < kb && c < kb && r >= c) ? neg_bits(A[r + c * lda]) : 0.0;
     V[r][c] = 0.0;
   }
   // entry e: u = 63 - c is the largest u with u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2
-  for (int e = tid; e < NB * (NB + 1) / 2; e += 256) {
+  for (int e = tid; e < NB * (NB + 1) / 2; e += DIAG_THREADS) {
     int u = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
     while (u * (u + 1) / 2 > e) --u;
     while ((u + 1) * (u + 2) / 2 <= e) ++u;
@@ -357,8 +358,9 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
   }
   __syncthreads();
   if (failed) return;
-  // update workers: warps 1-3 and 5-7 (warp 4 shares warp 0's sub-partition)
-  const int uw = warp < 4 ? warp - 1 : warp - 2;  // 0..5 for the update warps
+  // update workers: every warp off sub-partition 0 (warps 4, 8, 12 share warp 0's)
+  constexpr int NUPD = DIAG_THREADS / 32 - DIAG_THREADS / 128;  // 12 update warps
+  const int uw = warp - 1 - (warp >> 2);
   const int ut = uw * 32 + lane;
   for (int j = 0; j < kb; ++j) {
     if (warp == 0) {
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
         }
         pivot(j + 1, t);
       }
-    } else if (warp != 4) {
+    } else if ((warp & 3) != 0) {
       // factor step j: entries (r, c), c >= j + 2, of the fixed list; inverse step
       // k = j - 1: entries (i, c), k < i < kb, c < k, row-major by i. Both are
       // dst += a b with a, b >= sign-free operands (the trailing matrix is held
@@ -384,7 +386,7 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
       const int k = j - 1;
       const int ci = k >= 1 ? (kb - 1 - k) * k : 0;
       const int magic = k >= 1 ? ((1 << 20) + k - 1) / k : 0;
-      for (int e = ut; e < cf + ci; e += 192) {
+      for (int e = ut; e < cf + ci; e += NUPD * 32) {
         const double *pa, *pb;
         double *dst;
         if (e < cf) {
@@ -408,14 +410,14 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double *__restrict__ A,
     if (failed) return;
   }
   // write the factor back (lower part of the block)
-  for (int idx = tid; idx < kb * kb; idx += 256) {
+  for (int idx = tid; idx < kb * kb; idx += DIAG_THREADS) {
     const int r = idx % kb, c = idx / kb;
     if (r >= c) A[r + c * lda] = S[r][c];
   }
   if (tid < NB) lg[tid] = tid < kb ? log(S[tid][tid]) : 0.0;
   __syncthreads();
   // W = D^-1 V
-  for (int idx = tid; idx < NB * NB; idx += 256) {
+  for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
     const int r = idx % NB, c = idx / NB;
     double wv = 0.0;
     if (r < kb && c <= r) wv = (r == c) ? rdiag[r] : rdiag[r] * V[r][c];
@@ -502,7 +504,7 @@ void potrf(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, doub
     double *W = Winv + blk * NB * NB;
     {
       KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * kb * kb * kb / 3);
-      potrf_diag_kernel<<<1, 256, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0, 0, 0, 0);
+      potrf_diag_kernel<<<1, DIAG_THREADS, 0, s>>>(Akk, kb, lda, W, logdet_part + blk, status, k0, 0, 0, 0);
     }
     GPGP_CHECK_LAUNCH();
     const int64_t m = n - k0 - kb;
@@ -528,7 +530,7 @@ void potrf_batched(cudaStream_t s, double *A, int64_t n, int64_t lda, int64_t sA
     double *Akk = A + k0 + k0 * lda;
     {
       KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * kb * kb * kb / 3 * (double)batch);
-      potrf_diag_kernel<<<(unsigned)batch, 256, 0, s>>>(Akk, kb, lda, Winv + blk * NB * NB, logdet_part + blk,
+      potrf_diag_kernel<<<(unsigned)batch, DIAG_THREADS, 0, s>>>(Akk, kb, lda, Winv + blk * NB * NB, logdet_part + blk,
                                                         status, k0, sA, sW, sL);
     }
     GPGP_CHECK_LAUNCH();

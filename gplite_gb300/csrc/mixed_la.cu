@@ -63,7 +63,7 @@ void factor_panel(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Win
     double *Wb = Winv + blk * NB * NB;
     {
       KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * jb * jb * jb / 3);
-      potrf_diag_kernel<<<1, 256, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
+      potrf_diag_kernel<<<1, DIAG_THREADS, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
     }
     GPGP_CHECK_LAUNCH();
     const int64_t m = n - j0 - jb;
