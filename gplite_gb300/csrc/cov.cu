@@ -306,6 +306,19 @@ __device__ __forceinline__ void load_feats(double *dst, int lds, const double *F
   }
 }
 
+template <int TT>
+__device__ __forceinline__ void load_feats_t(double *dst, int lds, const double *F, int64_t ld, int64_t row0,
+                                             int64_t n, int nfeat) {
+  for (int idx = threadIdx.x; idx < TT * nfeat; idx += blockDim.x) {
+    int r = idx % TT, c = idx / TT;
+    int64_t row = row0 + r;
+    dst[r * lds + c] = row < n ? F[row + c * ld] : 0.0;
+  }
+}
+
+// TT x TT tiles (TT = 64; 16 for small matrices, so that their tiles spread over
+// more SMs); 256 / TT column groups of threads.
+template <int TT>
 __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1, int64_t ld1, int64_t n1,
                                 const double *__restrict__ F2, int64_t ld2, int64_t n2,
                                 double *__restrict__ out, int64_t ldo, int mode, int sym,
@@ -314,8 +327,8 @@ __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gm
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
   double *Fi = sm;
-  double *Fj = sm + CT * lds;
-  double *Tt = sm + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  double *Fj = sm + TT * lds;
+  double *Tt = sm + 2 * TT * lds;  // TT x (TT+1) staging for the mirrored write
   int64_t bi, bj;
   if (sym)
     tri_index(blockIdx.x, &bi, &bj);
@@ -323,18 +336,19 @@ __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gm
     bi = blockIdx.x;
     bj = blockIdx.y;
   }
-  const int64_t i0 = bi * CT, j0 = bj * CT;
-  load_feats(Fi, lds, F1, ld1, i0, n1, nf);
-  load_feats(Fj, lds, F2, ld2, j0, n2, nf);
+  const int64_t i0 = bi * TT, j0 = bj * TT;
+  constexpr int CG = 256 / TT;
+  load_feats_t<TT>(Fi, lds, F1, ld1, i0, n1, nf);
+  load_feats_t<TT>(Fj, lds, F2, ld2, j0, n2, nf);
   __syncthreads();
-  const int r = threadIdx.x % CT;
-  const int cb = threadIdx.x / CT;
+  const int r = threadIdx.x % TT;
+  const int cb = threadIdx.x / TT;
   const int64_t i = i0 + r;
   const double si = (mode == COV_ROWSCALE && i < n1) ? scale[i] : 1.0;
   const bool do_mirror = sym && mirror && bi != bj;
 #pragma unroll 1
-  for (int q = 0; q < CT / 4; ++q) {
-    const int c = cb + 4 * q;
+  for (int q = 0; q < TT / CG; ++q) {
+    const int c = cb + CG * q;
     const int64_t j = j0 + c;
     double v = 0.0;
     if (i < n1 && j < n2) {
@@ -343,17 +357,17 @@ __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gm
       if (mode == COV_ROWSCALE) v = si * v;
       out[i + j * ldo] = v;
     }
-    if (do_mirror) Tt[c * (CT + 1) + r] = v;
+    if (do_mirror) Tt[c * (TT + 1) + r] = v;
   }
   if (do_mirror) {
     __syncthreads();
     // transposed tile: rows j0.., cols i0..
 #pragma unroll 1
-    for (int q = 0; q < CT / 4; ++q) {
-      const int rr = threadIdx.x % CT;  // row inside the transposed tile (j index)
-      const int cc = threadIdx.x / CT + 4 * q;  // col (i index)
+    for (int q = 0; q < TT / CG; ++q) {
+      const int rr = threadIdx.x % TT;  // row inside the transposed tile (j index)
+      const int cc = threadIdx.x / TT + CG * q;  // col (i index)
       const int64_t jj = j0 + rr, ii = i0 + cc;
-      if (jj < n2 && ii < n1) out[jj + ii * ldo] = Tt[rr * (CT + 1) + cc];
+      if (jj < n2 && ii < n1) out[jj + ii * ldo] = Tt[rr * (TT + 1) + cc];
     }
   }
 }
@@ -366,19 +380,32 @@ void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const 
   size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
   static PerDevice attr;
   per_device(attr, [] {
-    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    2 * CT * 65 * 8 + CT * (CT + 1) * 8));
     return 1;
   });
-  const int64_t T1 = (n1 + CT - 1) / CT, T2 = (n2 + CT - 1) / CT;
-  if (sym) {
+  int64_t T1 = (n1 + CT - 1) / CT, T2 = (n2 + CT - 1) / CT;
+  // fewer 64-tiles than SMs: 16-tiles (the evaluation is FP64-bound per SM)
+  const bool small = (sym ? T1 * (T1 + 1) / 2 : T1 * T2) < device_sms();
+  if (small) {
+    constexpr int ST = 16;
+    smem = (size_t)(2 * ST * lds + ST * (ST + 1)) * sizeof(double);
+    T1 = (n1 + ST - 1) / ST;
+    T2 = (n2 + ST - 1) / ST;
+    if (sym)
+      cov_tile_kernel<ST><<<(unsigned)(T1 * (T1 + 1) / 2), 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2,
+                                                                            out, ldo, mode, 1, mirror, jitter, scale);
+    else
+      cov_tile_kernel<ST><<<dim3((unsigned)T1, (unsigned)T2), 256, smem, s>>>(
+          dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo, mode, 0, 0, 0.0, scale);
+  } else if (sym) {
     int64_t nt = T1 * (T1 + 1) / 2;
-    cov_tile_kernel<<<(unsigned)nt, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out,
-                                                    ldo, mode, 1, mirror, jitter, scale);
+    cov_tile_kernel<CT><<<(unsigned)nt, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out,
+                                                        ldo, mode, 1, mirror, jitter, scale);
   } else {
     dim3 grid((unsigned)T1, (unsigned)T2);
-    cov_tile_kernel<<<grid, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo,
-                                            mode, 0, 0, 0.0, scale);
+    cov_tile_kernel<CT><<<grid, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo,
+                                                mode, 0, 0, 0.0, scale);
   }
   GPGP_CHECK_LAUNCH();
 }

@@ -254,7 +254,7 @@ void gemm64(cudaStream_t s, bool ta, bool tb, int64_t M, int64_t N, int64_t K, d
 //    rsqrt_fast) while the update warps apply the rank-1 update of column j to
 //    the trailing triangle c >= j+2. The trailing triangle's entries are
 //    numbered by column, last column first, so that step j's entries are the
-//    first (62-j)(63-j)/2 of one fixed list. The warps that share warp 0's
+//    first (kb-2-j)(kb-1-j)/2 of one fixed list. The warps that share warp 0's
 //    sub-partition take no update work; the other twelve (three per
 //    sub-partition, enough to cover the FP64 latency) share it evenly.
 //  - inverse: W = L^-1 = D^-1 V with D = diag(L) and V the unit lower triangular
@@ -303,12 +303,14 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_kernel(double *__rest
     S[r][c] = (r < kb && c < kb && r >= c) ? neg_bits(A[r + c * lda]) : 0.0;
     V[r][c] = 0.0;
   }
-  // entry e: u = 63 - c is the largest u with u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2
-  for (int e = tid; e < NB * (NB + 1) / 2; e += DIAG_THREADS) {
+  // entry e of the kb x kb triangle: u = kb - 1 - c is the largest u with
+  // u (u + 1) / 2 <= e; r = c + e - u (u + 1) / 2 (a partial block lists only its
+  // own entries)
+  for (int e = tid; e < kb * (kb + 1) / 2; e += DIAG_THREADS) {
     int u = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
     while (u * (u + 1) / 2 > e) --u;
     while ((u + 1) * (u + 2) / 2 <= e) ++u;
-    const int c = NB - 1 - u, r = c + (e - u * (u + 1) / 2);
+    const int c = kb - 1 - u, r = c + (e - u * (u + 1) / 2);
     pairs[e] = (unsigned short)(r | (c << 8));
   }
   if (tid == 0) failed = 0;
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_kernel(double *__rest
       // k = j - 1: entries (i, c), k < i < kb, c < k, row-major by i. Both are
       // dst += a b with a, b >= sign-free operands (the trailing matrix is held
       // negated), so that each entry is exactly one FP64 instruction.
-      const int cf = j < NB - 2 ? (62 - j) * (63 - j) / 2 : 0;
+      const int cf = j < kb - 2 ? (kb - 2 - j) * (kb - 1 - j) / 2 : 0;
       const int k = j - 1;
       const int ci = k >= 1 ? (kb - 1 - k) * k : 0;
       const int magic = k >= 1 ? ((1 << 20) + k - 1) / k : 0;
