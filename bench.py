@@ -40,12 +40,14 @@ SIGMA = 0.05
 LSCALE, MAGN, CMAGN = 0.7, 1.0, 1.0
 NPRED = 8192
 
-# DRAM traffic of the sliced GEMM per launch of the n = 16384 mixed step, from one
-# ncu capture of all oz_gemm launches of one step (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass; the profile summary under profiles/ gives the
-# command). Filled in from that capture; None until it exists.
-OZ_TRAFFIC_PER_LAUNCH = {}
-OZ_TRAFFIC_SOURCE = None
+# DRAM traffic of the sliced GEMM per launch of the n = 16384 mixed step: the mean of
+# dram__bytes_read.sum + dram__bytes_write.sum over the first 579 oz_gemm launches of
+# one step, one-pass ncu capture (the profile summaries give the command and the
+# per-shape figures: the trailing updates move their FP64 C block in and out once,
+# e.g. 1.9 GB for a 16000 x 16000 lower triangle).
+OZ_TRAFFIC_PER_LAUNCH = {16384: 8.191e7}
+OZ_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum "
+                     "-k regex:oz_gemm (1 pass), mean over the 579 launches of one n = 16384 step")
 
 
 def theta_sequence(k):
