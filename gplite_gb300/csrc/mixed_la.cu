@@ -46,7 +46,10 @@ struct SplitBuf {
   }
 };
 
-constexpr int64_t NBO = 256;  // outer panel width of the mixed Cholesky
+#ifndef GPGP_NBO
+#define GPGP_NBO 256
+#endif
+constexpr int64_t NBO = GPGP_NBO;  // outer panel width of the mixed Cholesky (a build-time tuning knob)
 // Lookahead: a trailing update of at least LOOK_MIN_ROWS rows leaves LOOK_PANEL_SMS
 // SMs to the next panel's factorisation, whose GEMMs are capped to them.
 constexpr int64_t LOOK_MIN_ROWS = 6144;
