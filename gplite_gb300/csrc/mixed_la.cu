@@ -4,11 +4,12 @@
 // FP64 routines of dense.cu; only the contractions change precision (products
 // of 32-bit fixed-point row slices, accumulated exactly, summed in FP64).
 //
-// Cholesky is two-level right-looking: 256-wide outer panels, each factored
-// with the 64-wide FP64 diagonal kernel of dense.cu, a sliced GEMM for the
-// panel solve L21 = A21 W11^T and sliced GEMMs for the updates inside the
-// panel; one sliced SYRK with K = 256 then updates the trailing matrix, so
-// every trailing element is rewritten in FP64 once per 256 columns.
+// Cholesky is two-level right-looking: outer panels of NBO columns (384: faster
+// at n = 16384 than 256 or 512), each factored with the 64-wide FP64 diagonal
+// kernel of dense.cu, a sliced GEMM for the panel solve L21 = A21 W11^T and
+// sliced GEMMs for the updates inside the panel; one sliced SYRK with K = NBO
+// then updates the trailing matrix, so every trailing element is rewritten in
+// FP64 once per outer panel.
 #include <math.h>
 
 #include <algorithm>
@@ -47,7 +48,7 @@ struct SplitBuf {
 };
 
 #ifndef GPGP_NBO
-#define GPGP_NBO 256
+#define GPGP_NBO 384
 #endif
 constexpr int64_t NBO = GPGP_NBO;  // outer panel width of the mixed Cholesky (a build-time tuning knob)
 // Lookahead: a trailing update of at least LOOK_MIN_ROWS rows leaves LOOK_PANEL_SMS
