@@ -716,9 +716,9 @@ gpgp_status gpgp_create(gpgp_ctx **out, int device) {
     c->device = device;
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking));
-    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming));
-    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.a, cudaEventDisableTiming));
-    GPGP_CUDA(cudaEventCreateWithFlags(&c->side.l, cudaEventDisableTiming));
+    GPGP_CUDA(cudaStreamCreateWithFlags(&c->side.s2, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&c->side.fork, &c->side.a, &c->side.l, &c->side.c, &c->side.b})
+      GPGP_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     GPGP_CUDA(cudaMallocHost((void **)&c->h_pinned, 64 * sizeof(double)));
     return GPGP_OK;
   });
@@ -733,11 +733,12 @@ gpgp_status gpgp_destroy(gpgp_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
   }
-  if (ctx->side.s) {
-    cudaStreamSynchronize(ctx->side.s);
-    cudaStreamDestroy(ctx->side.s);
-  }
-  for (cudaEvent_t e : {ctx->side.fork, ctx->side.a, ctx->side.l})
+  for (cudaStream_t x : {ctx->side.s, ctx->side.s2})
+    if (x) {
+      cudaStreamSynchronize(x);
+      cudaStreamDestroy(x);
+    }
+  for (cudaEvent_t e : {ctx->side.fork, ctx->side.a, ctx->side.l, ctx->side.c, ctx->side.b})
     if (e) cudaEventDestroy(e);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   delete ctx;

@@ -269,11 +269,12 @@ struct OzGridCap {
   ~OzGridCap() { tl_oz_grid_cap = old; }
 };
 int oz_sms();  // SMs of the current device
-// A second stream with three events, owned by a context, for work that runs
-// beside its main stream.
+// Two more streams with their events, owned by a context, for work that runs
+// beside its main stream (the mixed Cholesky: s factors the diagonal chain of the
+// next panel, s2 the panel's rows below it).
 struct SideStream {
-  cudaStream_t s = nullptr;
-  cudaEvent_t fork = nullptr, a = nullptr, l = nullptr;
+  cudaStream_t s = nullptr, s2 = nullptr;
+  cudaEvent_t fork = nullptr, a = nullptr, l = nullptr, c = nullptr, b = nullptr;
 };
 // Batched versions: problem z uses P + z sP and the split's batch strides (set
 // bstride_ex / bstride_sl before splitting); C + z sC; status + z status_bs.

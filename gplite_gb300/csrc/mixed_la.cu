@@ -20,11 +20,13 @@
 
 namespace gpgp {
 
-// potrf_diag_kernel lives in dense.cu
+// potrf_diag_kernel and potrf_panel_inv_kernel live in dense.cu
 __global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                   double *__restrict__ Winv, double *__restrict__ logdet_part,
                                   int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
                                   int64_t sL);
+__global__ void potrf_panel_inv_kernel(double *__restrict__ A21, int64_t m, int kb, int64_t lda,
+                                       const double *__restrict__ W, const int *__restrict__ status);
 
 namespace {
 
@@ -56,34 +58,60 @@ constexpr int64_t NBO = GPGP_NBO;  // outer panel width of the mixed Cholesky (a
 constexpr int64_t LOOK_MIN_ROWS = 6144;
 constexpr int LOOK_PANEL_SMS = 32;
 
-// The 64-wide blocks of the outer panel [k0, k0 + kbo): FP64 factor and inverse of
-// the diagonal block, L21 = A21 W^T for every row below it (sliced GEMM), then the
-// update of the panel's remaining columns.
-void factor_panel(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv, double *logdet_part,
-                  int *status, int *err, int64_t k0, int64_t kbo, SplitBuf &a, SplitBuf &w) {
-  for (int64_t j0 = k0; j0 < k0 + kbo; j0 += NB) {
-    const int jb = (int)std::min<int64_t>(NB, k0 + kbo - j0);
+// The 64-wide blocks of the outer panel [k0, k0 + kbo). Only the panel's own rows
+// lie on the chain from one diagonal block to the next, so they are kept apart:
+//  - chain (stream x): the FP64 factor and inverse W of the diagonal block, the
+//    block's rows inside the panel L_p = A_p W^T (FP64, by the inverse), and the
+//    FP64 update of the rest of the panel's lower triangle by them;
+//  - bulk (stream y, after the chain's block): the rows below the panel,
+//    L_b = A_b W^T, and their update of the panel's remaining columns
+//    A_b,rest -= L_b L_p^T, both sliced GEMMs.
+// x and y may be the same stream (the single-stream schedule; same products in
+// the same order, so the same factor). With two streams the bulk GEMMs take no
+// status word: the chain's diagonal kernels may set it while they run.
+void factor_panel(cudaStream_t x, cudaStream_t y, const SideStream *sd, double *A, int64_t n, int64_t lda,
+                  double *Winv, double *logdet_part, int *status, int *err, int64_t k0, int64_t kbo, SplitBuf &a,
+                  SplitBuf &w, SplitBuf &lp) {
+  const bool two = x != y;
+  const int64_t pend = k0 + kbo;  // first row / column after the panel
+  const int64_t mb = n - pend;    // rows below the panel
+  for (int64_t j0 = k0; j0 < pend; j0 += NB) {
+    const int jb = (int)std::min<int64_t>(NB, pend - j0);
     const int64_t blk = j0 / NB;
     double *Wb = Winv + blk * NB * NB;
     {
-      KTScope kts(GPGP_KPROF_POTRF_DIAG, s, 2.0 * jb * jb * jb / 3);
-      potrf_diag_kernel<<<1, DIAG_THREADS, 0, s>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0, 0, 0);
+      KTScope kts(GPGP_KPROF_POTRF_DIAG, x, 2.0 * jb * jb * jb / 3);
+      potrf_diag_kernel<<<1, DIAG_THREADS, 0, x>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0,
+                                                   0, 0);
     }
     GPGP_CHECK_LAUNCH();
-    const int64_t m = n - j0 - jb;
-    if (m <= 0) continue;
-    double *A21 = A + (j0 + jb) + j0 * lda;
-    // L21 = A21 W^T (W = L11^-1): sliced GEMM, result written over A21
-    oz_split(s, A21, lda, 0, m, jb, &a.sp);
-    oz_split(s, Wb, NB, 0, jb, jb, &w.sp);
-    oz_gemm(s, a.sp, 0, w.sp, 0, m, jb, 0, 1, 0, 1.0, 0.0, A21, lda, false, err, status);
-    // update of the remaining columns of this outer panel
-    const int64_t nc = k0 + kbo - (j0 + jb);
-    if (nc > 0) {
-      oz_split(s, A21, lda, 0, m, jb, &a.sp);
-      oz_gemm(s, a.sp, 0, a.sp, 0, m, nc, 0, 1, 0, -1.0, 1.0, A + (j0 + jb) + (j0 + jb) * lda, lda,
-              true, err, status);
+    const int64_t mp = pend - (j0 + jb);  // panel rows below the block
+    double *Ap = A + (j0 + jb) + j0 * lda;
+    if (mp > 0) {
+      potrf_panel_inv_kernel<<<(unsigned)((mp + 3) / 4), 256, 0, x>>>(Ap, mp, jb, lda, Wb, status);
+      GPGP_CHECK_LAUNCH();
     }
+    if (two) {
+      GPGP_CUDA(cudaEventRecord(sd->c, x));
+      GPGP_CUDA(cudaStreamWaitEvent(y, sd->c, 0));
+    }
+    if (mp > 0)
+      gemm64(x, false, true, mp, mp, jb, -1.0, Ap, lda, Ap, lda, 1.0, A + (j0 + jb) + (j0 + jb) * lda, lda, true, 0);
+    if (mb <= 0) continue;
+    double *Ab = A + pend + j0 * lda;
+    const int *sst = two ? nullptr : status;
+    oz_split(y, Ab, lda, 0, mb, jb, &a.sp);
+    oz_split(y, Wb, NB, 0, jb, jb, &w.sp);
+    oz_gemm(y, a.sp, 0, w.sp, 0, mb, jb, 0, 1, 0, 1.0, 0.0, Ab, lda, false, err, sst);
+    if (mp > 0) {
+      oz_split(y, Ab, lda, 0, mb, jb, &a.sp);
+      oz_split(y, Ap, lda, 0, mp, jb, &lp.sp);
+      oz_gemm(y, a.sp, 0, lp.sp, 0, mb, mp, 0, 1, 0, -1.0, 1.0, A + pend + (j0 + jb) * lda, lda, false, err, sst);
+    }
+  }
+  if (two) {  // the panel is complete on x once the bulk is
+    GPGP_CUDA(cudaEventRecord(sd->b, y));
+    GPGP_CUDA(cudaStreamWaitEvent(x, sd->b, 0));
   }
 }
 
@@ -93,6 +121,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
                  double *logdet_part, int *status, int *err, const SideStream *side) {
   SplitBuf a(s, n, NBO);   // panel operand (rows below the current block)
   SplitBuf w(s, NB, NB);   // inverse of the diagonal block
+  SplitBuf lp(s, NBO, NB);  // the block's rows inside the panel
   cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
   GPGP_CUDA(cudaStreamIsCapturing(s, &cap_st));
   // Per-kernel timers (tl_kt) time each launch alone, so a profiled call runs the
@@ -100,7 +129,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
   if (!side || !side->s || n <= 2 * NBO || cap_st != cudaStreamCaptureStatusNone || tl_kt) {
     for (int64_t k0 = 0; k0 < n; k0 += NBO) {
       const int64_t kbo = std::min<int64_t>(NBO, n - k0);
-      factor_panel(s, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w);
+      factor_panel(s, s, nullptr, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, lp);
       const int64_t m2 = n - k0 - kbo;
       if (m2 > 0) {
         double *P = A + (k0 + kbo) + k0 * lda;
@@ -126,6 +155,10 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
     const SideStream *sd;
     cudaStream_t main;
     ~Join() {
+      if (sd->s2) {  // the bulk stream first (an error may leave the panel loop early)
+        cudaEventRecord(sd->b, sd->s2);
+        cudaStreamWaitEvent(sd->s, sd->b, 0);
+      }
       cudaEventRecord(sd->l, sd->s);
       cudaStreamWaitEvent(main, sd->l, 0);
     }
@@ -136,7 +169,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
     const int64_t kbo = std::min<int64_t>(NBO, n - k0);
     {
       OzGridCap cap(panel_cap);
-      factor_panel(x, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w);
+      factor_panel(x, side->s2 ? side->s2 : x, side, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, lp);
     }
     GPGP_CUDA(cudaEventRecord(side->l, x));
     GPGP_CUDA(cudaStreamWaitEvent(s, side->l, 0));
