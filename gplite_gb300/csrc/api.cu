@@ -714,6 +714,17 @@ gpgp_status gpgp_create(gpgp_ctx **out, int device) {
     if (device < 0 || device >= ndev) return fail(nullptr, GPGP_EINVAL, "no such CUDA device");
     GPGP_CUDA(cudaSetDevice(device));
     c->device = device;
+    {
+      // keep up to a quarter of the device's memory in the pool between fits
+      cudaMemPool_t pool;
+      GPGP_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+      uint64_t cur = 0;
+      GPGP_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur));
+      size_t freeb = 0, total = 0;
+      GPGP_CUDA(cudaMemGetInfo(&freeb, &total));
+      uint64_t want = (uint64_t)total / 4;
+      if (cur < want) GPGP_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &want));
+    }
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking));
     GPGP_CUDA(cudaStreamCreateWithFlags(&c->side.s2, cudaStreamNonBlocking));

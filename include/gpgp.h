@@ -42,7 +42,7 @@ typedef enum gpgp_status {
   GPGP_ENOT_PD = 1,       /* Cholesky met a non-positive pivot (see result.info) */
   GPGP_ENAN = 2,          /* NaN/Inf in inputs or in site parameters */
   GPGP_EMAXITER = 3,      /* iteration limit reached (Laplace / EP) */
-  GPGP_EUNSUPPORTED = 4,  /* combination not implemented (e.g. non-log-concave branch) */
+  GPGP_EUNSUPPORTED = 4,  /* combination not available (e.g. EP with method_rf, as in the reference) */
   GPGP_EOOM = 5,          /* device allocation failed or budget exceeded */
   GPGP_ETIMEOUT = 6,      /* a bounded device wait ran out */
   GPGP_ECUDA = 7,         /* CUDA runtime error (message in gpgp_last_error) */
@@ -179,9 +179,14 @@ typedef struct gpgp_ctx gpgp_ctx;
 typedef struct gpgp_model gpgp_model;
 
 /* ---- context ---------------------------------------------------------- */
-/* A context owns a CUDA stream (all its work is ordered on it) and a side
-   stream that the mixed-precision Cholesky uses for its lookahead; calls on one
-   context must not overlap, separate contexts may run from separate threads. */
+/* A context owns a CUDA stream (all its work is ordered on it) and two side
+   streams that the mixed-precision Cholesky uses for its lookahead; calls on one
+   context must not overlap, separate contexts may run from separate threads.
+   Device memory comes from the device's default stream-ordered pool; creating a
+   context raises that pool's release threshold to a quarter of the device's
+   memory (when it is lower), so that memory freed at the end of a fit is reused
+   by the next one instead of being unmapped at every synchronisation and mapped
+   again. The setting belongs to this process and ends with it. */
 gpgp_status gpgp_create(gpgp_ctx **ctx, int device);
 gpgp_status gpgp_destroy(gpgp_ctx *ctx);
 const char *gpgp_status_string(gpgp_status s);
