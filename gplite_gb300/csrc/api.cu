@@ -215,9 +215,12 @@ void refine_alpha(gpgp_model *m, Work &w, double *alpha, double *fnew, int iters
 // (optional): w.flags[0] read back with the factorisation status in the same
 // synchronisation; a set site flag (NaN or V <= 0) makes the result void, and no
 // FP64 retry is made for it.
+// hstatus_defer (optional, pinned host memory, FP64 only): the status and the
+// flags (into hflags, pinned too) are copied without a synchronisation and 0 is
+// returned; the caller reads both after its next one.
 int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alpha,
                          double *fnew, double *logdetL, bool force_fp64 = false, int refine = -1,
-                         int *hflags = nullptr) {
+                         int *hflags = nullptr, int *hstatus_defer = nullptr) {
   gpgp_ctx *ctx = m->ctx;
   cudaStream_t st = ctx->stream;
   const int64_t n = m->n;
@@ -255,6 +258,13 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   }
   const int64_t nblk = (n + NB - 1) / NB;
   sum_vec(st, w.logdet_part.p, nblk, logdetL);
+  if (hstatus_defer && !mixed) {
+    GPGP_CUDA(cudaMemcpyAsync(hstatus_defer, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (hflags) GPGP_CUDA(cudaMemcpyAsync(hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    m->have_binv_diag = false;
+    m->have_Linv = false;
+    return 0;
+  }
   int hstatus = 0;
   GPGP_CUDA(cudaMemcpyAsync(&hstatus, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (hflags) GPGP_CUDA(cudaMemcpyAsync(hflags, w.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -356,6 +366,12 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
     double diff = 0.0;
     int it = 0;
     bool nlc_iter = false;  // the last iteration took the non-log-concave branch
+    // FP64 Gaussian fit (one iteration, V = sigma^2 > 0): the factorisation's status
+    // and site flags are read with the evidence terms, in one synchronisation
+    const bool defer = m->opts.precision != GPGP_PREC_MIXED && maxiter == 1 &&
+                       m->lik.kind == GPGP_LIK_GAUSSIAN && m->lik.sigma > 0.0;
+    int *hdef = reinterpret_cast<int *>(ctx->h_pinned + 56);  // [0] status, [1] site flags
+    hdef[0] = hdef[1] = 0;
     double nlc_lml = 0.0;
     for (it = 1; it <= maxiter; ++it) {
       lik_pseudodata_la(st, m->lk, n, m->fmean.p, m->y.p, trials, offset, m->z.p, m->V.p);
@@ -370,7 +386,8 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       // flag discards it.
       int hflags = 0;
       const int64_t info = factor_and_solve(m, w, m->z.p, m->alpha.p, fnew.p, logdetL, false,
-                                            (mixed && maxiter > 1) ? 0 : -1, &hflags);
+                                            (mixed && maxiter > 1) ? 0 : -1, defer ? &hdef[1] : &hflags,
+                                            defer ? &hdef[0] : nullptr);
       if (hflags & 2) {  // all(V > 0) is NA in R: an error
         res->status = GPGP_ENAN;
         res->log_evidence = NAN;
@@ -423,6 +440,19 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       double hr[75];
       GPGP_CUDA(cudaMemcpyAsync(hr, red + 100, sizeof(hr), cudaMemcpyDeviceToHost, st));
       GPGP_CUDA(cudaStreamSynchronize(st));
+      if (defer) {
+        if (hdef[1] & 6) {  // NaN sites (non-finite sigma or inputs)
+          res->status = GPGP_ENAN;
+          res->log_evidence = NAN;
+          return fail(ctx, GPGP_ENAN, "NaN in the Laplace pseudo-data");
+        }
+        if (hdef[0] != 0) {
+          res->status = GPGP_ENOT_PD;
+          res->info = hdef[0];
+          res->log_evidence = -INFINITY;
+          return fail(ctx, GPGP_ENOT_PD, "Cholesky factorisation: matrix is not positive definite");
+        }
+      }
       const double ll = hr[1], fa = hr[74], ld = hr[0];
       m->log_evidence = ll - 0.5 * fa - 0.5 * (2.0 * ld);
     }
@@ -617,24 +647,24 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   GPGP_CUDA(cudaMemsetAsync(m->errflag.p, 0, sizeof(int), s));
   copy_in(s, m->x, x, (size_t)n * d, on_device);
   copy_in(s, m->y, y, n, on_device);
-  {
-    // NaN or Inf in x or y: an error here rather than NaN evidences further on
-    IBuf bad;
-    bad.alloc(s, 1);
-    GPGP_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
-    nonfinite_kernel<<<g1((int64_t)n * d), 256, 0, s>>>((int64_t)n * d, m->x.p, bad.p);
-    GPGP_CHECK_LAUNCH();
-    nonfinite_kernel<<<g1(n), 256, 0, s>>>(n, m->y.p, bad.p);
-    GPGP_CHECK_LAUNCH();
-    int hb = 0;
-    GPGP_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GPGP_CUDA(cudaStreamSynchronize(s));
-    if (hb) {
-      result->status = GPGP_ENAN;
-      result->log_evidence = NAN;
-      return fail(ctx, GPGP_ENAN, "x or y holds NaN or Inf");
-    }
-  }
+  // NaN or Inf in x or y: an error rather than NaN evidences. The flag travels to
+  // pinned host memory with the fit and is read after the fit's next
+  // synchronisation (the fit's result is discarded when it is set).
+  IBuf bad;
+  bad.alloc(s, 1);
+  GPGP_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  nonfinite_kernel<<<g1((int64_t)n * d), 256, 0, s>>>((int64_t)n * d, m->x.p, bad.p);
+  GPGP_CHECK_LAUNCH();
+  nonfinite_kernel<<<g1(n), 256, 0, s>>>(n, m->y.p, bad.p);
+  GPGP_CHECK_LAUNCH();
+  int *hflags = reinterpret_cast<int *>(ctx->h_pinned + 60);  // [0] inputs non-finite, [1] device wait timed out
+  hflags[0] = 0;
+  GPGP_CUDA(cudaMemcpyAsync(&hflags[0], bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  auto nan_inputs = [&]() -> gpgp_status {
+    result->status = GPGP_ENAN;
+    result->log_evidence = NAN;
+    return fail(ctx, GPGP_ENAN, "x or y holds NaN or Inf");
+  };
   if (trials) {
     copy_in(s, m->trials, trials, n, on_device);
     m->has_trials = true;
@@ -665,11 +695,15 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
   }
   if (st != GPGP_OK) {
     GPGP_CUDA(cudaStreamSynchronize(s));
+    if (hflags[0]) return nan_inputs();
     return st;
   }
-  if (tc_error(m.get())) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
-  m->fitted = 1;
+  hflags[1] = 0;
+  GPGP_CUDA(cudaMemcpyAsync(&hflags[1], m->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   GPGP_CUDA(cudaStreamSynchronize(s));
+  if (hflags[0]) return nan_inputs();
+  if (hflags[1]) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
+  m->fitted = 1;
   *model = m.release();
   return GPGP_OK;
 }

@@ -807,11 +807,71 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const double *__restrict
   }
 }
 
+// Small solves (n <= 512): one CTA walks the row blocks in order (a launch and a
+// 64-row step cost less than the flags of the multi-CTA version at this size).
+// Thread (r, p) sums the earlier (later, when transposed) blocks' columns
+// c = p mod 4 for row r of the block; the block's inverse then gives x_blk.
+__global__ void __launch_bounds__(256) trsv_small_kernel(const double *__restrict__ L, int64_t n, int64_t lda,
+                                                         const double *__restrict__ Winv,
+                                                         const double *__restrict__ b, double *__restrict__ x,
+                                                         int trans, const int *__restrict__ status) {
+  __shared__ double xs[8 * NB];
+  __shared__ double vs[NB];
+  __shared__ double red[4][NB + 1];
+  if (*(volatile const int *)status != 0) return;
+  const int tid = threadIdx.x, r = tid & 63, p = tid >> 6;
+  const int nblk = (int)((n + NB - 1) / NB);
+  for (int st = 0; st < nblk; ++st) {
+    const int blk = trans ? nblk - 1 - st : st;
+    const int k0 = blk * NB;
+    const int kb = (int)(n - k0 < NB ? n - k0 : NB);
+    double acc = 0.0;
+    if (r < kb) {
+      if (!trans)
+        for (int c = p; c < k0; c += 4) acc = fma(L[(k0 + r) + (int64_t)c * lda], xs[c], acc);
+      else
+        for (int c = k0 + kb + p; c < n; c += 4) acc = fma(L[c + (int64_t)(k0 + r) * lda], xs[c], acc);
+    }
+    red[p][r] = acc;
+    __syncthreads();
+    if (tid < NB) vs[tid] = tid < kb ? b[k0 + tid] - (((red[0][tid] + red[1][tid]) + red[2][tid]) + red[3][tid]) : 0.0;
+    __syncthreads();
+    if (tid < kb) {
+      const double *W = Winv + (int64_t)blk * NB * NB;
+      double s0 = 0.0, s1 = 0.0;
+      if (!trans) {
+        int c = 0;
+        for (; c + 1 <= tid; c += 2) {
+          s0 = fma(W[tid + c * NB], vs[c], s0);
+          s1 = fma(W[tid + (c + 1) * NB], vs[c + 1], s1);
+        }
+        if (c <= tid) s0 = fma(W[tid + c * NB], vs[c], s0);
+      } else {
+        int rr = tid;
+        for (; rr + 1 < kb; rr += 2) {
+          s0 = fma(W[rr + tid * NB], vs[rr], s0);
+          s1 = fma(W[rr + 1 + tid * NB], vs[rr + 1], s1);
+        }
+        if (rr < kb) s0 = fma(W[rr + tid * NB], vs[rr], s0);
+      }
+      xs[k0 + tid] = s0 + s1;
+      x[k0 + tid] = s0 + s1;
+    }
+    __syncthreads();
+  }
+}
+
 void trsv_flow(cudaStream_t s, const double *L, int64_t n, int64_t lda, const double *Winv, const double *b,
                double *x, bool trans, const int *status, unsigned *sync, int *err) {
   if (n <= 0) return;
   const int g_sms = device_sms();
   const int64_t nblk = (n + NB - 1) / NB;
+  if (nblk <= 8) {
+    KTScope kts(GPGP_KPROF_TRSV, s, (double)n * (double)n);
+    trsv_small_kernel<<<1, 256, 0, s>>>(L, n, lda, Winv, b, x, trans ? 1 : 0, status);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
   GPGP_CUDA(cudaMemsetAsync(sync, 0, (size_t)(nblk + 1) * sizeof(unsigned), s));
   const unsigned grid = (unsigned)std::min<int64_t>(nblk, g_sms);
   KTScope kts(GPGP_KPROF_TRSV, s, (double)n * (double)n);
