@@ -72,10 +72,10 @@ class BatchPlan:
         self.lib.gpgp_batch_info(self.h, C.byref(nb), None, None, None, None)
         k = nb.value
         bn, bc, bv = (C.c_int32 * k)(), (C.c_int32 * k)(), (C.c_int32 * k)()
-        tms = (C.c_double * 2)()
+        tms = (C.c_double * 3)()
         self.lib.gpgp_batch_info(self.h, C.byref(nb), bn, bc, bv, tms)
-        return dict(buckets=[(bn[i], bc[i], "fp64-pipe" if bv[i] == 0 else "tensor") for i in range(k)],
-                    autotune_ms=list(tms))
+        names = {0: "fp64-pipe", 1: "tensor-64", 2: "tensor-256"}
+        return dict(buckets=[(bn[i], bc[i], names[bv[i]]) for i in range(k)], autotune_ms=list(tms))
 
     def close(self):
         if getattr(self, "h", None):

@@ -43,7 +43,7 @@ struct Bucket {
   // sliced operands of the tensor-core variant
   void *sa = nullptr, *sb = nullptr;
   OzSplit SA, SB;
-  int variant = 0;  // 0: FP64 pipe, 1: sliced tensor cores
+  int variant = 0;  // 0: FP64 pipe; sliced tensor cores with 1: 64-wide, 2: 256-wide outer panels
   ~Bucket() {
     if (sa) cudaFreeAsync(sa, X.s);
     if (sb) cudaFreeAsync(sb, X.s);
@@ -366,7 +366,7 @@ struct gpgp_batch {
   IBuf err;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  double tune_ms[2] = {0, 0};
+  double tune_ms[3] = {0, 0, 0};  // autotuning time per variant
   int64_t graph_kernels = 0;  // kernel nodes of the captured graph
   ~gpgp_batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -396,7 +396,7 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
     const int64_t T = nb / BT;
     dim3 g((unsigned)(T * (T + 1) / 2), (unsigned)P);
     bat_cov_B_kernel<<<g, 256, 0, st>>>(nb, k.dm, k.X.p, k.prm.p, b->jitter, k.Bm.p,
-                                        k.variant == 1 ? k.Bc.p : nullptr);
+                                        k.variant >= 1 ? k.Bc.p : nullptr);
     GPGP_CHECK_LAUNCH();
   }
   {
@@ -408,28 +408,47 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
   if (k.variant == 0) {
     potrf_batched(st, k.Bm.p, nb, nb, nb * nb, k.Winv.p, nb * NB, k.ldp.p, nbl, k.status.p, P);
   } else {
-    for (int64_t k0 = 0, blk = 0; k0 < nb; k0 += NB, ++blk) {
-      double *Akk = k.Bm.p + k0 + k0 * nb;
-      {
-        KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
-        potrf_diag_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB, k.ldp.p + blk,
-                                                       k.status.p, k0, nb * nb, nb * NB, nbl);
+    // tensor variants: outer panels of 64 (variant 1: a trailing update after every
+    // diagonal block, K = 64) or 256 columns (variant 2: the panel's blocks update
+    // the rest of the panel, then one trailing update with K = 256)
+    const int64_t outer = k.variant == 2 ? 4 * NB : NB;
+    for (int64_t k0 = 0; k0 < nb; k0 += outer) {
+      const int64_t kbo = std::min<int64_t>(outer, nb - k0);
+      for (int64_t j0 = k0; j0 < k0 + kbo; j0 += NB) {
+        const int64_t blk = j0 / NB;
+        double *Akk = k.Bm.p + j0 + j0 * nb;
+        {
+          KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
+          potrf_diag_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB,
+                                                                  k.ldp.p + blk, k.status.p, j0, nb * nb, nb * NB,
+                                                                  nbl);
+        }
+        GPGP_CHECK_LAUNCH();
+        const int64_t m = nb - j0 - NB;
+        if (m <= 0) continue;
+        double *A21 = k.Bm.p + (j0 + NB) + j0 * nb;
+        // L21 = A21 W^T
+        oz_split_batched(st, A21, nb, nb * nb, 0, m, NB, &k.SA, P);
+        oz_split_batched(st, k.Winv.p + blk * NB * NB, NB, nb * NB, 0, NB, NB, &k.SB, P);
+        oz_gemm_batched(st, k.SA, 0, k.SB, 0, m, NB, 0, 1, 0, 1.0, 0.0, A21, nb, nb * nb, false, b->err.p,
+                        k.status.p, 1, P);
+        // the rest of this outer panel's columns
+        const int64_t nc = k0 + kbo - (j0 + NB);
+        if (nc > 0) {
+          oz_split_batched(st, A21, nb, nb * nb, 0, m, NB, &k.SA, P);
+          oz_gemm_batched(st, k.SA, 0, k.SA, 0, m, nc, 0, 1, 0, -1.0, 1.0, k.Bm.p + (j0 + NB) * (1 + nb), nb,
+                          nb * nb, true, b->err.p, k.status.p, 1, P);
+        }
       }
-      GPGP_CHECK_LAUNCH();
-      const int64_t m = nb - k0 - NB;
-      if (m <= 0) continue;
-      double *A21 = k.Bm.p + (k0 + NB) + k0 * nb;
-      // L21 = A21 W^T, then the trailing update with the refreshed panel
-      oz_split_batched(st, A21, nb, nb * nb, 0, m, NB, &k.SA, P);
-      oz_split_batched(st, k.Winv.p + blk * NB * NB, NB, nb * NB, 0, NB, NB, &k.SB, P);
-      oz_gemm_batched(st, k.SA, 0, k.SB, 0, m, NB, 0, 1, 0, 1.0, 0.0, A21, nb, nb * nb, false, b->err.p,
-                      k.status.p, 1, P);
-      oz_split_batched(st, A21, nb, nb * nb, 0, m, NB, &k.SA, P);
-      oz_gemm_batched(st, k.SA, 0, k.SA, 0, m, m, 0, 1, 0, -1.0, 1.0, k.Bm.p + (k0 + NB) * (1 + nb), nb,
+      // trailing update with the finished outer panel
+      const int64_t m2 = nb - k0 - kbo;
+      if (m2 <= 0) continue;
+      oz_split_batched(st, k.Bm.p + (k0 + kbo) + k0 * nb, nb, nb * nb, 0, m2, kbo, &k.SA, P);
+      oz_gemm_batched(st, k.SA, 0, k.SA, 0, m2, m2, 0, kbo / NB, 0, -1.0, 1.0, k.Bm.p + (k0 + kbo) * (1 + nb), nb,
                       nb * nb, true, b->err.p, k.status.p, 1, P);
     }
   }
-  bat_solve_kernel<<<(unsigned)P, 256, 0, st>>>(nb, k.Bm.p, k.Winv.p, k.variant == 1 ? k.Bc.p : nullptr,
+  bat_solve_kernel<<<(unsigned)P, 256, 0, st>>>(nb, k.Bm.p, k.Winv.p, k.variant >= 1 ? k.Bc.p : nullptr,
                                                 kRefine, k.Y.p, k.prm.p, k.status.p, k.tmp.p, k.tmp.p + P * nb,
                                                 k.tmp.p + 2 * P * nb, k.alpha.p, k.fhat.p);
   GPGP_CHECK_LAUNCH();
@@ -652,7 +671,7 @@ gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, in
     GPGP_CUDA(cudaEventCreate(&e1));
     for (auto &kp : b->buckets) {
       Bucket &k = *kp;
-      const int nvar = precision == GPGP_PREC_MIXED ? 2 : 1;
+      const int nvar = precision == GPGP_PREC_MIXED ? 3 : 1;
       float best = 1e30f;
       int bestv = 0;
       for (int v = 0; v < nvar; ++v) {
@@ -780,10 +799,8 @@ gpgp_status gpgp_batch_info(gpgp_batch *b, int32_t *nbuckets, int32_t *bucket_n,
     if (bucket_count) bucket_count[g] = (int32_t)b->buckets[g]->count;
     if (bucket_variant) bucket_variant[g] = b->buckets[g]->variant;
   }
-  if (tune_ms) {
-    tune_ms[0] = b->tune_ms[0];
-    tune_ms[1] = b->tune_ms[1];
-  }
+  if (tune_ms)
+    for (int v = 0; v < 3; ++v) tune_ms[v] = b->tune_ms[v];
   return GPGP_OK;
 }
 
