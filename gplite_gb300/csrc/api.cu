@@ -346,11 +346,30 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
   m->fmean.alloc(st, n);
   m->z.alloc(st, n);
   m->V.alloc(st, n);
-  // K = eval_cf(x, x) + jitter I, stored in full (R/gp_fit.R:91-96)
+  // K = eval_cf(x, x) + jitter I, stored in full (R/gp_fit.R:91-96). When the
+  // energy gradient follows (gpgp_fit_grad), the same pass writes K's derivative
+  // matrices, so the gradient does not evaluate the kernel a second time: for
+  // matrices of at least as many 64-tiles as SMs, while they take at most half
+  // of the free device memory.
   {
     Phase ph(ctx, GPGP_PHASE_COV);
-    cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
-               m->opts.jitter, nullptr);
+    m->dK.reset();
+    m->have_dK = false;
+    const int64_t T = (n + NB - 1) / NB;
+    if (m->want_dk && T * (T + 1) / 2 >= device_sms() && plan_grad_store(m->dk, &m->gplan) &&
+        m->gplan.m.nmat > 0) {
+      size_t fr = 0, tot = 0;
+      GPGP_CUDA(cudaMemGetInfo(&fr, &tot));
+      const size_t need = (size_t)m->gplan.m.nmat * n * n * sizeof(double);
+      if (need <= fr / 2) {
+        m->dK.alloc(st, (size_t)m->gplan.m.nmat * n * n);
+        cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
+        m->have_dK = true;
+      }
+    }
+    if (!m->have_dK)
+      cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
+                 m->opts.jitter, nullptr);
   }
   double *red = w.red.p;  // [0..63] partials, [64] result, [100..] scalars
   double *logdetL = red + 100;
@@ -691,6 +710,7 @@ gpgp_status fit_common(gpgp_ctx *ctx, const gpgp_kernel *k, const gpgp_lik *lik,
     st = fit_fitc(m.get(), result, method->inducing, on_device);
   } else {
     m->want_linv = want_grad && lik->kind == GPGP_LIK_GAUSSIAN && opts->precision == GPGP_PREC_MIXED;
+    m->want_dk = want_grad && lik->kind == GPGP_LIK_GAUSSIAN;
     st = fit_full(m.get(), result);
   }
   if (st != GPGP_OK) {
@@ -1287,23 +1307,42 @@ gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_
     red.alloc(s, 256);
     sum_vec(s, dg.p, n, red.p + 200);
     dot_partial(s, n, m->alpha.p, m->alpha.p, red.p);
-    dim3 gg((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
-    grad_w_kernel<<<gg, 256, 0, s>>>(n, m->alpha.p, m->s.p, Bi.p);
-    GPGP_CHECK_LAUNCH();
-    part.alloc(s, cov_grad_partials(n));
-    g.alloc(s, GPGP_MAX_TERMS * GPGP_TERM_NPARAM);
-    gpgp_status st;
-    {
-      Phase ph(ctx, GPGP_PHASE_GRAD);
-      st = cov_grad_contract(s, m->dk, m->F.p, n, n, Bi.p, n, part.p, g.p);
-    }
-    if (st != GPGP_OK) return fail(ctx, st, "gradient contraction failed");
     std::vector<double> hg(m->dk.nterms * GPGP_TERM_NPARAM);
-    GPGP_CUDA(cudaMemcpyAsync(hg.data(), g.p, hg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     double h2[2];
-    GPGP_CUDA(cudaMemcpyAsync(&h2[0], red.p + 200, sizeof(double), cudaMemcpyDeviceToHost, s));
-    GPGP_CUDA(cudaMemcpyAsync(&h2[1], red.p + 64, sizeof(double), cudaMemcpyDeviceToHost, s));
-    GPGP_CUDA(cudaStreamSynchronize(s));
+    if (m->have_dK) {
+      // the derivative matrices written with K: one pass over Binv and them, with
+      // alpha alpha^T - diag(s) Binv diag(s) formed on the fly
+      part.alloc(s, grad_stored_partials(n));
+      g.alloc(s, GPGP_GRAD_MAXMAT + 1);
+      {
+        Phase ph(ctx, GPGP_PHASE_GRAD);
+        grad_stored_contract(s, m->gplan, n, Bi.p, n, m->alpha.p, m->s.p, m->dK.p, n, (int64_t)n * n, part.p, g.p);
+      }
+      double hs[GPGP_GRAD_MAXMAT + 1];
+      GPGP_CUDA(cudaMemcpyAsync(hs, g.p, (m->gplan.m.nmat + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(&h2[0], red.p + 200, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(&h2[1], red.p + 64, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaStreamSynchronize(s));
+      grad_stored_assemble(m->gplan, m->dk.nterms, hs, hg.data());
+      m->dK.reset();  // made for this fit's gradient only
+      m->have_dK = false;
+    } else {
+      dim3 gg((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(n, 65535));
+      grad_w_kernel<<<gg, 256, 0, s>>>(n, m->alpha.p, m->s.p, Bi.p);
+      GPGP_CHECK_LAUNCH();
+      part.alloc(s, cov_grad_partials(n));
+      g.alloc(s, GPGP_MAX_TERMS * GPGP_TERM_NPARAM);
+      gpgp_status st;
+      {
+        Phase ph(ctx, GPGP_PHASE_GRAD);
+        st = cov_grad_contract(s, m->dk, m->F.p, n, n, Bi.p, n, part.p, g.p);
+      }
+      if (st != GPGP_OK) return fail(ctx, st, "gradient contraction failed");
+      GPGP_CUDA(cudaMemcpyAsync(hg.data(), g.p, hg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(&h2[0], red.p + 200, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(&h2[1], red.p + 64, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaStreamSynchronize(s));
+    }
     if (tc_error(m)) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
     for (size_t i = 0; i < hg.size(); ++i) grad_terms[i] = 0.5 * hg[i];
     if (grad_lik_sigma) {

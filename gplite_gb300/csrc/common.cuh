@@ -161,6 +161,40 @@ gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double 
                               int64_t n, const double *W, int64_t ldw, double *part, double *g);
 int64_t cov_grad_partials(int64_t n);
 
+// Derivative matrices of K written by the covariance pass when the energy
+// gradient follows the fit (cov.cu). Matrix q is the value of product group
+// a[q] (kind 0; every magnitude slot of the group is twice it) or the
+// derivative of K with respect to slot b[q] of term a[q] (kind 1).
+constexpr int GPGP_GRAD_MAXMAT = 8;
+struct GradMats {
+  int nmat;
+  int kind[GPGP_GRAD_MAXMAT];
+  int a[GPGP_GRAD_MAXMAT];
+  int b[GPGP_GRAD_MAXMAT];
+  int grp[GPGP_GRAD_MAXMAT];  // the product group of matrix q
+};
+// slot_mat[t*5 + p]: the slot's matrix (gradient = slot_scale x its sum), -1: a
+// constant derivative (slot_scale x the sum of W), -2: not a parameter.
+struct GradPlan {
+  GradMats m;
+  int slot_mat[GPGP_MAX_TERMS * GPGP_TERM_NPARAM];
+  double slot_scale[GPGP_MAX_TERMS * GPGP_TERM_NPARAM];
+};
+// false: more than GPGP_GRAD_MAXMAT matrices would be needed.
+bool plan_grad_store(const DevKernel &dk, GradPlan *pl);
+// K (n x n, ldk, lower tiles mirrored, jitter on the diagonal) and the planned
+// matrices D + q dstride (ldd; entries i >= j only), 64 x 64 tiles.
+void cov_matrix_grad(cudaStream_t s, const DevKernel &dk, const GradPlan &pl, const double *F, int64_t ldf,
+                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride);
+// g[q] = sum_ij W_ij D_q(i, j), g[nmat] = sum_ij W_ij, with W = alpha alpha^T -
+// diag(s) Binv diag(s) formed on the fly from the lower triangle of Binv.
+void grad_stored_contract(cudaStream_t s, const GradPlan &pl, int64_t n, const double *Bi, int64_t ldb,
+                          const double *alpha, const double *sv, const double *D, int64_t ldd, int64_t dstride,
+                          double *part, double *g);
+int64_t grad_stored_partials(int64_t n);
+// hg[t*5 + p] from the contraction's sums g (host).
+void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, double *hg);
+
 // ---------------------------------------------------------------------------
 // dense FP64 linear algebra (column-major)
 // ---------------------------------------------------------------------------

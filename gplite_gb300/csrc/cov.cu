@@ -623,7 +623,7 @@ __device__ __forceinline__ double term_value_grad(const DevTerm &T, const double
 }
 
 // parameter slots that term_value_grad can set for a term (bit p: slot p)
-__device__ __forceinline__ int term_param_mask(const DevTerm &T) {
+__host__ __device__ __forceinline__ int term_param_mask(const DevTerm &T) {
   switch (T.kind) {
     case GPGP_CF_CONST:
       return 2;
@@ -763,6 +763,285 @@ gpgp_status cov_grad_contract(cudaStream_t s, const DevKernel &dk, const double 
   reduce_partials_kernel<<<1, 256, 0, s>>>(part, nt, dk.nterms * GPGP_TERM_NPARAM, g);
   GPGP_CHECK_LAUNCH();
   return GPGP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// K together with its derivative matrices (the energy gradient follows the fit)
+// ---------------------------------------------------------------------------
+// The gradient contraction above regenerates every derivative tile from the
+// features after the factorisation: the same distances, square roots and
+// exponentials as the covariance, on the FP64 pipe, a second time. When the
+// gradient is known to follow the fit, the covariance pass writes the
+// derivative matrices beside K instead (the extra FP64 work per pair is a few
+// multiplications), and the contraction becomes a stream over W and them.
+//
+// Every magnitude slot of a product group has the derivative 2 x (the group's
+// value), so one matrix per group serves all of them; a group made only of
+// cf_const terms has a constant value and needs none. Every other active slot
+// (lscale, sigma0, sigma, period) gets its own matrix: (the product of the
+// group's other terms) x (the term's derivative).
+bool plan_grad_store(const DevKernel &dk, GradPlan *pl) {
+  std::memset(pl, 0, sizeof(*pl));
+  bool allconst[GPGP_MAX_TERMS];
+  double constprod[GPGP_MAX_TERMS];
+  int gmat[GPGP_MAX_TERMS];
+  for (int g = 0; g < GPGP_MAX_TERMS; ++g) {
+    allconst[g] = true;
+    constprod[g] = 1.0;
+    gmat[g] = -1;
+  }
+  for (int t = 0; t < dk.nterms; ++t) {
+    if (dk.t[t].kind != GPGP_CF_CONST) allconst[dk.t[t].group] = false;
+    constprod[dk.t[t].group] *= dk.t[t].m2;
+  }
+  for (int t = 0; t < dk.nterms; ++t) {
+    const DevTerm &T = dk.t[t];
+    const int mask = term_param_mask(T);
+    for (int p = 0; p < GPGP_TERM_NPARAM; ++p) {
+      const int idx = t * GPGP_TERM_NPARAM + p;
+      pl->slot_mat[idx] = -2;
+      pl->slot_scale[idx] = 0.0;
+      if (!(mask & (1 << p))) continue;
+      if (p == 1) {
+        if (allconst[T.group]) {
+          pl->slot_mat[idx] = -1;  // constant 2 x (product of the group's m^2)
+          pl->slot_scale[idx] = 2.0 * constprod[T.group];
+          continue;
+        }
+        if (gmat[T.group] < 0) {
+          if (pl->m.nmat == GPGP_GRAD_MAXMAT) return false;
+          gmat[T.group] = pl->m.nmat;
+          pl->m.kind[pl->m.nmat] = 0;
+          pl->m.a[pl->m.nmat] = T.group;
+          pl->m.grp[pl->m.nmat] = T.group;
+          pl->m.b[pl->m.nmat] = 0;
+          ++pl->m.nmat;
+        }
+        pl->slot_mat[idx] = gmat[T.group];
+        pl->slot_scale[idx] = 2.0;
+      } else {
+        if (pl->m.nmat == GPGP_GRAD_MAXMAT) return false;
+        pl->m.kind[pl->m.nmat] = 1;
+        pl->m.a[pl->m.nmat] = t;
+        pl->m.grp[pl->m.nmat] = T.group;
+        pl->m.b[pl->m.nmat] = p;
+        pl->slot_mat[idx] = pl->m.nmat++;
+        pl->slot_scale[idx] = 1.0;
+      }
+    }
+  }
+  return true;
+}
+
+// Lower 64 x 64 tiles of K (mirrored, jitter on the diagonal; the same values
+// as cov_tile_kernel) and, for entries i >= j, the planned derivative matrices
+// D + q dstride (leading dimension ldd).
+template <int NT>
+__global__ void __launch_bounds__(256) cov_tile_grad_kernel(DevKernel dk, GradMats gm, const double *__restrict__ F,
+                                                            int64_t ldf, int64_t n, double *__restrict__ K,
+                                                            int64_t ldk, double jitter, double *__restrict__ D,
+                                                            int64_t ldd, int64_t dstride) {
+  extern __shared__ double sm[];
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  double *Fi = sm;
+  double *Fj = sm + CT * lds;
+  double *Tt = sm + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  int64_t bi, bj;
+  tri_index(blockIdx.x, &bi, &bj);
+  const int64_t i0 = bi * CT, j0 = bj * CT;
+  load_feats(Fi, lds, F, ldf, i0, n, nf);
+  load_feats(Fj, lds, F, ldf, j0, n, nf);
+  __syncthreads();
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  const bool do_mirror = bi != bj;
+  double kv[MT];
+  double dv[MT][GPGP_TERM_NPARAM];
+#pragma unroll 1
+  for (int q = 0; q < CT / 4; ++q) {
+    const int c = cb + 4 * q;
+    const int64_t j = j0 + c;
+    double v = 0.0;
+    if (i < n && j < n) {
+#pragma unroll
+      for (int t = 0; t < MT; ++t)
+        if (t < nterms)
+          kv[t] = term_value_grad(dk.t[t], Fi + r * lds + dk.t[t].off, Fj + c * lds + dk.t[t].off, dv[t]);
+      // the sum over groups of the products of their terms, in kernel_value's order
+      double sum = 0.0, prod = 1.0;
+      int g = dk.t[0].group;
+#pragma unroll
+      for (int t = 0; t < MT; ++t) {
+        if (t >= nterms) break;
+        if (dk.t[t].group != g) {
+          sum += prod;
+          prod = 1.0;
+          g = dk.t[t].group;
+        }
+        prod *= kv[t];
+      }
+      sum += prod;
+      v = (i == j) ? sum + jitter : sum;
+      K[i + j * ldk] = v;
+      if (i >= j) {
+#pragma unroll
+        for (int mi = 0; mi < GPGP_GRAD_MAXMAT; ++mi) {
+          if (mi >= gm.nmat) break;
+          const int ga = gm.grp[mi];
+          double val = 1.0, dsel = 0.0;
+#pragma unroll
+          for (int t = 0; t < MT; ++t) {
+            if (t >= nterms) break;
+            if (dk.t[t].group != ga) continue;
+            if (gm.kind[mi] == 1 && t == gm.a[mi]) {
+#pragma unroll
+              for (int p = 0; p < GPGP_TERM_NPARAM; ++p)
+                if (p == gm.b[mi]) dsel = dv[t][p];
+            } else {
+              val *= kv[t];
+            }
+          }
+          if (gm.kind[mi] == 1) val *= dsel;
+          D[mi * dstride + i + j * ldd] = val;
+        }
+      }
+    }
+    if (do_mirror) Tt[c * (CT + 1) + r] = v;
+  }
+  if (do_mirror) {
+    __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < CT / 4; ++q) {
+      const int rr = threadIdx.x % CT;
+      const int cc = threadIdx.x / CT + 4 * q;
+      const int64_t jj = j0 + rr, ii = i0 + cc;
+      if (jj < n && ii < n) K[jj + ii * ldk] = Tt[rr * (CT + 1) + cc];
+    }
+  }
+}
+
+void cov_matrix_grad(cudaStream_t s, const DevKernel &dk, const GradPlan &pl, const double *F, int64_t ldf,
+                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+  if (n == 0) return;
+  const int lds = (dk.nfeat | 1);
+  const size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
+  static PerDevice attr;
+  per_device(attr, [] {
+    const int mx = 2 * CT * 65 * 8 + CT * (CT + 1) * 8;
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return 1;
+  });
+  const int64_t T = (n + CT - 1) / CT;
+  const unsigned nt = (unsigned)(T * (T + 1) / 2);
+  switch (dk.nterms) {
+    case 1:
+      cov_tile_grad_kernel<1><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    case 2:
+      cov_tile_grad_kernel<2><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    case 3:
+      cov_tile_grad_kernel<3><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    default:
+      cov_tile_grad_kernel<0><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+  }
+  GPGP_CHECK_LAUNCH();
+}
+
+// Contraction with the stored matrices. Per lower tile: W_ij = alpha_i alpha_j -
+// s_i s_j Binv_ij (Binv given by its lower triangle, ldb), counted twice off the
+// diagonal; part[tile (nmat + 1) + q] = sum W_ij D_q(i, j) for q < nmat and
+// part[tile (nmat + 1) + nmat] = sum W_ij. Warp-shuffle sums in a fixed order,
+// then the block's eight warps in order.
+template <int NM>
+__global__ void __launch_bounds__(256) grad_stored_kernel(int nmat, const double *__restrict__ Bi, int64_t ldb,
+                                                          int64_t n, const double *__restrict__ alpha,
+                                                          const double *__restrict__ sv, const double *__restrict__ D,
+                                                          int64_t ldd, int64_t dstride, double *__restrict__ part) {
+  constexpr int MM = NM > 0 ? NM : GPGP_GRAD_MAXMAT;
+  const int nm = NM > 0 ? NM : nmat;
+  __shared__ double red[8][MM + 1];
+  int64_t bi, bj;
+  tri_index(blockIdx.x, &bi, &bj);
+  const int64_t i0 = bi * CT, j0 = bj * CT;
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  double acc[MM + 1];
+#pragma unroll
+  for (int q = 0; q <= MM; ++q) acc[q] = 0.0;
+  if (i < n) {
+    const double ai = alpha[i], si = sv[i];
+#pragma unroll 4
+    for (int q = 0; q < CT / 4; ++q) {
+      const int64_t j = j0 + cb + 4 * q;
+      if (j > i) continue;
+      const double w = (ai * alpha[j] - si * sv[j] * Bi[i + j * ldb]) * (i == j ? 1.0 : 2.0);
+      acc[MM] += w;
+#pragma unroll
+      for (int mi = 0; mi < MM; ++mi)
+        if (mi < nm) acc[mi] = fma(w, D[mi * dstride + i + j * ldd], acc[mi]);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q <= MM; ++q) {
+    double v = acc[q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x <= nm) {
+    const int q = threadIdx.x < nm ? threadIdx.x : MM;
+    double t = red[0][q];
+    for (int w = 1; w < 8; ++w) t += red[w][q];
+    part[(int64_t)blockIdx.x * (nm + 1) + threadIdx.x] = t;
+  }
+}
+
+int64_t grad_stored_partials(int64_t n) {
+  const int64_t T = (n + CT - 1) / CT;
+  return T * (T + 1) / 2 * (GPGP_GRAD_MAXMAT + 1);
+}
+
+void grad_stored_contract(cudaStream_t s, const GradPlan &pl, int64_t n, const double *Bi, int64_t ldb,
+                          const double *alpha, const double *sv, const double *D, int64_t ldd, int64_t dstride,
+                          double *part, double *g) {
+  const int64_t T = (n + CT - 1) / CT;
+  const unsigned nt = (unsigned)(T * (T + 1) / 2);
+  const int nm = pl.m.nmat;
+  switch (nm) {
+    case 1:
+      grad_stored_kernel<1><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+      break;
+    case 2:
+      grad_stored_kernel<2><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+      break;
+    case 3:
+      grad_stored_kernel<3><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+      break;
+    default:
+      grad_stored_kernel<0><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+  }
+  GPGP_CHECK_LAUNCH();
+  reduce_partials_kernel<<<1, 256, 0, s>>>(part, nt, nm + 1, g);
+  GPGP_CHECK_LAUNCH();
+}
+
+void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, double *hg) {
+  for (int idx = 0; idx < nterms * GPGP_TERM_NPARAM; ++idx) {
+    const int q = pl.slot_mat[idx];
+    hg[idx] = q == -2 ? 0.0 : pl.slot_scale[idx] * g[q >= 0 ? q : pl.m.nmat];
+  }
 }
 
 }  // namespace gpgp

@@ -191,6 +191,10 @@ struct gpgp_model {
   gpgp::DBuf Linv;                     // W = L^-1, kept resident once computed
   bool have_Linv = false;
   bool want_linv = false;              // the gradient follows the fit: form L^-1 right after the factor (mixed)
+  bool want_dk = false;                // the gradient follows the fit: write K's derivative matrices with K
+  gpgp::DBuf dK;                       // those matrices (plan gplan), valid while have_dK
+  gpgp::GradPlan gplan;
+  bool have_dK = false;
   gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
   std::unique_ptr<gpgp::FitcState> fitc;
   std::unique_ptr<gpgp::NlcState> nlc;  // set when the last iteration was non-log-concave

@@ -343,8 +343,13 @@ def get_inducing(gp, x, device=0):
     return np.vstack(zs)
 
 
-def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", device=0):
-    """gp_fit (R/gp_fit.R:54-60): posterior approximation with the current hyperparameters."""
+def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", device=0, grad=False):
+    """gp_fit (R/gp_fit.R:54-60): posterior approximation with the current hyperparameters.
+
+    grad=True (lik_gaussian, method_full; new, the reference has no gradient) also
+    computes the energy gradient in the same call (gpgp_fit_grad): the covariance
+    pass then writes K's derivative matrices beside K, and gp_energy_grad returns
+    the gradient without evaluating the kernel again."""
     x = _as_x(x)
     y = np.ascontiguousarray(y, dtype=np.float64).ravel()
     n, d = x.shape
@@ -381,8 +386,19 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     h = C.c_void_p()
     res = L.FitResult()
     gp._free()
-    st = lib.gpgp_fit(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf), n, d,
-                      L.ptr(y), L.ptr(tr), L.ptr(of), C.byref(h), C.byref(res))
+    graw = None
+    if grad:
+        if gp.lik.kind != "gaussian" or gp.method.kind != "full":
+            raise ValueError("the energy gradient needs lik_gaussian and method_full")
+        gt = np.zeros(len(_flat_terms(gp)) * L.TERM_NPARAM)
+        gs = C.c_double(0.0)
+        st = lib.gpgp_fit_grad(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf),
+                               n, d, L.ptr(y), L.ptr(tr), L.ptr(of), C.byref(h), C.byref(res), L.ptr(gt),
+                               C.byref(gs))
+        graw = (gt, gs.value)
+    else:
+        st = lib.gpgp_fit(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf), n,
+                          d, L.ptr(y), L.ptr(tr), L.ptr(of), C.byref(h), C.byref(res))
     L.check(st, ctx.h)
     if res.status == L.EMAXITER and gp.approx.kind == "ep":
         warnings.warn("Maximum number of iterations in EP reached")
@@ -393,7 +409,7 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     gp.fit = dict(type="analytic", log_evidence=res.log_evidence, iters=res.iters,
                   quad_ok=bool(res.quad_ok), status=res.status, jitter=op.jitter, n=n,
                   converged=bool(res.converged), precision_used="mixed" if res.precision_used == 1 else "fp64",
-                  y=y, trials=tr, offset=of)
+                  y=y, trials=tr, offset=of, grad_raw=graw)
     gp.fitted = True
     return gp
 
@@ -445,10 +461,14 @@ def gp_energy_grad(gp, include_prior=True):
     if not _is_fitted(gp):
         raise RuntimeError("The GP must be fitted. Call gp_fit first.")
     terms = _flat_terms(gp)
-    gt = np.zeros(len(terms) * L.TERM_NPARAM)
-    gs = C.c_double(0.0)
-    st = L.load().gpgp_model_grad(gp._model, L.ptr(gt), C.byref(gs))
-    L.check(st, None)
+    if gp.fit.get("grad_raw") is not None:  # computed with the fit (gp_fit(..., grad=True))
+        gt, gsv = gp.fit["grad_raw"]
+    else:
+        gt = np.zeros(len(terms) * L.TERM_NPARAM)
+        gs = C.c_double(0.0)
+        st = L.load().gpgp_model_grad(gp._model, L.ptr(gt), C.byref(gs))
+        L.check(st, None)
+        gsv = gs.value
     g = []
     for ti, (grp, c) in enumerate(terms):
         if c.kind == "periodic":
@@ -460,7 +480,7 @@ def gp_energy_grad(gp, include_prior=True):
             for nme in c.param_names():
                 g.append(gt[ti * L.TERM_NPARAM + GRAD_SLOT[nme]])
     if gp.lik.kind == "gaussian" and not gp.lik.is_fixed("sigma"):
-        g.append(gs.value)
+        g.append(gsv)
     g = -np.array(g, dtype=np.float64)
     if include_prior:
         g = g - _dlpdf_prior(gp)
@@ -820,10 +840,10 @@ def gp_optim(gp, x, y, tol=1e-4, tol_param=1e-1, maxiter=500, restarts=1, verbos
     method="lbfgs" uses the device energy gradient (lik_gaussian, method_full)."""
     it = [0]
 
-    def energy(param):
+    def energy(param, grad=False):
         set_param(gp, param)
         try:
-            gp_fit(gp, x, y, **fit_args)
+            gp_fit(gp, x, y, grad=grad, **fit_args)
         except np.linalg.LinAlgError:
             return np.inf
         e = gp_energy(gp)
@@ -838,8 +858,9 @@ def gp_optim(gp, x, y, tol=1e-4, tol_param=1e-1, maxiter=500, restarts=1, verbos
         from scipy.optimize import minimize
 
         def fg(param):
-            e = energy(param)
-            return e, gp_energy_grad(gp)
+            # fit and gradient in one call (gpgp_fit_grad)
+            e = energy(param, grad=True)
+            return e, (gp_energy_grad(gp) if np.isfinite(e) else np.zeros(len(param)))
 
         r = minimize(fg, p0, jac=True, method="L-BFGS-B", options=dict(maxiter=maxiter, ftol=tol / n))
         p_opt, e_opt = r.x, r.fun

@@ -187,10 +187,12 @@ def _fit_grad_abi(gp, x, y, prec, fused):
 
 @pytest.mark.parametrize("n", [700, 2248])
 def test_fit_grad_entry_point(n):
-    """gpgp_fit_grad = gpgp_fit + gpgp_model_grad. In FP64 the two are the same
-    computation; under mixed precision the fused call solves for alpha with W = L^-1
-    (formed right after the factor) and its results agree with the separate calls
-    (1e-10 on the evidence) and with FP64 within the mixed path's bound (1e-8)."""
+    """gpgp_fit_grad = gpgp_fit + gpgp_model_grad. In FP64 the two factor the same K;
+    at n = 2248 the fused call's gradient is a pass over K's derivative matrices
+    written with K (summed in another order than the separate call's regenerated
+    tiles: 1e-12). Under mixed precision the fused call also solves for alpha with
+    W = L^-1 (formed right after the factor) and its results agree with the separate
+    calls (1e-10 on the evidence) and with FP64 within the mixed path's bound (1e-8)."""
     rng = np.random.default_rng(n + 1)
     x = rng.uniform(-1, 1, (n, 3))
     y = np.sin(3 * x[:, 0]) + x[:, 1] + 0.05 * rng.standard_normal(n)
@@ -199,7 +201,7 @@ def test_fit_grad_entry_point(n):
         return G.gp_init([G.cf_matern52(lscale=0.6, magn=1.0), G.cf_const(magn=0.7)], G.lik_gaussian(sigma=0.05))
     l64f, g64f = _fit_grad_abi(gp(), x, y, "fp64", True)
     l64, g64 = _fit_grad_abi(gp(), x, y, "fp64", False)
-    assert l64f == l64 and np.array_equal(g64f, g64)
+    assert abs(l64f - l64) <= 1e-13 * abs(l64) and relmax(g64f, g64) < 1e-12
     lmf, gmf = _fit_grad_abi(gp(), x, y, "mixed", True)
     lm, gm = _fit_grad_abi(gp(), x, y, "mixed", False)
     assert abs(lmf - lm) <= 1e-10 * abs(lm)
