@@ -24,11 +24,11 @@
 
 namespace gpgp {
 
-// potrf_diag_kernel lives in dense.cu
-__global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
-                                  double *__restrict__ Winv, double *__restrict__ logdet_part,
-                                  int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
-                                  int64_t sL);
+// potrf_diag_df_kernel lives in dense.cu
+__global__ void potrf_diag_df_kernel(double *__restrict__ A, int kb, int64_t lda,
+                                     double *__restrict__ Winv, double *__restrict__ logdet_part,
+                                     int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
+                                     int64_t sL);
 
 namespace {
 
@@ -44,6 +44,7 @@ struct Bucket {
   void *sa = nullptr, *sb = nullptr;
   OzSplit SA, SB;
   int variant = 0;  // 0: FP64 pipe; sliced tensor cores with 1: 64-wide, 2: 256-wide outer panels
+  double best_ms = 0.0;  // the autotuner's time of the chosen variant
   ~Bucket() {
     if (sa) cudaFreeAsync(sa, X.s);
     if (sb) cudaFreeAsync(sb, X.s);
@@ -368,9 +369,18 @@ struct gpgp_batch {
   cudaGraphExec_t exec = nullptr;
   double tune_ms[3] = {0, 0, 0};  // autotuning time per variant
   int64_t graph_kernels = 0;  // kernel nodes of the captured graph
+  // streams and events of the graph's concurrent bucket lanes (capture only)
+  cudaStream_t lanes[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t join[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr;
   ~gpgp_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    for (int l = 0; l < 4; ++l) {
+      if (lanes[l]) cudaStreamDestroy(lanes[l]);
+      if (join[l]) cudaEventDestroy(join[l]);
+    }
+    if (fork) cudaEventDestroy(fork);
   }
 };
 
@@ -387,9 +397,8 @@ size_t split_stride_bytes(int64_t rows, int64_t K) {
   return (oz_split_bytes(rows, K, kSlices) + 1023) / 1024 * 1024;
 }
 
-// one bucket's pipeline, enqueued on the context stream (no allocation, no sync)
-void run_bucket(gpgp_batch *b, Bucket &k) {
-  cudaStream_t st = b->ctx->stream;
+// one bucket's pipeline, enqueued on stream st (no allocation, no sync)
+void run_bucket(gpgp_batch *b, Bucket &k, cudaStream_t st) {
   const int64_t nb = k.nb, mb = k.mb, P = k.count, nbl = nb / NB;
   GPGP_CUDA(cudaMemsetAsync(k.status.p, 0, P * sizeof(int), st));
   {
@@ -408,9 +417,10 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
   if (k.variant == 0) {
     potrf_batched(st, k.Bm.p, nb, nb, nb * nb, k.Winv.p, nb * NB, k.ldp.p, nbl, k.status.p, P);
   } else {
-    // tensor variants: outer panels of 64 (variant 1: a trailing update after every
-    // diagonal block, K = 64) or 256 columns (variant 2: the panel's blocks update
-    // the rest of the panel, then one trailing update with K = 256)
+    // tensor variants: double-float diagonal blocks and outer panels of 64 (variant 1:
+    // a trailing update after every diagonal block, K = 64) or 256 columns (variant
+    // 2: the panel's blocks update the rest of the panel, then one trailing update
+    // with K = 256)
     const int64_t outer = k.variant == 2 ? 4 * NB : NB;
     for (int64_t k0 = 0; k0 < nb; k0 += outer) {
       const int64_t kbo = std::min<int64_t>(outer, nb - k0);
@@ -419,9 +429,9 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
         double *Akk = k.Bm.p + j0 + j0 * nb;
         {
           KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
-          potrf_diag_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB,
-                                                                  k.ldp.p + blk, k.status.p, j0, nb * nb, nb * NB,
-                                                                  nbl);
+          potrf_diag_df_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB,
+                                                                     k.ldp.p + blk, k.status.p, j0, nb * nb,
+                                                                     nb * NB, nbl);
         }
         GPGP_CHECK_LAUNCH();
         const int64_t m = nb - j0 - NB;
@@ -494,7 +504,43 @@ void run_bucket(gpgp_batch *b, Bucket &k) {
 }
 
 void run_all(gpgp_batch *b) {
-  for (auto &k : b->buckets) run_bucket(b, *k);
+  for (auto &k : b->buckets) run_bucket(b, *k, b->ctx->stream);
+}
+
+// The buckets share nothing but the read-only quadrature nodes and the error word
+// (set, never cleared, by the kernels), so they can run side by side: the graph
+// forks from the context stream into up to kLanes streams, each running its
+// buckets in turn, and joins back. Buckets go to lanes longest first by their
+// measured time (the autotuner's; FP64 plans: count x nb^3), each to the lane
+// with the least work so far. Small buckets whose launches fill few SMs then
+// overlap with the large ones.
+constexpr int kLanes = 4;
+
+void run_all_lanes(gpgp_batch *b) {
+  cudaStream_t st = b->ctx->stream;
+  const int nl = std::min<int>(kLanes, (int)b->buckets.size());
+  if (nl <= 1) return run_all(b);
+  std::vector<int> order(b->buckets.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  auto cost = [&](int i) {
+    const Bucket &k = *b->buckets[i];
+    return k.best_ms > 0 ? k.best_ms : (double)k.count * k.nb * k.nb * k.nb;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+  std::vector<double> load(nl, 0.0);
+  std::vector<std::vector<int>> lane(nl);
+  for (int i : order) {
+    const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    lane[l].push_back(i);
+    load[l] += cost(i);
+  }
+  GPGP_CUDA(cudaEventRecord(b->fork, st));
+  for (int l = 0; l < nl; ++l) {
+    GPGP_CUDA(cudaStreamWaitEvent(b->lanes[l], b->fork, 0));
+    for (int i : lane[l]) run_bucket(b, *b->buckets[i], b->lanes[l]);
+    GPGP_CUDA(cudaEventRecord(b->join[l], b->lanes[l]));
+    GPGP_CUDA(cudaStreamWaitEvent(st, b->join[l], 0));
+  }
 }
 
 // copy the inputs of every problem into its bucket slot (host buffers)
@@ -676,9 +722,9 @@ gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, in
       int bestv = 0;
       for (int v = 0; v < nvar; ++v) {
         k.variant = v;
-        run_bucket(b.get(), k);  // warm
+        run_bucket(b.get(), k, st);  // warm
         GPGP_CUDA(cudaEventRecord(e0, st));
-        run_bucket(b.get(), k);
+        run_bucket(b.get(), k, st);
         GPGP_CUDA(cudaEventRecord(e1, st));
         GPGP_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -690,14 +736,20 @@ gpgp_status gpgp_batch_create(gpgp_ctx *ctx, const gpgp_batch_problem *probs, in
         }
       }
       k.variant = bestv;
+      k.best_ms = nvar > 1 ? best : 0.0;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    for (int l = 0; l < kLanes; ++l) {
+      GPGP_CUDA(cudaStreamCreateWithFlags(&b->lanes[l], cudaStreamNonBlocking));
+      GPGP_CUDA(cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming));
+    }
+    GPGP_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     // capture the whole pipeline once; the graph's kernel nodes are counted per replay
     GPGP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     tl_capturing = true;
     try {
-      run_all(b.get());
+      run_all_lanes(b.get());
     } catch (...) {
       tl_capturing = false;
       cudaGraph_t g = nullptr;

@@ -39,6 +39,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "model.cuh"
 
 namespace gpgp {
@@ -487,23 +488,6 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// (double)f * 2^sh, exact, by moving the float's fields into a double: the
-// float exponent is rebiased and sh added; zero and out-of-range cases take ldexp
-// out of line so that the common path is never if-converted into FP64 work
-__device__ __noinline__ double f2d_scaled_slow(float f, int sh) { return ldexp((double)f, sh); }
-
-__device__ __forceinline__ double f2d_scaled(float f, int sh) {
-  const uint32_t b = __float_as_uint(f);
-  if ((b << 1) == 0u) return 0.0;
-  const uint32_t ef = (b >> 23) & 0xFFu;
-  const int ed = (int)ef - 127 + 1023 + sh;
-  if (ef == 0u || ef == 0xFFu || ed <= 0 || ed >= 2047) return f2d_scaled_slow(f, sh);
-  const unsigned long long db = ((unsigned long long)(b >> 31) << 63) |
-                                ((unsigned long long)ed << 52) |
-                                ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)db);
-}
-
 // double-float accumulation of v into (hi, lo) with an error-free TwoSum
 __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
   const float s = __fadd_rn(hi, v);
@@ -511,47 +495,6 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
   const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
   hi = s;
   lo = __fadd_rn(lo, e);
-}
-
-__device__ __noinline__ double df2d_scaled_slow(float hi, float lo, int sh) {
-  return f2d_scaled_slow(hi, sh) + f2d_scaled_slow(lo, sh);
-}
-
-// (hi + lo) 2^sh as a double without FP64 instructions. The pair is first
-// renormalised (TwoSum), so |lo| <= ulp_float(hi) / 2 = 2^28 units in the last
-// place of hi's double. hi's double has its low 29 mantissa bits clear, so lo,
-// counted in those units, is added to or subtracted from the bit pattern of |hi|
-// directly; a subtraction below a power of two lands in the binade beneath, whose
-// unit is half as large, and takes twice the count. lo bits below the double's
-// last place are dropped (an error under one unit). Zero, subnormal and
-// out-of-range cases go to the FP64 path out of line.
-__device__ __forceinline__ double df2d_scaled(float hi, float lo, int sh) {
-  {
-    const float s = __fadd_rn(hi, lo);
-    const float bp = __fsub_rn(s, hi);
-    lo = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(lo, bp));
-    hi = s;
-  }
-  const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
-  // a zero sum (hi = 0 forces lo = 0 after TwoSum): common in zero-padded and
-  // triangular operands, so it stays off the slow path
-  if ((bh << 1) == 0u) return 0.0;
-  const uint32_t eh = (bh >> 23) & 0xFFu, el = (bl >> 23) & 0xFFu;
-  const int ed = (int)eh - 127 + 1023 + sh;
-  const int shift = (int)el - (int)eh + 29;
-  if (eh == 0u || eh == 0xFFu || el == 0xFFu || ed <= 1 || ed >= 2047 || shift > 5)
-    return df2d_scaled_slow(hi, lo, sh);
-  const uint32_t mh = bh & 0x7FFFFFu;
-  uint32_t k = 0u;
-  if (el != 0u) {
-    const uint32_t ml = (bl & 0x7FFFFFu) | 0x800000u;
-    k = shift >= 0 ? (ml << shift) : (shift > -24 ? (ml >> -shift) : 0u);
-  }
-  const bool opposite = ((bh ^ bl) >> 31) != 0u;
-  if (opposite && mh == 0u) k <<= 1;
-  unsigned long long mag = ((unsigned long long)ed << 52) | ((unsigned long long)mh << 29);
-  mag = opposite ? mag - k : mag + k;
-  return __longlong_as_double((long long)(mag | ((unsigned long long)(bh >> 31) << 63)));
 }
 
 // ---------------------------------------------------------------------------
