@@ -158,6 +158,7 @@ SIGNATURES = {
     "gpgp_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "gpgp_server_destroy": (C.c_int, [_P]),
     "gpgp_mixed_selftest": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P]),
+    "gpgp_cov_df_selftest": (C.c_int, [_P, C.POINTER(Kernel), _P, C.c_int64, C.c_int32, C.c_double, _P]),
     "gpgp_wait_selftest": (C.c_int, [_P, C.c_int32]),
     "gpgp_fit_gaussian_noalloc": (C.c_int, [_P, C.POINTER(Kernel), C.c_double, C.c_double, _P, C.c_int64,
                                             C.c_int32, _P, _P, _P]),

@@ -351,10 +351,14 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
   // matrices, so the gradient does not evaluate the kernel a second time: for
   // matrices of at least as many 64-tiles as SMs, while they take at most half
   // of the free device memory.
+  // Under mixed precision, kernels of stationary and constant terms are evaluated in
+  // double-float arithmetic on the FP32 pipe (~2^-44 relative; the sliced
+  // factorisation carries ~2^-33).
   {
     Phase ph(ctx, GPGP_PHASE_COV);
     m->dK.reset();
     m->have_dK = false;
+    const bool df = m->opts.precision == GPGP_PREC_MIXED && n >= NB && cov_df_eligible(m->dk);
     const int64_t T = (n + NB - 1) / NB;
     if (m->want_dk && T * (T + 1) / 2 >= device_sms() && plan_grad_store(m->dk, &m->gplan) &&
         m->gplan.m.nmat > 0) {
@@ -363,13 +367,20 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       const size_t need = (size_t)m->gplan.m.nmat * n * n * sizeof(double);
       if (need <= fr / 2) {
         m->dK.alloc(st, (size_t)m->gplan.m.nmat * n * n);
-        cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
+        if (df)
+          cov_matrix_df(st, m->dk, &m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
+        else
+          cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
         m->have_dK = true;
       }
     }
-    if (!m->have_dK)
-      cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
-                 m->opts.jitter, nullptr);
+    if (!m->have_dK) {
+      if (df)
+        cov_matrix_df(st, m->dk, nullptr, m->F.p, n, n, w.K.p, n, m->opts.jitter, nullptr, 0, 0);
+      else
+        cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
+                   m->opts.jitter, nullptr);
+    }
   }
   double *red = w.red.p;  // [0..63] partials, [64] result, [100..] scalars
   double *logdetL = red + 100;
@@ -1122,10 +1133,15 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       if (tc_error(m)) return fail(ctx, GPGP_ETIMEOUT, "a tensor-core kernel wait timed out");
       return GPGP_OK;
     }
-    // mean = Kt alpha (R/gp_pred.R:209), fused: Kt is never stored
+    // mean = Kt alpha (R/gp_pred.R:209), fused: Kt is never stored. Mixed
+    // precision evaluates the kernel in double-float arithmetic where it can.
+    const bool df = m->opts.precision == GPGP_PREC_MIXED && cov_df_eligible(m->dk);
     {
       Phase ph(ctx, GPGP_PHASE_PRED_MEAN);
-      cov_matvec(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, mout);
+      if (df)
+        cov_matvec_df(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, mout);
+      else
+        cov_matvec(s, m->dk, gm, Ft.p, mt, mt, m->F.p, n, n, m->alpha.p, mout);
     }
     if (var && m->nlc) {
       // a fit whose last iteration was non-log-concave: (K + V)^-1 through the blocks
@@ -1151,8 +1167,11 @@ static gpgp_status pred_impl(gpgp_model *m, const double *xt, int64_t mt, uint32
       if (mixed) compute_linv(m);
       for (int64_t c0 = 0; c0 < mt; c0 += chunk) {
         const int64_t mc = std::min(chunk, mt - c0);
-        cov_matrix(s, m->dk, gm, m->F.p, n, n, Ft.p + c0, mt, mc, R.p, n, COV_ROWSCALE, 0, 0, 0.0,
-                   m->s.p);
+        if (df)
+          cov_cross_df(s, m->dk, gm, m->F.p, n, n, Ft.p + c0, mt, mc, R.p, n, m->s.p);
+        else
+          cov_matrix(s, m->dk, gm, m->F.p, n, n, Ft.p + c0, mt, mc, R.p, n, COV_ROWSCALE, 0, 0, 0.0,
+                     m->s.p);
         if (mixed) {
           trmv_sumsq_mixed(s, m->Linv.p, n, n, R.p, mc, n, csum.p + c0, m->errflag.p);
         } else {
@@ -1349,6 +1368,61 @@ gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_
       const double s2 = m->lik.sigma * m->lik.sigma;
       *grad_lik_sigma = s2 * (h2[1] - h2[0]);
     }
+    return GPGP_OK;
+  });
+}
+
+gpgp_status gpgp_cov_df_selftest(gpgp_ctx *ctx, const gpgp_kernel *k, const double *x, int64_t n, int32_t d,
+                                 double jitter, double *max_rel_err) {
+  if (!ctx || !k || !x || n < 1 || d < 1 || !max_rel_err) return fail(ctx, GPGP_EINVAL, "invalid argument");
+  return guarded(ctx, [&]() -> gpgp_status {
+    GPGP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    DevKernel dk;
+    std::vector<HostTermPrep> prep;
+    std::string err;
+    gpgp_status st = build_dev_kernel(k, d, &dk, &prep, &err);
+    if (st != GPGP_OK) return fail(ctx, st, err);
+    if (!cov_df_eligible(dk)) return fail(ctx, GPGP_EUNSUPPORTED, "kernel has no double-float path");
+    GradPlan pl;
+    if (!plan_grad_store(dk, &pl)) return fail(ctx, GPGP_EUNSUPPORTED, "too many derivative matrices");
+    const int nm = pl.m.nmat;
+    DBuf dx, F, K64, Kdf, D64, Ddf;
+    copy_in(s, dx, x, (size_t)n * d, false);
+    F.alloc(s, (size_t)n * std::max(1, dk.nfeat));
+    prep_features(s, dk, prep, dx.p, n, n, F.p, n);
+    K64.alloc(s, (size_t)n * n);
+    Kdf.alloc(s, (size_t)n * n);
+    D64.alloc(s, (size_t)std::max(1, nm) * n * n);
+    Ddf.alloc(s, (size_t)std::max(1, nm) * n * n);
+    GPGP_CUDA(cudaMemsetAsync(D64.p, 0, D64.n * sizeof(double), s));
+    GPGP_CUDA(cudaMemsetAsync(Ddf.p, 0, Ddf.n * sizeof(double), s));
+    cov_matrix_grad(s, dk, pl, F.p, n, n, K64.p, n, jitter, D64.p, n, (int64_t)n * n);
+    cov_matrix_df(s, dk, &pl, F.p, n, n, Kdf.p, n, jitter, Ddf.p, n, (int64_t)n * n);
+    std::vector<double> a((size_t)n * n), b((size_t)n * n);
+    double out[2] = {0.0, 0.0};
+    for (int q = -1; q < nm; ++q) {
+      const double *pa = q < 0 ? K64.p : D64.p + (size_t)q * n * n;
+      const double *pb = q < 0 ? Kdf.p : Ddf.p + (size_t)q * n * n;
+      GPGP_CUDA(cudaMemcpyAsync(a.data(), pa, a.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaMemcpyAsync(b.data(), pb, b.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPGP_CUDA(cudaStreamSynchronize(s));
+      double mx = 0.0, dmax = 0.0;
+      for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = j; i < n; ++i) mx = std::max(mx, std::fabs(a[i + j * n]));
+      double rmax = 0.0;
+      for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = j; i < n; ++i) {
+          const double e = std::fabs(a[i + j * n] - b[i + j * n]);
+          if (!(e == e)) return fail(ctx, GPGP_ENAN, "NaN in a covariance");
+          dmax = std::max(dmax, e);
+          if (std::fabs(a[i + j * n]) > 1e-20 * mx) rmax = std::max(rmax, e / std::fabs(a[i + j * n]));
+        }
+      out[0] = std::max(out[0], mx > 0.0 ? dmax / mx : dmax);
+      if (q < 0) out[1] = rmax;
+    }
+    max_rel_err[0] = out[0];
+    max_rel_err[1] = out[1];
     return GPGP_OK;
   });
 }

@@ -24,11 +24,11 @@
 
 namespace gpgp {
 
-// potrf_diag_df_kernel lives in dense.cu
-__global__ void potrf_diag_df_kernel(double *__restrict__ A, int kb, int64_t lda,
-                                     double *__restrict__ Winv, double *__restrict__ logdet_part,
-                                     int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
-                                     int64_t sL);
+// potrf_diag_kernel lives in dense.cu
+__global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
+                                  double *__restrict__ Winv, double *__restrict__ logdet_part,
+                                  int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
+                                  int64_t sL);
 
 namespace {
 
@@ -417,10 +417,9 @@ void run_bucket(gpgp_batch *b, Bucket &k, cudaStream_t st) {
   if (k.variant == 0) {
     potrf_batched(st, k.Bm.p, nb, nb, nb * nb, k.Winv.p, nb * NB, k.ldp.p, nbl, k.status.p, P);
   } else {
-    // tensor variants: double-float diagonal blocks and outer panels of 64 (variant 1:
-    // a trailing update after every diagonal block, K = 64) or 256 columns (variant
-    // 2: the panel's blocks update the rest of the panel, then one trailing update
-    // with K = 256)
+    // tensor variants: outer panels of 64 (variant 1: a trailing update after every
+    // diagonal block, K = 64) or 256 columns (variant 2: the panel's blocks update
+    // the rest of the panel, then one trailing update with K = 256)
     const int64_t outer = k.variant == 2 ? 4 * NB : NB;
     for (int64_t k0 = 0; k0 < nb; k0 += outer) {
       const int64_t kbo = std::min<int64_t>(outer, nb - k0);
@@ -429,9 +428,9 @@ void run_bucket(gpgp_batch *b, Bucket &k, cudaStream_t st) {
         double *Akk = k.Bm.p + j0 + j0 * nb;
         {
           KTScope kts(GPGP_KPROF_POTRF_DIAG, st, 2.0 * NB * NB * NB / 3 * (double)P);
-          potrf_diag_df_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB,
-                                                                     k.ldp.p + blk, k.status.p, j0, nb * nb,
-                                                                     nb * NB, nbl);
+          potrf_diag_kernel<<<(unsigned)P, DIAG_THREADS, 0, st>>>(Akk, NB, nb, k.Winv.p + blk * NB * NB,
+                                                                  k.ldp.p + blk, k.status.p, j0, nb * nb, nb * NB,
+                                                                  nbl);
         }
         GPGP_CHECK_LAUNCH();
         const int64_t m = nb - j0 - NB;

@@ -194,6 +194,18 @@ void grad_stored_contract(cudaStream_t s, const GradPlan &pl, int64_t n, const d
 int64_t grad_stored_partials(int64_t n);
 // hg[t*5 + p] from the contraction's sums g (host).
 void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, double *hg);
+// Mixed precision: K (and with pl the planned derivative matrices) evaluated in
+// double-float arithmetic on the FP32 pipe, for kernels of cf_const, cf_sexp,
+// cf_matern32 and cf_matern52 terms without periodic inputs (cov_df_eligible).
+bool cov_df_eligible(const DevKernel &dk);
+void cov_matrix_df(cudaStream_t s, const DevKernel &dk, const GradPlan *pl, const double *F, int64_t ldf, int64_t n,
+                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride);
+// Mixed precision, the same kernels: out_ij = s_i K(x1_i, x2_j) (scale null: 1) and
+// out_i = sum_j K(x1_i, x2_j) v_j over the groups of gmask, in double-float arithmetic.
+void cov_cross_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const double *F1, int64_t ld1, int64_t n1,
+                  const double *F2, int64_t ld2, int64_t n2, double *out, int64_t ldo, const double *scale);
+void cov_matvec_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const double *F1, int64_t ld1, int64_t n1,
+                   const double *F2, int64_t ld2, int64_t n2, const double *v, double *out);
 
 // ---------------------------------------------------------------------------
 // dense FP64 linear algebra (column-major)

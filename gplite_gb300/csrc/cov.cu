@@ -10,6 +10,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fp64math.cuh"
 
 namespace gpgp {
@@ -1041,6 +1042,412 @@ void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, doubl
   for (int idx = 0; idx < nterms * GPGP_TERM_NPARAM; ++idx) {
     const int q = pl.slot_mat[idx];
     hg[idx] = q == -2 ? 0.0 : pl.slot_scale[idx] * g[q >= 0 ? q : pl.m.nmat];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K (and its derivative matrices) in double-float arithmetic (mixed precision)
+// ---------------------------------------------------------------------------
+// The FP64 tile kernels above are bound by this part's FP64 pipe (~35 FP64
+// operations per matern52 pair). Under mixed precision the covariance is instead
+// evaluated in pair arithmetic (dfloat.cuh) on the FP32 pipe, which retires 64
+// times the lane operations: the distance, its square root, the exponential
+// and the polynomial factor, each to ~2^-44 relative, then converted to doubles
+// without FP64 instructions. That is far below the ~2^-33 the sliced
+// factorisation carries. Kernels made only of cf_const, cf_sexp, cf_matern32 and
+// cf_matern52 terms (without periodic inputs) take this path.
+bool cov_df_eligible(const DevKernel &dk) {
+  for (int t = 0; t < dk.nterms; ++t) {
+    const DevTerm &T = dk.t[t];
+    if (T.periodic || (T.kind != GPGP_CF_CONST && T.kind != GPGP_CF_SEXP && T.kind != GPGP_CF_MATERN32 &&
+                       T.kind != GPGP_CF_MATERN52))
+      return false;
+  }
+  return true;
+}
+
+// One term's value and its derivatives with respect to log lscale (dv0) and log
+// magn (dv1 = 2 k) as pairs; m2 and c1 are the term's constants as pairs.
+template <bool GRAD>
+__device__ __forceinline__ f2 term_value_df(int kind, f2 m2, f2 c1, const f2 *fi, const f2 *fj, int dt, f2 *dv0) {
+  if (kind == GPGP_CF_CONST) return m2;
+  // squared distance: each difference as a pair, its square as a pair, summed
+  f2 r2 = f2{0.0f, 0.0f};
+  for (int c = 0; c < dt; ++c) {
+    const f2 a = fi[c], b = fj[c];
+    const f2 dh = f2_two_sum(a.h, -b.h);
+    const f2 df = f2_fast_two_sum(dh.h, __fadd_rn(dh.l, __fsub_rn(a.l, b.l)));
+    r2 = f2_fma(df, df, r2);
+  }
+  if (kind == GPGP_CF_SEXP) {
+    const f2 q = f2_mul(r2, c1);  // r^2 / lscale^2
+    const f2 k = f2_mul(m2, f2_exp_neg(f2{-0.5f * q.h, -0.5f * q.l}));
+    if (GRAD) *dv0 = f2_mul(k, q);
+    return k;
+  }
+  const f2 a = f2_mul(c1, f2_sqrt(r2));
+  const f2 me = f2_mul(m2, f2_exp_neg(f2_neg(a)));
+  const f2 a2 = f2_mul(a, a);
+  if (kind == GPGP_CF_MATERN32) {
+    if (GRAD) *dv0 = f2_mul(me, a2);
+    return f2_fma(me, a, me);  // m2 (1 + a) e^-a
+  }
+  const f2 a2_3 = f2_mul(a2, f2{0x1.555556p-2f, -0x1.555556p-27f});  // a^2 / 3
+  if (GRAD) *dv0 = f2_mul(me, f2_fma(a2_3, a, a2_3));  // m2 a^2 (1 + a) / 3 e^-a
+  return f2_mul(me, f2_add(f2_fast_two_sum(1.0f, 0.0f), f2_add(a, a2_3)));
+}
+
+// Lower 64 x 64 tiles of K = sum over groups of the products of their terms, with
+// jitter on the diagonal, mirrored above it (cov_tile_kernel's layout); with GRAD,
+// also the planned derivative matrices (entries i >= j).
+template <int NT, bool GRAD>
+__global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats gm, const double *__restrict__ F,
+                                                          int64_t ldf, int64_t n, double *__restrict__ K, int64_t ldk,
+                                                          double jitter, double *__restrict__ D, int64_t ldd,
+                                                          int64_t dstride) {
+  extern __shared__ double smd[];
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  f2 *Fi = reinterpret_cast<f2 *>(smd);
+  f2 *Fj = Fi + CT * lds;
+  double *Tt = smd + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  int64_t bi, bj;
+  tri_index(blockIdx.x, &bi, &bj);
+  const int64_t i0 = bi * CT, j0 = bj * CT;
+  for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+    const int r = idx % CT, c = idx / CT;
+    Fi[r * lds + c] = i0 + r < n ? f2_of(F[i0 + r + c * ldf]) : f2{0.0f, 0.0f};
+    Fj[r * lds + c] = j0 + r < n ? f2_of(F[j0 + r + c * ldf]) : f2{0.0f, 0.0f};
+  }
+  f2 m2[MT], c1[MT];
+#pragma unroll
+  for (int t = 0; t < MT; ++t) {
+    if (t < nterms) {
+      m2[t] = f2_of(dk.t[t].m2);
+      c1[t] = f2_of(dk.t[t].c1);
+    }
+  }
+  __syncthreads();
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  const bool do_mirror = bi != bj;
+  f2 kv[MT], dv0[MT];
+#pragma unroll 1
+  for (int q = 0; q < CT / 4; ++q) {
+    const int c = cb + 4 * q;
+    const int64_t j = j0 + c;
+    double v = 0.0;
+    if (i < n && j < n) {
+#pragma unroll
+      for (int t = 0; t < MT; ++t)
+        if (t < nterms)
+          kv[t] = term_value_df<GRAD>(dk.t[t].kind, m2[t], c1[t], Fi + r * lds + dk.t[t].off,
+                                      Fj + c * lds + dk.t[t].off, dk.t[t].dt, &dv0[t]);
+      f2 sum = f2{0.0f, 0.0f}, prod = f2{1.0f, 0.0f};
+      int g = dk.t[0].group;
+#pragma unroll
+      for (int t = 0; t < MT; ++t) {
+        if (t >= nterms) break;
+        if (dk.t[t].group != g) {
+          sum = f2_add(sum, prod);
+          prod = f2{1.0f, 0.0f};
+          g = dk.t[t].group;
+        }
+        prod = t == 0 || dk.t[t - 1].group != dk.t[t].group ? kv[t] : f2_mul(prod, kv[t]);
+      }
+      sum = f2_add(sum, prod);
+      v = f2_to_double(sum);
+      if (i == j) v += jitter;
+      K[i + j * ldk] = v;
+      if (GRAD && i >= j) {
+#pragma unroll
+        for (int mi = 0; mi < GPGP_GRAD_MAXMAT; ++mi) {
+          if (mi >= gm.nmat) break;
+          const int ga = gm.grp[mi];
+          f2 val = f2{1.0f, 0.0f};
+          bool first = true;
+#pragma unroll
+          for (int t = 0; t < MT; ++t) {
+            if (t >= nterms) break;
+            if (dk.t[t].group != ga) continue;
+            // kind 1: the slot's derivative in place of its term (lscale: dv0;
+            // magnitude slots are kind 0, the group value)
+            const f2 f = (gm.kind[mi] == 1 && t == gm.a[mi]) ? dv0[t] : kv[t];
+            val = first ? f : f2_mul(val, f);
+            first = false;
+          }
+          D[mi * dstride + i + j * ldd] = f2_to_double(val);
+        }
+      }
+    }
+    if (do_mirror) Tt[c * (CT + 1) + r] = v;
+  }
+  if (do_mirror) {
+    __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < CT / 4; ++q) {
+      const int rr = threadIdx.x % CT;
+      const int cc = threadIdx.x / CT + 4 * q;
+      const int64_t jj = j0 + rr, ii = i0 + cc;
+      if (jj < n && ii < n) K[jj + ii * ldk] = Tt[rr * (CT + 1) + cc];
+    }
+  }
+}
+
+template <bool GRAD>
+static void launch_cov_df(cudaStream_t s, const DevKernel &dk, const GradMats &gm, const double *F, int64_t ldf,
+                          int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+  const int lds = (dk.nfeat | 1);
+  const size_t smem = (size_t)(2 * CT * lds) * sizeof(f2) + (size_t)CT * (CT + 1) * sizeof(double);
+  static PerDevice attr;
+  per_device(attr, [] {
+    const int mx = 2 * CT * 65 * 8 + CT * (CT + 1) * 8;
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<0, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<1, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<2, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<3, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return 1;
+  });
+  const int64_t T = (n + CT - 1) / CT;
+  const unsigned nt = (unsigned)(T * (T + 1) / 2);
+  switch (dk.nterms) {
+    case 1:
+      cov_tile_df_kernel<1, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    case 2:
+      cov_tile_df_kernel<2, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    case 3:
+      cov_tile_df_kernel<3, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      break;
+    default:
+      cov_tile_df_kernel<0, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+  }
+  GPGP_CHECK_LAUNCH();
+}
+
+void cov_matrix_df(cudaStream_t s, const DevKernel &dk, const GradPlan *pl, const double *F, int64_t ldf, int64_t n,
+                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+  if (n == 0) return;
+  if (pl) {
+    launch_cov_df<true>(s, dk, pl->m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+  } else {
+    GradMats none;
+    std::memset(&none, 0, sizeof(none));
+    launch_cov_df<false>(s, dk, none, F, ldf, n, K, ldk, jitter, nullptr, 0, 0);
+  }
+}
+
+// K(x1_i, x2_j) as a pair: the sum over the groups selected by gmask of the
+// products of their terms (kernel_value's order).
+template <int NT>
+__device__ __forceinline__ f2 kernel_value_df(const DevKernel &dk, uint32_t gmask, const f2 *m2, const f2 *c1,
+                                              const f2 *fi, const f2 *fj) {
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
+  f2 sum = f2{0.0f, 0.0f}, prod = f2{1.0f, 0.0f};
+  int g = dk.t[0].group;
+  bool first = true;
+#pragma unroll
+  for (int t = 0; t < MT; ++t) {
+    if (t >= nterms) break;
+    if (dk.t[t].group != g) {
+      if (gmask & (1u << g)) sum = f2_add(sum, prod);
+      prod = f2{1.0f, 0.0f};
+      g = dk.t[t].group;
+      first = true;
+    }
+    if (gmask & (1u << g)) {
+      const f2 kv = term_value_df<false>(dk.t[t].kind, m2[t], c1[t], fi + dk.t[t].off, fj + dk.t[t].off,
+                                         dk.t[t].dt, nullptr);
+      prod = first ? kv : f2_mul(prod, kv);
+      first = false;
+    }
+  }
+  if (gmask & (1u << g)) sum = f2_add(sum, prod);
+  return sum;
+}
+
+template <int MT>
+__device__ __forceinline__ void load_consts_df(const DevKernel &dk, int nterms, f2 *m2, f2 *c1) {
+#pragma unroll
+  for (int t = 0; t < MT; ++t) {
+    if (t < nterms) {
+      m2[t] = f2_of(dk.t[t].m2);
+      c1[t] = f2_of(dk.t[t].c1);
+    }
+  }
+}
+
+// Cross covariance out_ij = s_i K(x1_i, x2_j) (s null: 1), 64 x 64 tiles (grid T1 x T2).
+template <int NT>
+__global__ void __launch_bounds__(256) cov_cross_df_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1,
+                                                           int64_t ld1, int64_t n1, const double *__restrict__ F2,
+                                                           int64_t ld2, int64_t n2, double *__restrict__ out,
+                                                           int64_t ldo, const double *__restrict__ scale) {
+  extern __shared__ double smd[];
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  f2 *Fi = reinterpret_cast<f2 *>(smd);
+  f2 *Fj = Fi + CT * lds;
+  const int64_t i0 = (int64_t)blockIdx.x * CT, j0 = (int64_t)blockIdx.y * CT;
+  for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+    const int r = idx % CT, c = idx / CT;
+    Fi[r * lds + c] = i0 + r < n1 ? f2_of(F1[i0 + r + c * ld1]) : f2{0.0f, 0.0f};
+    Fj[r * lds + c] = j0 + r < n2 ? f2_of(F2[j0 + r + c * ld2]) : f2{0.0f, 0.0f};
+  }
+  f2 m2[MT], c1[MT];
+  load_consts_df<MT>(dk, nterms, m2, c1);
+  __syncthreads();
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  if (i >= n1) return;
+  const f2 si = scale ? f2_of(scale[i]) : f2{1.0f, 0.0f};
+#pragma unroll 1
+  for (int q = 0; q < CT / 4; ++q) {
+    const int c = cb + 4 * q;
+    const int64_t j = j0 + c;
+    if (j >= n2) continue;
+    const f2 v = kernel_value_df<NT>(dk, gmask, m2, c1, Fi + r * lds, Fj + c * lds);
+    out[i + j * ldo] = f2_to_double(scale ? f2_mul(si, v) : v);
+  }
+}
+
+void cov_cross_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const double *F1, int64_t ld1, int64_t n1,
+                  const double *F2, int64_t ld2, int64_t n2, double *out, int64_t ldo, const double *scale) {
+  if (n1 == 0 || n2 == 0) return;
+  const int lds = (dk.nfeat | 1);
+  const size_t smem = (size_t)(2 * CT * lds) * sizeof(f2);
+  static PerDevice attr;
+  per_device(attr, [] {
+    const int mx = 2 * CT * 65 * 8;
+    GPGP_CUDA(cudaFuncSetAttribute(cov_cross_df_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_cross_df_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_cross_df_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_cross_df_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return 1;
+  });
+  const dim3 grid((unsigned)((n1 + CT - 1) / CT), (unsigned)((n2 + CT - 1) / CT));
+  switch (dk.nterms) {
+    case 1:
+      cov_cross_df_kernel<1><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, out, ldo, scale);
+      break;
+    case 2:
+      cov_cross_df_kernel<2><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, out, ldo, scale);
+      break;
+    case 3:
+      cov_cross_df_kernel<3><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, out, ldo, scale);
+      break;
+    default:
+      cov_cross_df_kernel<0><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, out, ldo, scale);
+  }
+  GPGP_CHECK_LAUNCH();
+}
+
+// out[i] = sum_j K(x1_i, x2_j) v_j with the products accumulated as pairs: block
+// (x, y) takes rows [x CT, (x+1) CT) and the y-th range of x2 tiles; with several
+// ranges the partial sums go to out + y n1 (as cov_matvec_kernel).
+template <int NT>
+__global__ void __launch_bounds__(256) cov_matvec_df_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1,
+                                                            int64_t ld1, int64_t n1, const double *__restrict__ F2,
+                                                            int64_t ld2, int64_t n2, const double *__restrict__ v,
+                                                            double *__restrict__ out, int64_t tiles_per_range) {
+  extern __shared__ double smd[];
+  constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
+  const int nterms = NT > 0 ? NT : dk.nterms;
+  const int nf = dk.nfeat;
+  const int lds = (nf | 1);
+  f2 *Fi = reinterpret_cast<f2 *>(smd);
+  f2 *Fj = Fi + CT * lds;
+  f2 *vj = Fj + CT * lds;
+  f2 *red = vj + CT;  // 4 x CT partial pairs
+  const int64_t i0 = (int64_t)blockIdx.x * CT;
+  out += (int64_t)blockIdx.y * n1;
+  for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+    const int r = idx % CT, c = idx / CT;
+    Fi[r * lds + c] = i0 + r < n1 ? f2_of(F1[i0 + r + c * ld1]) : f2{0.0f, 0.0f};
+  }
+  f2 m2[MT], c1[MT];
+  load_consts_df<MT>(dk, nterms, m2, c1);
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  f2 acc = f2{0.0f, 0.0f};
+  const int64_t jbeg = (int64_t)blockIdx.y * tiles_per_range * CT;
+  const int64_t jlim = jbeg + tiles_per_range * CT;
+  const int64_t jend = jlim < n2 ? jlim : n2;
+  for (int64_t j0 = jbeg; j0 < jend; j0 += CT) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+      const int rr = idx % CT, c = idx / CT;
+      Fj[rr * lds + c] = j0 + rr < n2 ? f2_of(F2[j0 + rr + c * ld2]) : f2{0.0f, 0.0f};
+    }
+    if (threadIdx.x < CT) vj[threadIdx.x] = (j0 + threadIdx.x < n2) ? f2_of(v[j0 + threadIdx.x]) : f2{0.0f, 0.0f};
+    __syncthreads();
+    if (i0 + r < n1) {
+#pragma unroll 1
+      for (int q = 0; q < CT / 4; ++q) {
+        const int c = cb * (CT / 4) + q;
+        if (j0 + c < n2) acc = f2_fma(kernel_value_df<NT>(dk, gmask, m2, c1, Fi + r * lds, Fj + c * lds), vj[c], acc);
+      }
+    }
+  }
+  red[cb * CT + r] = acc;
+  __syncthreads();
+  if (threadIdx.x < CT && i0 + threadIdx.x < n1) {
+    f2 t = red[threadIdx.x];
+    for (int k = 1; k < 4; ++k) t = f2_add(t, red[k * CT + threadIdx.x]);
+    out[i0 + threadIdx.x] = f2_to_double(t);
+  }
+}
+
+void cov_matvec_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const double *F1, int64_t ld1, int64_t n1,
+                   const double *F2, int64_t ld2, int64_t n2, const double *v, double *out) {
+  if (n1 == 0) return;
+  const int lds = (dk.nfeat | 1);
+  const size_t smem = (size_t)(2 * CT * lds + CT + 4 * CT) * sizeof(f2);
+  static PerDevice attr;
+  per_device(attr, [] {
+    const int mx = (2 * CT * 65 + 5 * CT) * 8;
+    GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_df_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_df_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_df_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    GPGP_CUDA(cudaFuncSetAttribute(cov_matvec_df_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return 1;
+  });
+  const int64_t T1 = (n1 + CT - 1) / CT, T2 = std::max<int64_t>(1, (n2 + CT - 1) / CT);
+  const int64_t want = std::max<int64_t>(1, (2 * device_sms() + T1 - 1) / T1);
+  const int64_t tpr = (T2 + std::min(want, T2) - 1) / std::min(want, T2);
+  const int64_t nrange = (T2 + tpr - 1) / tpr;
+  double *dst = out, *part = nullptr;
+  if (nrange > 1) {
+    GPGP_CUDA(cudaMallocAsync((void **)&part, (size_t)nrange * n1 * sizeof(double), s));
+    dst = part;
+  }
+  const dim3 grid((unsigned)T1, (unsigned)nrange);
+  switch (dk.nterms) {
+    case 1:
+      cov_matvec_df_kernel<1><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, v, dst, tpr);
+      break;
+    case 2:
+      cov_matvec_df_kernel<2><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, v, dst, tpr);
+      break;
+    case 3:
+      cov_matvec_df_kernel<3><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, v, dst, tpr);
+      break;
+    default:
+      cov_matvec_df_kernel<0><<<grid, 256, smem, s>>>(dk, gmask, F1, ld1, n1, F2, ld2, n2, v, dst, tpr);
+  }
+  GPGP_CHECK_LAUNCH();
+  if (nrange > 1) {
+    sum_ranges_kernel<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(part, nrange, n1, out);
+    GPGP_CHECK_LAUNCH();
+    GPGP_CUDA(cudaFreeAsync(part, s));
   }
 }
 

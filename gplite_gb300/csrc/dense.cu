@@ -16,7 +16,6 @@
 #include <algorithm>
 
 #include "common.cuh"
-#include "dfloat.cuh"
 #include "fp64math.cuh"
 
 namespace gpgp {
@@ -424,201 +423,6 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_kernel(double *__rest
     const int r = idx % NB, c = idx / NB;
     double wv = 0.0;
     if (r < kb && c <= r) wv = (r == c) ? rdiag[r] : rdiag[r] * V[r][c];
-    Winv[r + c * NB] = wv;
-  }
-  for (int st = NB / 2; st > 0; st >>= 1) {
-    if (tid < st) lg[tid] += lg[tid + st];
-    __syncthreads();
-  }
-  if (tid == 0) *logdet_part = lg[0];
-}
-
-// ---------------------------------------------------------------------------
-// diagonal block in double-float arithmetic (mixed precision)
-// ---------------------------------------------------------------------------
-// The factor and inverse of potrf_diag_kernel in double-float arithmetic
-// (dfloat.cuh): every entry a pair of FP32 numbers. The FP32 pipe retires 64 times
-// the lane operations of this part's FP64 pipe and a dependent FP32 step takes a
-// few cycles where an FP64 one takes 64, so the work per entry is no longer the
-// arithmetic but the instructions around it. The kernel keeps them few:
-//  - the trailing entries live in registers. Each of the fifteen update warps
-//    (every warp but warp 0) owns a fixed set of factor entries (r, c), c >= 2,
-//    and of inverse entries (i, c), i >= c + 2, dealt round-robin from lists
-//    ordered so that every step's active entries are spread over all threads. A
-//    step reads only the two column values it needs from shared memory, and an
-//    entry goes to shared memory once, when it is final: a factor column c
-//    after step c - 2 (warp 0 applies its last update and pivots it at step
-//    c - 1), an inverse entry after its last update.
-//  - warp 0 runs the pivot chain one column ahead, as in the FP64 kernel.
-// The inverse is W = D^-1 V with V the unit lower triangular inverse of the
-// column-scaled factor: V(i, c) = V1(i, c) + sum_{k=c+1..i-1} V1(i, k) V(k, c),
-// V1(i, k) = -L(i, k) / L(k, k) written by the pivot of column k; step k runs
-// beside the factor's step k + 1.
-// The pairs carry ~2^-44 of each operand's size per operation; the mixed-precision
-// factorisations feed the block entries that carry ~2^-33 of their row's size
-// already (the sliced trailing updates), so the block adds nothing measurable.
-// Pivots must be normal FP32 numbers within [2^-100, 2^100] (the matrices of the
-// mixed path, I + S K S and its kin, have pivots >= 1); any other value sets the
-// status, and the caller refactors on the FP64 pipe.
-constexpr int DF_UPD = DIAG_THREADS - 32;                // update threads (warps 1..15)
-constexpr int DF_SLOTS = (62 * 63 / 2 + DF_UPD - 1) / DF_UPD;  // entries per thread and list (5)
-
-__global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_df_kernel(double *__restrict__ A, int kb, int64_t lda,
-                                                                     double *__restrict__ Winv,
-                                                                     double *__restrict__ logdet_part,
-                                                                     int *__restrict__ status, int64_t k0,
-                                                                     int64_t sA, int64_t sW, int64_t sL) {
-  A += blockIdx.x * sA;
-  Winv += blockIdx.x * sW;
-  logdet_part += blockIdx.x * sL;
-  status += blockIdx.x;
-  __shared__ f2 S[NB][NB + 1];
-  __shared__ f2 V[NB][NB + 1];
-  __shared__ f2 rdiag[NB];
-  __shared__ double lg[NB];
-  __shared__ int failed;
-  if (*(volatile int *)status != 0) return;
-  const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
-    const int r = idx % NB, c = idx / NB;
-    // held negated until its column is pivoted
-    S[r][c] = (r < kb && c < kb && r >= c) ? f2_neg(f2_of(A[r + c * lda])) : f2{0.0f, 0.0f};
-    V[r][c] = f2{0.0f, 0.0f};
-  }
-  if (tid == 0) failed = 0;
-  // Entry lists. Factor: entries (r, c), c >= 2, numbered by column from the last
-  // one (step j updates the first nf(j) = (kb-2-j)(kb-1-j)/2 of them). Inverse:
-  // entries (i, c), i >= c + 2, numbered by column c, then row i; step k updates
-  // those with c < k < i.
-  const int ut = tid - 32;  // update thread index (warp 0: negative)
-  const int nF = kb >= 2 ? (kb - 2) * (kb - 1) / 2 : 0;  // also the inverse list's length
-  int fr[DF_SLOTS], fc[DF_SLOTS], vi[DF_SLOTS], vc[DF_SLOTS];
-#pragma unroll
-  for (int q = 0; q < DF_SLOTS; ++q) {
-    const int e = ut + q * DF_UPD;
-    fr[q] = fc[q] = vi[q] = vc[q] = -1;
-    if (ut >= 0 && e < nF) {
-      // factor: entry e lies in column c = kb - 1 - u, u the largest integer with
-      // u (u + 1) / 2 <= e, at row c + e - u (u + 1) / 2
-      int u = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
-      while (u * (u + 1) / 2 > e) --u;
-      while ((u + 1) * (u + 2) / 2 <= e) ++u;
-      const int c = kb - 1 - u;
-      fc[q] = c;
-      fr[q] = c + (e - u * (u + 1) / 2);
-      // inverse: column c holds kb - 2 - c entries; columns 0, 1, ... in order
-      int rem = e, cc = 0;
-      while (rem >= kb - 2 - cc) {
-        rem -= kb - 2 - cc;
-        ++cc;
-      }
-      vc[q] = cc;
-      vi[q] = cc + 2 + rem;
-    }
-  }
-  __syncthreads();
-  f2 fx[DF_SLOTS], vx[DF_SLOTS];
-#pragma unroll
-  for (int q = 0; q < DF_SLOTS; ++q) {
-    fx[q] = fr[q] >= 0 ? S[fr[q]][fc[q]] : f2{0.0f, 0.0f};
-    vx[q] = f2{0.0f, 0.0f};
-  }
-  f2 lreg[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-  auto pivot = [&](int j, const f2 (&t)[2]) {
-    const int src = j & 31;
-    const float th = __shfl_sync(0xffffffffu, j < 32 ? t[0].h : t[1].h, src);
-    const float tl = __shfl_sync(0xffffffffu, j < 32 ? t[0].l : t[1].l, src);
-    const f2 dj = f2{-th, -tl};
-    // a normal FP32 in [2^-100, 2^100] (NaN fails the test too)
-    if (!(dj.h >= 7.8886090522101181e-31f && dj.h <= 1.2676506002282294e30f)) {
-      if (lane == 0) {
-        failed = 1;
-        atomicCAS(status, 0, (int)(k0 + j + 1));
-      }
-      return;
-    }
-    const f2 rp = f2_rsqrt(dj);
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (u == 1 || j < 31) {
-        const int r = lane + 32 * u;
-        if (r > j && r < kb) {
-          const f2 l = f2_neg(f2_mul(t[u], rp));
-          S[r][j] = l;
-          V[r][j] = f2_neg(f2_mul(l, rp));
-          lreg[u] = l;
-        }
-      }
-    }
-    if (lane == src) {
-      S[j][j] = f2_mul(dj, rp);
-      rdiag[j] = rp;
-    }
-  };
-  if (warp == 0) {
-    f2 t0[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) t0[u] = (lane + 32 * u < kb) ? S[lane + 32 * u][0] : f2{0.0f, 0.0f};
-    pivot(0, t0);
-  }
-  __syncthreads();
-  if (failed) return;
-  for (int j = 0; j < kb; ++j) {
-    if (warp == 0) {
-      if (j + 1 < kb) {
-        // column j + 1 (final in shared memory but for column j's update): that
-        // update, then its pivot
-        const int src = (j + 1) & 31;
-        const f2 l = f2{__shfl_sync(0xffffffffu, (j + 1) < 32 ? lreg[0].h : lreg[1].h, src),
-                        __shfl_sync(0xffffffffu, (j + 1) < 32 ? lreg[0].l : lreg[1].l, src)};
-        f2 t[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          if (u == 1 || j < 31) {
-            const int r = lane + 32 * u;
-            if (r > j && r < kb) t[u] = f2_fma(lreg[u], l, S[r][j + 1]);
-          }
-        }
-        pivot(j + 1, t);
-      }
-    } else {
-      // factor step j: entries with c >= j + 2; the entries of column j + 2 are
-      // then final but for step j + 1, which warp 0 applies
-      const int nf = j < kb - 2 ? (kb - 2 - j) * (kb - 1 - j) / 2 : 0;
-#pragma unroll
-      for (int q = 0; q < DF_SLOTS; ++q) {
-        if (ut + q * DF_UPD < nf) {
-          fx[q] = f2_fma(S[fr[q]][j], S[fc[q]][j], fx[q]);
-          if (fc[q] == j + 2) S[fr[q]][fc[q]] = fx[q];
-        }
-      }
-      // inverse step k = j - 1: V(i, c) += V1(i, k) V(k, c) for c < k < i; V(i, c)
-      // joins the registers at its first step (k = c + 1) and goes back to shared
-      // memory after its last (k = i - 1)
-      const int k = j - 1;
-#pragma unroll
-      for (int q = 0; q < DF_SLOTS; ++q) {
-        if (vc[q] >= 0 && vc[q] < k && k < vi[q]) {
-          if (k == vc[q] + 1) vx[q] = V[vi[q]][vc[q]];
-          vx[q] = f2_fma(V[vi[q]][k], V[k][vc[q]], vx[q]);
-          if (k == vi[q] - 1) V[vi[q]][vc[q]] = vx[q];
-        }
-      }
-    }
-    __syncthreads();
-    if (failed) return;
-  }
-  for (int idx = tid; idx < kb * kb; idx += DIAG_THREADS) {
-    const int r = idx % kb, c = idx / kb;
-    if (r >= c) A[r + c * lda] = f2_to_double(S[r][c]);
-  }
-  if (tid < NB) lg[tid] = tid < kb ? log(f2_to_double(S[tid][tid])) : 0.0;
-  __syncthreads();
-  for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
-    const int r = idx % NB, c = idx / NB;
-    double wv = 0.0;
-    if (r < kb && c <= r) wv = f2_to_double(r == c ? rdiag[r] : f2_mul(rdiag[r], V[r][c]));
     Winv[r + c * NB] = wv;
   }
   for (int st = NB / 2; st > 0; st >>= 1) {

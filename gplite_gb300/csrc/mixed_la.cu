@@ -5,8 +5,8 @@
 // of 32-bit fixed-point row slices, accumulated exactly, summed in FP64).
 //
 // Cholesky is two-level right-looking: outer panels of NBO columns (384: faster
-// at n = 16384 than 256 or 512), each factored with the 64-wide double-float
-// diagonal kernel of dense.cu, a sliced GEMM for the panel solve L21 = A21 W11^T and
+// at n = 16384 than 256 or 512), each factored with the 64-wide FP64 diagonal
+// kernel of dense.cu, a sliced GEMM for the panel solve L21 = A21 W11^T and
 // sliced GEMMs for the updates inside the panel; one sliced SYRK with K = NBO
 // then updates the trailing matrix, so every trailing element is rewritten in
 // FP64 once per outer panel.
@@ -20,8 +20,8 @@
 
 namespace gpgp {
 
-// potrf_diag_df_kernel and potrf_panel_inv_kernel live in dense.cu
-__global__ void potrf_diag_df_kernel(double *__restrict__ A, int kb, int64_t lda,
+// potrf_diag_kernel and potrf_panel_inv_kernel live in dense.cu
+__global__ void potrf_diag_kernel(double *__restrict__ A, int kb, int64_t lda,
                                   double *__restrict__ Winv, double *__restrict__ logdet_part,
                                   int *__restrict__ status, int64_t k0, int64_t sA, int64_t sW,
                                   int64_t sL);
@@ -60,7 +60,7 @@ constexpr int LOOK_PANEL_SMS = 32;
 
 // The 64-wide blocks of the outer panel [k0, k0 + kbo). Only the panel's own rows
 // lie on the chain from one diagonal block to the next, so they are kept apart:
-//  - chain (stream x): the double-float factor and inverse W of the diagonal block, the
+//  - chain (stream x): the FP64 factor and inverse W of the diagonal block, the
 //    block's rows inside the panel L_p = A_p W^T (FP64, by the inverse), and the
 //    FP64 update of the rest of the panel's lower triangle by them;
 //  - bulk (stream y, after the chain's block): the rows below the panel,
@@ -81,8 +81,8 @@ void factor_panel(cudaStream_t x, cudaStream_t y, const SideStream *sd, double *
     double *Wb = Winv + blk * NB * NB;
     {
       KTScope kts(GPGP_KPROF_POTRF_DIAG, x, 2.0 * jb * jb * jb / 3);
-      potrf_diag_df_kernel<<<1, DIAG_THREADS, 0, x>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0,
-                                                      0, 0, 0);
+      potrf_diag_kernel<<<1, DIAG_THREADS, 0, x>>>(A + j0 + j0 * lda, jb, lda, Wb, logdet_part + blk, status, j0, 0,
+                                                   0, 0);
     }
     GPGP_CHECK_LAUNCH();
     const int64_t mp = pend - (j0 + jb);  // panel rows below the block

@@ -498,6 +498,24 @@ gpgp_status gpgp_fit_gaussian_noalloc(gpgp_ctx *ctx, const gpgp_kernel *k, doubl
 gpgp_status gpgp_mixed_selftest(gpgp_ctx *ctx, int64_t M, int64_t N, int64_t K, int32_t slices,
                                 double *max_rel_err);
 
+/* ---- self-test of the mixed-precision covariance: K(x, x) + jitter I and its
+ *      derivative matrices for the energy gradient (lscale and magnitude slots),
+ *      evaluated in double-float arithmetic (the mixed-precision fit's path for
+ *      kernels of cf_const, cf_sexp, cf_matern32 and cf_matern52 terms) and with
+ *      the FP64 kernels. x is n-by-d column-major (host). Returns in
+ *      max_rel_err[0] the largest max |difference| / max |FP64 entry| over the
+ *      lower triangles of K and of every derivative matrix, and in
+ *      max_rel_err[1] the largest per-entry relative difference of K over its
+ *      entries above 1e-20 of its maximum (smaller entries lose relative
+ *      accuracy as the pair's low part leaves the FP32 normal range; their
+ *      absolute error stays below 1e-35 of it). Derivative entries that vanish
+ *      with the distance (lscale slots of nearly coincident points) carry the
+ *      inputs' 48-bit representation error relative to that distance, so they
+ *      are held in the max norm only. GPGP_EUNSUPPORTED for other kernels. No
+ *      counterpart in the reference. ---- */
+gpgp_status gpgp_cov_df_selftest(gpgp_ctx *ctx, const gpgp_kernel *k, const double *x, int64_t n, int32_t d,
+                                 double jitter, double *max_rel_err);
+
 /* ---- bounded-wait self-test: a kernel polls an mbarrier that nothing completes
  *      for `polls` iterations (the same loop as the tensor-core kernels' waits,
  *      whose bound is 2^24), records the timeout and returns; the call returns

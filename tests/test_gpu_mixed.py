@@ -43,6 +43,34 @@ def test_sliced_gemm_selftest(M, N, K, slices, bound):
     assert 0 <= e.value < bound, e.value
 
 
+@pytest.mark.parametrize("kind", ["sexp", "matern32", "matern52_const", "prod_sum"])
+def test_double_float_covariance_matches_fp64(kind):
+    """Under mixed precision K and its derivative matrices are evaluated in
+    double-float arithmetic (gpgp_cov_df_selftest against the FP64 kernels):
+    max-norm relative difference <= 1e-13 over K and every derivative matrix;
+    per entry of K (entries above 1e-20 of the largest) <= 1e-11: the relative
+    error of e^-a grows with a (~a 2^-44). Derivative entries proportional to
+    the squared distance are held in the max norm only: near-coincident points
+    amplify the inputs' 48-bit representation error relative to that distance."""
+    from gplite_gb300 import gp as GP
+    rng = np.random.default_rng(3)
+    n, d = 700, 3
+    x = rng.uniform(-1, 1, (n, d)) * np.array([1.0, 2.0, 0.5])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")  # a product with two free magnitudes warns (R/misc.R:76)
+        cfs = {"sexp": [G.cf_sexp(lscale=0.4, magn=1.3)], "matern32": [G.cf_matern32(lscale=0.7)],
+               "matern52_const": [G.cf_matern52(lscale=0.6), G.cf_const(0.8)],
+               "prod_sum": [G.cf_const(0.9) * G.cf_matern52(lscale=0.5, vars=[0, 1]),
+                            G.cf_sexp(lscale=0.3, vars=[2])]}[kind]
+    k = GP.kernel_struct(cfs, d)
+    err = (C.c_double * 2)()
+    xf = L.fortran(x)
+    ctx = L.default_context()
+    st = L.load().gpgp_cov_df_selftest(ctx.h, C.byref(k), L.ptr(xf), n, d, 1e-6, err)
+    L.check(st, ctx.h)
+    assert err[0] <= 1e-13 and err[1] <= 1e-11, (kind, err[0], err[1])
+
+
 @pytest.mark.parametrize("n", [65, 200, 700, 2048])
 def test_mixed_gaussian_matches_oracle(n):
     rng = np.random.default_rng(n)
