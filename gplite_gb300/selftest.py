@@ -7,11 +7,11 @@ tcgen05 GEMM and with the FP64 GEMM (gpgp_mixed_selftest), and prints the
 relative difference with the GEMM's launch count, time and BF16 MMA rate from
 the library's kernel timers. The first call is a warm-up.
 
-    python -m gplite_gb300.selftest fit N M [fp64|mixed] [repeats]
+    python -m gplite_gb300.selftest fit|fitgrad N M [fp64|mixed] [repeats]
 
-runs a full GP regression fit, its energy gradient and a prediction with
-variance at M points (see fit_pred): the profiling entry point of the other
-kernels.
+runs a full GP regression fit, its energy gradient (fitgrad: in the same call)
+and a prediction with variance at M points (see fit_pred): the profiling entry
+point of the other kernels.
 """
 from __future__ import annotations
 
@@ -36,11 +36,12 @@ def run(M, N, K, slices=4, repeats=1):
                 tflops=fl.value / max(ms.value / 1e3, 1e-30) / 1e12)
 
 
-def fit_pred(n, m, precision="fp64", d=8, repeats=1):
+def fit_pred(n, m, precision="fp64", d=8, repeats=1, fused=False):
     """A full GP regression (matern52 + const, lik_gaussian 0.05) on n seeded points in
-    [-1, 1]^d: gp_fit, the energy gradient and gp_pred with variance at m points,
-    `repeats` times after one warm-up round. The profiling entry point of the
-    covariance, Cholesky, solve and prediction kernels."""
+    [-1, 1]^d: gp_fit, the energy gradient (fused: in the same call, gpgp_fit_grad)
+    and gp_pred with variance at m points, `repeats` times after one warm-up round.
+    The profiling entry point of the covariance, Cholesky, solve, gradient and
+    prediction kernels."""
     import time
 
     import numpy as np
@@ -55,7 +56,7 @@ def fit_pred(n, m, precision="fp64", d=8, repeats=1):
     for r in range(repeats + 1):
         t0 = time.perf_counter()
         g = G.gp_fit(G.gp_init([cf_matern52(lscale=0.7), cf_const(1.0)], lik_gaussian(sigma=0.05)), x, y,
-                     precision=precision)
+                     precision=precision, grad=fused)
         G.gp_energy_grad(g)
         p = G.gp_pred(g, xt, var=True)
         if r:
@@ -64,12 +65,13 @@ def fit_pred(n, m, precision="fp64", d=8, repeats=1):
 
 
 def main(argv):
-    if argv and argv[0] == "fit":
+    if argv and argv[0] in ("fit", "fitgrad"):
         n, m = int(argv[1]), int(argv[2])
         prec = argv[3] if len(argv) > 3 else "fp64"
-        r = fit_pred(n, m, prec, repeats=int(argv[4]) if len(argv) > 4 else 1)
-        print("fit + gradient + pred n %d m %d %s: lml %.12g, %.3f s per round"
-              % (n, m, prec, r["lml"], r["s_per_round"]))
+        r = fit_pred(n, m, prec, repeats=int(argv[4]) if len(argv) > 4 else 1, fused=argv[0] == "fitgrad")
+        print("%s + pred n %d m %d %s: lml %.12g, %.3f s per round"
+              % ("fit and gradient in one call" if argv[0] == "fitgrad" else "fit, gradient",
+                 n, m, prec, r["lml"], r["s_per_round"]))
         return 0
     if len(argv) < 3:
         print(__doc__)
