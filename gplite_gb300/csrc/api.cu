@@ -226,7 +226,11 @@ int64_t factor_and_solve(gpgp_model *m, Work &w, const double *zvec, double *alp
   const int64_t n = m->n;
   GPGP_CUDA(cudaMemsetAsync(w.status.p, 0, sizeof(int), st));
   vec_rsqrt(st, n, m->V.p, m->s.p);
-  make_B(st, w.K.p, n, m->s.p, m->L.p);
+  if (m->b_ready && !force_fp64)
+    m->b_ready = false;  // B was written with K by the covariance kernel
+  else
+    make_B(st, w.K.p, n, m->s.p, m->L.p);
+  m->b_ready = false;
   const bool mixed = !force_fp64 && m->opts.precision == GPGP_PREC_MIXED;
   {
     Phase ph(ctx, GPGP_PHASE_POTRF);
@@ -359,6 +363,12 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
     m->dK.reset();
     m->have_dK = false;
     const bool df = m->opts.precision == GPGP_PREC_MIXED && n >= NB && cov_df_eligible(m->dk);
+    // lik_gaussian (one factorisation, V = sigma^2): the covariance kernel also
+    // writes B = I + K / sigma^2 into the factor's buffer, which the Cholesky
+    // then starts from (factor_and_solve skips its own pass over K)
+    const bool fuse_b = df && m->lik.kind == GPGP_LIK_GAUSSIAN && m->lik.sigma > 0.0 && m->approx.kind == GPGP_APPROX_LAPLACE;
+    const double s2 = fuse_b ? 1.0 / (m->lik.sigma * m->lik.sigma) : 0.0;
+    m->b_ready = false;
     const int64_t T = (n + NB - 1) / NB;
     if (m->want_dk && T * (T + 1) / 2 >= device_sms() && plan_grad_store(m->dk, &m->gplan) &&
         m->gplan.m.nmat > 0) {
@@ -368,16 +378,20 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
       if (need <= fr / 2) {
         m->dK.alloc(st, (size_t)m->gplan.m.nmat * n * n);
         if (df)
-          cov_matrix_df(st, m->dk, &m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
+          cov_matrix_df(st, m->dk, &m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n,
+                        m->errflag.p, fuse_b ? m->L.p : nullptr, n, s2);
         else
           cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
         m->have_dK = true;
+        m->b_ready = fuse_b;
       }
     }
     if (!m->have_dK) {
-      if (df)
-        cov_matrix_df(st, m->dk, nullptr, m->F.p, n, n, w.K.p, n, m->opts.jitter, nullptr, 0, 0);
-      else
+      if (df) {
+        cov_matrix_df(st, m->dk, nullptr, m->F.p, n, n, w.K.p, n, m->opts.jitter, nullptr, 0, 0, m->errflag.p,
+                      fuse_b ? m->L.p : nullptr, n, s2);
+        m->b_ready = fuse_b;
+      } else
         cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
                    m->opts.jitter, nullptr);
     }
@@ -1398,7 +1412,10 @@ gpgp_status gpgp_cov_df_selftest(gpgp_ctx *ctx, const gpgp_kernel *k, const doub
     GPGP_CUDA(cudaMemsetAsync(D64.p, 0, D64.n * sizeof(double), s));
     GPGP_CUDA(cudaMemsetAsync(Ddf.p, 0, Ddf.n * sizeof(double), s));
     cov_matrix_grad(s, dk, pl, F.p, n, n, K64.p, n, jitter, D64.p, n, (int64_t)n * n);
-    cov_matrix_df(s, dk, &pl, F.p, n, n, Kdf.p, n, jitter, Ddf.p, n, (int64_t)n * n);
+    IBuf derr;
+    derr.alloc(s, 1);
+    GPGP_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), s));
+    cov_matrix_df(s, dk, &pl, F.p, n, n, Kdf.p, n, jitter, Ddf.p, n, (int64_t)n * n, derr.p);
     std::vector<double> a((size_t)n * n), b((size_t)n * n);
     double out[2] = {0.0, 0.0};
     for (int q = -1; q < nm; ++q) {

@@ -198,8 +198,11 @@ void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, doubl
 // double-float arithmetic on the FP32 pipe, for kernels of cf_const, cf_sexp,
 // cf_matern32 and cf_matern52 terms without periodic inputs (cov_df_eligible).
 bool cov_df_eligible(const DevKernel &dk);
+// err (device) receives 1 when a bounded wait of the kernel's TMA staging ran out
+// (null: plain loads). With B, the lower triangle of B = I + s2 K (ldb) as well.
 void cov_matrix_df(cudaStream_t s, const DevKernel &dk, const GradPlan *pl, const double *F, int64_t ldf, int64_t n,
-                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride);
+                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride, int *err,
+                   double *B = nullptr, int64_t ldb = 0, double s2 = 0.0);
 // Mixed precision, the same kernels: out_ij = s_i K(x1_i, x2_j) (scale null: 1) and
 // out_i = sum_j K(x1_i, x2_j) v_j over the groups of gmask, in double-float arithmetic.
 void cov_cross_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const double *F1, int64_t ld1, int64_t n1,

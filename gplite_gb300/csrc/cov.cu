@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "fp64math.cuh"
@@ -1099,27 +1100,84 @@ __device__ __forceinline__ f2 term_value_df(int kind, f2 m2, f2 c1, const f2 *fi
 
 // Lower 64 x 64 tiles of K = sum over groups of the products of their terms, with
 // jitter on the diagonal, mirrored above it (cov_tile_kernel's layout); with GRAD,
-// also the planned derivative matrices (entries i >= j).
+// also the planned derivative matrices (entries i >= j); with Bout, also the lower
+// triangle of B = I + s2 K (a constant scale, lik_gaussian: s2 = 1/sigma^2), so that
+// the Cholesky starts from these tiles without a pass of its own over K.
+// The tile's feature rows are staged in shared memory by the TMA unit: one bulk
+// copy (cp.async.bulk) per feature column and tile, completing on an mbarrier,
+// when every copy is 16-byte aligned and a multiple of 16 bytes long (even n and
+// leading dimension); otherwise by plain loads. The wait is bounded: on timeout
+// the kernel records it in *err (1), lets the copies land (bounded) and returns.
+struct DfArgs {
+  const double *F;
+  int64_t ldf, n;
+  double *K;
+  int64_t ldk;
+  double jitter;
+  double *D;
+  int64_t ldd, dstride;
+  double *B;  // null: no B
+  int64_t ldb;
+  double s2;
+  int bulk;   // 1: TMA staging allowed
+  int *err;
+};
+
 template <int NT, bool GRAD>
-__global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats gm, const double *__restrict__ F,
-                                                          int64_t ldf, int64_t n, double *__restrict__ K, int64_t ldk,
-                                                          double jitter, double *__restrict__ D, int64_t ldd,
-                                                          int64_t dstride) {
-  extern __shared__ double smd[];
+__global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats gm, DfArgs g) {
+  extern __shared__ __align__(16) double smd[];
   constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
   const int nterms = NT > 0 ? NT : dk.nterms;
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
-  f2 *Fi = reinterpret_cast<f2 *>(smd);
-  f2 *Fj = Fi + CT * lds;
-  double *Tt = smd + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  const int64_t n = g.n;
   int64_t bi, bj;
   tri_index(blockIdx.x, &bi, &bj);
   const int64_t i0 = bi * CT, j0 = bj * CT;
-  for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
-    const int r = idx % CT, c = idx / CT;
-    Fi[r * lds + c] = i0 + r < n ? f2_of(F[i0 + r + c * ldf]) : f2{0.0f, 0.0f};
-    Fj[r * lds + c] = j0 + r < n ? f2_of(F[j0 + r + c * ldf]) : f2{0.0f, 0.0f};
+  const bool do_mirror = bi != bj;
+  // shared memory: raw feature columns [2][nf][CT] doubles (TMA destination), the
+  // mbarrier, the pair tiles, the mirror staging
+  double *raw = smd;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(raw + 2 * nf * CT);
+  f2 *Fi = reinterpret_cast<f2 *>(bar + 2);
+  f2 *Fj = Fi + CT * lds;
+  double *Tt = reinterpret_cast<double *>(Fj + CT * lds);  // CT x (CT+1) staging for the mirrored write
+  const int64_t ri = n - i0 < CT ? n - i0 : CT, rj = n - j0 < CT ? n - j0 : CT;
+  if (g.bulk) {
+    // thread 0 issues the copies and waits for them; the block learns the outcome
+    // at the barrier (the copies' data is visible to it from there on)
+    volatile int *landed = reinterpret_cast<volatile int *>(bar + 1);
+    if (threadIdx.x == 0) {
+      const uint32_t b0 = smem_u32(bar);
+      mbar_init(b0, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      const uint32_t bytes = (uint32_t)((ri + (do_mirror ? rj : 0)) * nf * sizeof(double));
+      mbar_expect_tx(b0, bytes);
+      for (int c = 0; c < nf; ++c) {
+        bulk_g2s(smem_u32(raw + c * CT), g.F + i0 + c * g.ldf, (uint32_t)(ri * sizeof(double)), b0);
+        if (do_mirror)
+          bulk_g2s(smem_u32(raw + (nf + c) * CT), g.F + j0 + c * g.ldf, (uint32_t)(rj * sizeof(double)), b0);
+      }
+      const bool ok = mbar_wait_bounded(b0, 0);
+      if (!ok) {
+        atomicOr(g.err, 1);
+        mbar_wait_bounded(b0, 0);  // let the copies land before the block's shared memory goes
+      }
+      *landed = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!*landed) return;
+    for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+      const int r = idx % CT, c = idx / CT;
+      Fi[r * lds + c] = r < ri ? f2_of(raw[c * CT + r]) : f2{0.0f, 0.0f};
+      Fj[r * lds + c] = r < rj ? f2_of(raw[((do_mirror ? nf : 0) + c) * CT + r]) : f2{0.0f, 0.0f};
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+      const int r = idx % CT, c = idx / CT;
+      Fi[r * lds + c] = r < ri ? f2_of(g.F[i0 + r + c * g.ldf]) : f2{0.0f, 0.0f};
+      Fj[r * lds + c] = r < rj ? f2_of(g.F[j0 + r + c * g.ldf]) : f2{0.0f, 0.0f};
+    }
   }
   f2 m2[MT], c1[MT];
 #pragma unroll
@@ -1129,11 +1187,11 @@ __global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats
       c1[t] = f2_of(dk.t[t].c1);
     }
   }
+  const f2 s2 = f2_of(g.s2);
   __syncthreads();
   const int r = threadIdx.x % CT;
   const int cb = threadIdx.x / CT;
   const int64_t i = i0 + r;
-  const bool do_mirror = bi != bj;
   f2 kv[MT], dv0[MT];
 #pragma unroll 1
   for (int q = 0; q < CT / 4; ++q) {
@@ -1147,21 +1205,21 @@ __global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats
           kv[t] = term_value_df<GRAD>(dk.t[t].kind, m2[t], c1[t], Fi + r * lds + dk.t[t].off,
                                       Fj + c * lds + dk.t[t].off, dk.t[t].dt, &dv0[t]);
       f2 sum = f2{0.0f, 0.0f}, prod = f2{1.0f, 0.0f};
-      int g = dk.t[0].group;
+      int grp = dk.t[0].group;
 #pragma unroll
       for (int t = 0; t < MT; ++t) {
         if (t >= nterms) break;
-        if (dk.t[t].group != g) {
+        if (dk.t[t].group != grp) {
           sum = f2_add(sum, prod);
           prod = f2{1.0f, 0.0f};
-          g = dk.t[t].group;
+          grp = dk.t[t].group;
         }
         prod = t == 0 || dk.t[t - 1].group != dk.t[t].group ? kv[t] : f2_mul(prod, kv[t]);
       }
       sum = f2_add(sum, prod);
-      v = f2_to_double(sum);
-      if (i == j) v += jitter;
-      K[i + j * ldk] = v;
+      v = f2_to_double(sum);  // the jitter is added below, outside the pair loop
+      g.K[i + j * g.ldk] = v;
+      if (g.B && i > j) g.B[i + j * g.ldb] = f2_to_double(f2_mul(sum, s2));
       if (GRAD && i >= j) {
 #pragma unroll
         for (int mi = 0; mi < GPGP_GRAD_MAXMAT; ++mi) {
@@ -1179,7 +1237,7 @@ __global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats
             val = first ? f : f2_mul(val, f);
             first = false;
           }
-          D[mi * dstride + i + j * ldd] = f2_to_double(val);
+          g.D[mi * g.dstride + i + j * g.ldd] = f2_to_double(val);
         }
       }
     }
@@ -1192,52 +1250,79 @@ __global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats
       const int rr = threadIdx.x % CT;
       const int cc = threadIdx.x / CT + 4 * q;
       const int64_t jj = j0 + rr, ii = i0 + cc;
-      if (jj < n && ii < n) K[jj + ii * ldk] = Tt[rr * (CT + 1) + cc];
+      if (jj < n && ii < n) g.K[jj + ii * g.ldk] = Tt[rr * (CT + 1) + cc];
+    }
+  } else {
+    // diagonal tile: the jitter, once per diagonal entry (written above by the
+    // thread with c == r, visible to the block after the barrier), and B's diagonal
+    __syncthreads();
+    if (threadIdx.x < CT && i0 + threadIdx.x < n) {
+      const int64_t d = i0 + threadIdx.x;
+      const double kd = g.K[d * (g.ldk + 1)] + g.jitter;
+      g.K[d * (g.ldk + 1)] = kd;
+      if (g.B) g.B[d * (g.ldb + 1)] = 1.0 + g.s2 * kd;
     }
   }
 }
 
 template <bool GRAD>
-static void launch_cov_df(cudaStream_t s, const DevKernel &dk, const GradMats &gm, const double *F, int64_t ldf,
-                          int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+static void launch_cov_df(cudaStream_t s, const DevKernel &dk, const GradMats &gm, const DfArgs &a) {
   const int lds = (dk.nfeat | 1);
-  const size_t smem = (size_t)(2 * CT * lds) * sizeof(f2) + (size_t)CT * (CT + 1) * sizeof(double);
+  const size_t smem = (size_t)2 * dk.nfeat * CT * sizeof(double) + 16 + (size_t)(2 * CT * lds) * sizeof(f2) +
+                      (size_t)CT * (CT + 1) * sizeof(double);
   static PerDevice attr;
   per_device(attr, [] {
-    const int mx = 2 * CT * 65 * 8 + CT * (CT + 1) * 8;
+    const int mx = 2 * 64 * CT * 8 + 16 + 2 * CT * 65 * 8 + CT * (CT + 1) * 8;
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<0, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<1, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<2, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_df_kernel<3, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     return 1;
   });
-  const int64_t T = (n + CT - 1) / CT;
+  const int64_t T = (a.n + CT - 1) / CT;
   const unsigned nt = (unsigned)(T * (T + 1) / 2);
   switch (dk.nterms) {
     case 1:
-      cov_tile_df_kernel<1, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_df_kernel<1, GRAD><<<nt, 256, smem, s>>>(dk, gm, a);
       break;
     case 2:
-      cov_tile_df_kernel<2, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_df_kernel<2, GRAD><<<nt, 256, smem, s>>>(dk, gm, a);
       break;
     case 3:
-      cov_tile_df_kernel<3, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_df_kernel<3, GRAD><<<nt, 256, smem, s>>>(dk, gm, a);
       break;
     default:
-      cov_tile_df_kernel<0, GRAD><<<nt, 256, smem, s>>>(dk, gm, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_df_kernel<0, GRAD><<<nt, 256, smem, s>>>(dk, gm, a);
   }
   GPGP_CHECK_LAUNCH();
 }
 
 void cov_matrix_df(cudaStream_t s, const DevKernel &dk, const GradPlan *pl, const double *F, int64_t ldf, int64_t n,
-                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+                   double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride, int *err,
+                   double *B, int64_t ldb, double s2) {
   if (n == 0) return;
+  DfArgs a;
+  a.F = F;
+  a.ldf = ldf;
+  a.n = n;
+  a.K = K;
+  a.ldk = ldk;
+  a.jitter = jitter;
+  a.D = D;
+  a.ldd = ldd;
+  a.dstride = dstride;
+  a.B = B;
+  a.ldb = ldb;
+  a.s2 = s2;
+  // every bulk copy starts on a 16-byte boundary and moves a multiple of 16 bytes
+  a.bulk = (err && dk.nfeat <= 64 && ldf % 2 == 0 && n % 2 == 0 && ((uintptr_t)F & 15) == 0) ? 1 : 0;
+  a.err = err;
   if (pl) {
-    launch_cov_df<true>(s, dk, pl->m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+    launch_cov_df<true>(s, dk, pl->m, a);
   } else {
     GradMats none;
     std::memset(&none, 0, sizeof(none));
-    launch_cov_df<false>(s, dk, none, F, ldf, n, K, ldk, jitter, nullptr, 0, 0);
+    launch_cov_df<false>(s, dk, none, a);
   }
 }
 

@@ -195,6 +195,7 @@ struct gpgp_model {
   gpgp::DBuf dK;                       // those matrices (plan gplan), valid while have_dK
   gpgp::GradPlan gplan;
   bool have_dK = false;
+  bool b_ready = false;                // B = I + K / sigma^2 already written into L by the covariance kernel
   gpgp::IBuf errflag;                  // bounded-wait timeouts of the device kernels
   std::unique_ptr<gpgp::FitcState> fitc;
   std::unique_ptr<gpgp::NlcState> nlc;  // set when the last iteration was non-log-concave
