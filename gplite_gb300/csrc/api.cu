@@ -381,7 +381,8 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
           cov_matrix_df(st, m->dk, &m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n,
                         m->errflag.p, fuse_b ? m->L.p : nullptr, n, s2);
         else
-          cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n);
+          cov_matrix_grad(st, m->dk, m->gplan, m->F.p, n, n, w.K.p, n, m->opts.jitter, m->dK.p, n, n * n,
+                          m->errflag.p);
         m->have_dK = true;
         m->b_ready = fuse_b;
       }
@@ -393,7 +394,7 @@ gpgp_status fit_full(gpgp_model *m, gpgp_fit_result *res) {
         m->b_ready = fuse_b;
       } else
         cov_matrix(st, m->dk, 0xffffffffu, m->F.p, n, n, m->F.p, n, n, w.K.p, n, COV_FULL, 1, 1,
-                   m->opts.jitter, nullptr);
+                   m->opts.jitter, nullptr, m->errflag.p);
     }
   }
   double *red = w.red.p;  // [0..63] partials, [64] result, [100..] scalars
@@ -1349,7 +1350,8 @@ gpgp_status gpgp_model_grad(gpgp_model *m, double *grad_terms, double *grad_lik_
       g.alloc(s, GPGP_GRAD_MAXMAT + 1);
       {
         Phase ph(ctx, GPGP_PHASE_GRAD);
-        grad_stored_contract(s, m->gplan, n, Bi.p, n, m->alpha.p, m->s.p, m->dK.p, n, (int64_t)n * n, part.p, g.p);
+        grad_stored_contract(s, m->gplan, n, Bi.p, n, m->alpha.p, m->s.p, m->dK.p, n, (int64_t)n * n, part.p, g.p,
+                             m->opts.precision == GPGP_PREC_MIXED);
       }
       double hs[GPGP_GRAD_MAXMAT + 1];
       GPGP_CUDA(cudaMemcpyAsync(hs, g.p, (m->gplan.m.nmat + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));

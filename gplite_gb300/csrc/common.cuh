@@ -140,10 +140,13 @@ enum CovMode {
 };
 
 // out (n1 x n2, ldo). sym: x1 == x2 (only lower tiles evaluated; upper mirrored
-// when mirror = 1). s: per-row scale (COV_B, COV_ROWSCALE) or null.
+// when mirror = 1). s: per-row scale (COV_B, COV_ROWSCALE) or null. err (device,
+// optional): the feature tiles are staged by TMA bulk copies where they are
+// aligned for it, and a bounded wait that runs out sets *err to 1; null: plain loads.
 void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
                 int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2, double *out,
-                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale);
+                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale,
+                int *err = nullptr);
 
 // out[i] = K(x1_i, x2_i) for i < n (diagonal).
 void cov_diag(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
@@ -185,12 +188,14 @@ bool plan_grad_store(const DevKernel &dk, GradPlan *pl);
 // K (n x n, ldk, lower tiles mirrored, jitter on the diagonal) and the planned
 // matrices D + q dstride (ldd; entries i >= j only), 64 x 64 tiles.
 void cov_matrix_grad(cudaStream_t s, const DevKernel &dk, const GradPlan &pl, const double *F, int64_t ldf,
-                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride);
+                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride,
+                     int *err = nullptr);
 // g[q] = sum_ij W_ij D_q(i, j), g[nmat] = sum_ij W_ij, with W = alpha alpha^T -
-// diag(s) Binv diag(s) formed on the fly from the lower triangle of Binv.
+// diag(s) Binv diag(s) formed on the fly from the lower triangle of Binv; df: in
+// double-float arithmetic (mixed precision).
 void grad_stored_contract(cudaStream_t s, const GradPlan &pl, int64_t n, const double *Bi, int64_t ldb,
                           const double *alpha, const double *sv, const double *D, int64_t ldd, int64_t dstride,
-                          double *part, double *g);
+                          double *part, double *g, bool df = false);
 int64_t grad_stored_partials(int64_t n);
 // hg[t*5 + p] from the contraction's sums g (host).
 void grad_stored_assemble(const GradPlan &pl, int nterms, const double *g, double *hg);

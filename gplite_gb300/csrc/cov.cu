@@ -318,19 +318,61 @@ __device__ __forceinline__ void load_feats_t(double *dst, int lds, const double 
   }
 }
 
+// Stages rows [i0, i0 + ri) of the nf feature columns of F1 (leading dimension ld1)
+// and, when two, rows [j0, j0 + rj) of F2's into raw (column-major, TT rows per
+// column: raw[c TT + r], then raw[(nf + c) TT + r]) with the TMA unit: thread 0
+// issues one cp.async.bulk per column completing on the mbarrier bar and waits for
+// them (bounded). Every copy must start on a 16-byte boundary and move a multiple
+// of 16 bytes (the caller checks). All threads call it; it ends with a barrier and
+// returns false for the whole block when the wait ran out (*err |= 1), after
+// letting the copies land.
+template <int TT>
+__device__ __forceinline__ bool stage_features_bulk(double *raw, uint64_t *bar, const double *F1, int64_t ld1,
+                                                    int64_t i0, int64_t ri, const double *F2, int64_t ld2,
+                                                    int64_t j0, int64_t rj, bool two, int nf, int *err) {
+  volatile int *landed = reinterpret_cast<volatile int *>(bar + 1);
+  if (threadIdx.x == 0) {
+    const uint32_t b0 = smem_u32(bar);
+    mbar_init(b0, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(b0, (uint32_t)((ri + (two ? rj : 0)) * nf * sizeof(double)));
+    for (int c = 0; c < nf; ++c) {
+      bulk_g2s(smem_u32(raw + c * TT), F1 + i0 + c * ld1, (uint32_t)(ri * sizeof(double)), b0);
+      if (two) bulk_g2s(smem_u32(raw + (nf + c) * TT), F2 + j0 + c * ld2, (uint32_t)(rj * sizeof(double)), b0);
+    }
+    const bool ok = mbar_wait_bounded(b0, 0);
+    if (!ok) {
+      atomicOr(err, 1);
+      mbar_wait_bounded(b0, 0);  // let the copies land before the block's shared memory goes
+    }
+    *landed = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *landed != 0;
+}
+
+// TMA staging is possible when every copy of a TT-row tile of F (leading
+// dimension ld, n rows) starts on a 16-byte boundary and moves a multiple of 16 bytes.
+inline bool bulk_ok(const double *F, int64_t ld, int64_t n) {
+  return F && ((uintptr_t)F & 15) == 0 && ld % 2 == 0 && n % 2 == 0;
+}
+
 // TT x TT tiles (TT = 64; 16 for small matrices, so that their tiles spread over
 // more SMs); 256 / TT column groups of threads.
 template <int TT>
 __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gmask, const double *__restrict__ F1, int64_t ld1, int64_t n1,
                                 const double *__restrict__ F2, int64_t ld2, int64_t n2,
                                 double *__restrict__ out, int64_t ldo, int mode, int sym,
-                                int mirror, double jitter, const double *__restrict__ scale) {
-  extern __shared__ double sm[];
+                                int mirror, double jitter, const double *__restrict__ scale, int *err) {
+  extern __shared__ __align__(16) double sm[];
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
-  double *Fi = sm;
-  double *Fj = sm + TT * lds;
-  double *Tt = sm + 2 * TT * lds;  // TT x (TT+1) staging for the mirrored write
+  // err: TMA staging of the feature rows (raw, the mbarrier), else plain loads
+  double *raw = sm;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(raw + (err ? 2 * nf * TT : 0));
+  double *Fi = reinterpret_cast<double *>(bar + (err ? 2 : 0));
+  double *Fj = Fi + TT * lds;
+  double *Tt = Fi + 2 * TT * lds;  // TT x (TT+1) staging for the mirrored write
   int64_t bi, bj;
   if (sym)
     tri_index(blockIdx.x, &bi, &bj);
@@ -340,8 +382,18 @@ __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gm
   }
   const int64_t i0 = bi * TT, j0 = bj * TT;
   constexpr int CG = 256 / TT;
-  load_feats_t<TT>(Fi, lds, F1, ld1, i0, n1, nf);
-  load_feats_t<TT>(Fj, lds, F2, ld2, j0, n2, nf);
+  if (err) {
+    const int64_t ri = n1 - i0 < TT ? n1 - i0 : TT, rj = n2 - j0 < TT ? n2 - j0 : TT;
+    if (!stage_features_bulk<TT>(raw, bar, F1, ld1, i0, ri, F2, ld2, j0, rj, true, nf, err)) return;
+    for (int idx = threadIdx.x; idx < TT * nf; idx += blockDim.x) {
+      const int r = idx % TT, c = idx / TT;
+      Fi[r * lds + c] = r < ri ? raw[c * TT + r] : 0.0;
+      Fj[r * lds + c] = r < rj ? raw[(nf + c) * TT + r] : 0.0;
+    }
+  } else {
+    load_feats_t<TT>(Fi, lds, F1, ld1, i0, n1, nf);
+    load_feats_t<TT>(Fj, lds, F2, ld2, j0, n2, nf);
+  }
   __syncthreads();
   const int r = threadIdx.x % TT;
   const int cb = threadIdx.x / TT;
@@ -376,14 +428,17 @@ __global__ void __launch_bounds__(256) cov_tile_kernel(DevKernel dk, uint32_t gm
 
 void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const double *F1,
                 int64_t ld1, int64_t n1, const double *F2, int64_t ld2, int64_t n2, double *out,
-                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale) {
+                int64_t ldo, int mode, int sym, int mirror, double jitter, const double *scale, int *err) {
   if (n1 == 0 || n2 == 0) return;
   const int lds = (dk.nfeat | 1);
-  size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
+  // TMA staging when asked for (err) and every copy is aligned
+  if (!(err && dk.nfeat <= 64 && bulk_ok(F1, ld1, n1) && bulk_ok(F2, ld2, n2))) err = nullptr;
+  const size_t stage = err ? (size_t)2 * dk.nfeat * sizeof(double) : 0;  // per tile row, plus the mbarrier
+  size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double) + (err ? CT * stage + 16 : 0);
   static PerDevice attr;
   per_device(attr, [] {
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   2 * CT * 65 * 8 + CT * (CT + 1) * 8));
+                                   2 * CT * 65 * 8 + CT * (CT + 1) * 8 + 2 * 64 * CT * 8 + 16));
     return 1;
   });
   int64_t T1 = (n1 + CT - 1) / CT, T2 = (n2 + CT - 1) / CT;
@@ -391,23 +446,24 @@ void cov_matrix(cudaStream_t s, const DevKernel &dk, uint32_t group_mask, const 
   const bool small = (sym ? T1 * (T1 + 1) / 2 : T1 * T2) < device_sms();
   if (small) {
     constexpr int ST = 16;
-    smem = (size_t)(2 * ST * lds + ST * (ST + 1)) * sizeof(double);
+    smem = (size_t)(2 * ST * lds + ST * (ST + 1)) * sizeof(double) + (err ? ST * stage + 16 : 0);
     T1 = (n1 + ST - 1) / ST;
     T2 = (n2 + ST - 1) / ST;
     if (sym)
       cov_tile_kernel<ST><<<(unsigned)(T1 * (T1 + 1) / 2), 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2,
-                                                                            out, ldo, mode, 1, mirror, jitter, scale);
+                                                                            out, ldo, mode, 1, mirror, jitter, scale,
+                                                                            err);
     else
       cov_tile_kernel<ST><<<dim3((unsigned)T1, (unsigned)T2), 256, smem, s>>>(
-          dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo, mode, 0, 0, 0.0, scale);
+          dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo, mode, 0, 0, 0.0, scale, err);
   } else if (sym) {
     int64_t nt = T1 * (T1 + 1) / 2;
     cov_tile_kernel<CT><<<(unsigned)nt, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out,
-                                                        ldo, mode, 1, mirror, jitter, scale);
+                                                        ldo, mode, 1, mirror, jitter, scale, err);
   } else {
     dim3 grid((unsigned)T1, (unsigned)T2);
     cov_tile_kernel<CT><<<grid, 256, smem, s>>>(dk, group_mask, F1, ld1, n1, F2, ld2, n2, out, ldo,
-                                                mode, 0, 0, 0.0, scale);
+                                                mode, 0, 0, 0.0, scale, err);
   }
   GPGP_CHECK_LAUNCH();
 }
@@ -842,20 +898,33 @@ template <int NT>
 __global__ void __launch_bounds__(256) cov_tile_grad_kernel(DevKernel dk, GradMats gm, const double *__restrict__ F,
                                                             int64_t ldf, int64_t n, double *__restrict__ K,
                                                             int64_t ldk, double jitter, double *__restrict__ D,
-                                                            int64_t ldd, int64_t dstride) {
-  extern __shared__ double sm[];
+                                                            int64_t ldd, int64_t dstride, int *err) {
+  extern __shared__ __align__(16) double sm[];
   constexpr int MT = NT > 0 ? NT : GPGP_MAX_TERMS;
   const int nterms = NT > 0 ? NT : dk.nterms;
   const int nf = dk.nfeat;
   const int lds = (nf | 1);
-  double *Fi = sm;
-  double *Fj = sm + CT * lds;
-  double *Tt = sm + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
+  // err: TMA staging of the feature rows (raw, the mbarrier), else plain loads
+  double *raw = sm;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(raw + (err ? 2 * nf * CT : 0));
+  double *Fi = reinterpret_cast<double *>(bar + (err ? 2 : 0));
+  double *Fj = Fi + CT * lds;
+  double *Tt = Fi + 2 * CT * lds;  // CT x (CT+1) staging for the mirrored write
   int64_t bi, bj;
   tri_index(blockIdx.x, &bi, &bj);
   const int64_t i0 = bi * CT, j0 = bj * CT;
-  load_feats(Fi, lds, F, ldf, i0, n, nf);
-  load_feats(Fj, lds, F, ldf, j0, n, nf);
+  if (err) {
+    const int64_t ri = n - i0 < CT ? n - i0 : CT, rj = n - j0 < CT ? n - j0 : CT;
+    if (!stage_features_bulk<CT>(raw, bar, F, ldf, i0, ri, F, ldf, j0, rj, true, nf, err)) return;
+    for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
+      const int r = idx % CT, c = idx / CT;
+      Fi[r * lds + c] = r < ri ? raw[c * CT + r] : 0.0;
+      Fj[r * lds + c] = r < rj ? raw[(nf + c) * CT + r] : 0.0;
+    }
+  } else {
+    load_feats(Fi, lds, F, ldf, i0, n, nf);
+    load_feats(Fj, lds, F, ldf, j0, n, nf);
+  }
   __syncthreads();
   const int r = threadIdx.x % CT;
   const int cb = threadIdx.x / CT;
@@ -927,13 +996,16 @@ __global__ void __launch_bounds__(256) cov_tile_grad_kernel(DevKernel dk, GradMa
 }
 
 void cov_matrix_grad(cudaStream_t s, const DevKernel &dk, const GradPlan &pl, const double *F, int64_t ldf,
-                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride) {
+                     int64_t n, double *K, int64_t ldk, double jitter, double *D, int64_t ldd, int64_t dstride,
+                     int *err) {
   if (n == 0) return;
   const int lds = (dk.nfeat | 1);
-  const size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double);
+  if (!(err && dk.nfeat <= 64 && bulk_ok(F, ldf, n))) err = nullptr;
+  const size_t smem = (size_t)(2 * CT * lds + CT * (CT + 1)) * sizeof(double) +
+                      (err ? (size_t)2 * dk.nfeat * CT * sizeof(double) + 16 : 0);
   static PerDevice attr;
   per_device(attr, [] {
-    const int mx = 2 * CT * 65 * 8 + CT * (CT + 1) * 8;
+    const int mx = 2 * CT * 65 * 8 + CT * (CT + 1) * 8 + 2 * 64 * CT * 8 + 16;
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     GPGP_CUDA(cudaFuncSetAttribute(cov_tile_grad_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -944,16 +1016,16 @@ void cov_matrix_grad(cudaStream_t s, const DevKernel &dk, const GradPlan &pl, co
   const unsigned nt = (unsigned)(T * (T + 1) / 2);
   switch (dk.nterms) {
     case 1:
-      cov_tile_grad_kernel<1><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_grad_kernel<1><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride, err);
       break;
     case 2:
-      cov_tile_grad_kernel<2><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_grad_kernel<2><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride, err);
       break;
     case 3:
-      cov_tile_grad_kernel<3><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_grad_kernel<3><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride, err);
       break;
     default:
-      cov_tile_grad_kernel<0><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride);
+      cov_tile_grad_kernel<0><<<nt, 256, smem, s>>>(dk, pl.m, F, ldf, n, K, ldk, jitter, D, ldd, dstride, err);
   }
   GPGP_CHECK_LAUNCH();
 }
@@ -1010,6 +1082,69 @@ __global__ void __launch_bounds__(256) grad_stored_kernel(int nmat, const double
   }
 }
 
+// The same contraction in double-float arithmetic (mixed precision): per entry
+// ~100 FP32 and integer operations where the FP64 kernel spends 7 FP64 ones (the
+// FP64 pipe of this part retires 1/64 of the FP32 pipe's lane operations), so
+// the kernel is bound by its reads. Each thread sums its 16 entries as pairs; the
+// block's sums are formed in FP64 in the fixed order of grad_stored_kernel.
+template <int NM>
+__global__ void __launch_bounds__(256) grad_stored_df_kernel(int nmat, const double *__restrict__ Bi, int64_t ldb,
+                                                             int64_t n, const double *__restrict__ alpha,
+                                                             const double *__restrict__ sv,
+                                                             const double *__restrict__ D, int64_t ldd,
+                                                             int64_t dstride, double *__restrict__ part) {
+  constexpr int MM = NM > 0 ? NM : GPGP_GRAD_MAXMAT;
+  const int nm = NM > 0 ? NM : nmat;
+  __shared__ double red[8][MM + 1];
+  __shared__ f2 aj_s[CT], sj_s[CT];
+  int64_t bi, bj;
+  tri_index(blockIdx.x, &bi, &bj);
+  const int64_t i0 = bi * CT, j0 = bj * CT;
+  if (threadIdx.x < CT) {
+    const int64_t j = j0 + threadIdx.x;
+    aj_s[threadIdx.x] = j < n ? f2_of(alpha[j]) : f2{0.0f, 0.0f};
+    sj_s[threadIdx.x] = j < n ? f2_of(sv[j]) : f2{0.0f, 0.0f};
+  }
+  __syncthreads();
+  const int r = threadIdx.x % CT;
+  const int cb = threadIdx.x / CT;
+  const int64_t i = i0 + r;
+  f2 acc[MM + 1];
+#pragma unroll
+  for (int q = 0; q <= MM; ++q) acc[q] = f2{0.0f, 0.0f};
+  if (i < n) {
+    const f2 ai = f2_of(alpha[i]), si = f2_of(sv[i]);
+#pragma unroll 4
+    for (int q = 0; q < CT / 4; ++q) {
+      const int c = cb + 4 * q;
+      const int64_t j = j0 + c;
+      if (j > i) continue;
+      const f2 t = f2_mul(f2_mul(si, sj_s[c]), f2_of(Bi[i + j * ldb]));
+      f2 w = f2_add(f2_mul(ai, aj_s[c]), f2_neg(t));
+      if (i != j) w = f2{2.0f * w.h, 2.0f * w.l};
+      acc[MM] = f2_add(acc[MM], w);
+#pragma unroll
+      for (int mi = 0; mi < MM; ++mi)
+        if (mi < nm) acc[mi] = f2_fma(w, f2_of(D[mi * dstride + i + j * ldd]), acc[mi]);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q <= MM; ++q) {
+    double v = f2_to_double(acc[q]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x <= nm) {
+    const int q = threadIdx.x < nm ? threadIdx.x : MM;
+    double t = red[0][q];
+    for (int w = 1; w < 8; ++w) t += red[w][q];
+    part[(int64_t)blockIdx.x * (nm + 1) + threadIdx.x] = t;
+  }
+}
+
 int64_t grad_stored_partials(int64_t n) {
   const int64_t T = (n + CT - 1) / CT;
   return T * (T + 1) / 2 * (GPGP_GRAD_MAXMAT + 1);
@@ -1017,10 +1152,29 @@ int64_t grad_stored_partials(int64_t n) {
 
 void grad_stored_contract(cudaStream_t s, const GradPlan &pl, int64_t n, const double *Bi, int64_t ldb,
                           const double *alpha, const double *sv, const double *D, int64_t ldd, int64_t dstride,
-                          double *part, double *g) {
+                          double *part, double *g, bool df) {
   const int64_t T = (n + CT - 1) / CT;
   const unsigned nt = (unsigned)(T * (T + 1) / 2);
   const int nm = pl.m.nmat;
+  if (df) {
+    switch (nm) {
+      case 1:
+        grad_stored_df_kernel<1><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+        break;
+      case 2:
+        grad_stored_df_kernel<2><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+        break;
+      case 3:
+        grad_stored_df_kernel<3><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+        break;
+      default:
+        grad_stored_df_kernel<0><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
+    }
+    GPGP_CHECK_LAUNCH();
+    reduce_partials_kernel<<<1, 256, 0, s>>>(part, nt, nm + 1, g);
+    GPGP_CHECK_LAUNCH();
+    return;
+  }
   switch (nm) {
     case 1:
       grad_stored_kernel<1><<<nt, 256, 0, s>>>(nm, Bi, ldb, n, alpha, sv, D, ldd, dstride, part);
@@ -1144,29 +1298,8 @@ __global__ void __launch_bounds__(256) cov_tile_df_kernel(DevKernel dk, GradMats
   double *Tt = reinterpret_cast<double *>(Fj + CT * lds);  // CT x (CT+1) staging for the mirrored write
   const int64_t ri = n - i0 < CT ? n - i0 : CT, rj = n - j0 < CT ? n - j0 : CT;
   if (g.bulk) {
-    // thread 0 issues the copies and waits for them; the block learns the outcome
-    // at the barrier (the copies' data is visible to it from there on)
-    volatile int *landed = reinterpret_cast<volatile int *>(bar + 1);
-    if (threadIdx.x == 0) {
-      const uint32_t b0 = smem_u32(bar);
-      mbar_init(b0, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      const uint32_t bytes = (uint32_t)((ri + (do_mirror ? rj : 0)) * nf * sizeof(double));
-      mbar_expect_tx(b0, bytes);
-      for (int c = 0; c < nf; ++c) {
-        bulk_g2s(smem_u32(raw + c * CT), g.F + i0 + c * g.ldf, (uint32_t)(ri * sizeof(double)), b0);
-        if (do_mirror)
-          bulk_g2s(smem_u32(raw + (nf + c) * CT), g.F + j0 + c * g.ldf, (uint32_t)(rj * sizeof(double)), b0);
-      }
-      const bool ok = mbar_wait_bounded(b0, 0);
-      if (!ok) {
-        atomicOr(g.err, 1);
-        mbar_wait_bounded(b0, 0);  // let the copies land before the block's shared memory goes
-      }
-      *landed = ok ? 1 : 0;
-    }
-    __syncthreads();
-    if (!*landed) return;
+    // a diagonal tile needs its rows once
+    if (!stage_features_bulk<CT>(raw, bar, g.F, g.ldf, i0, ri, g.F, g.ldf, j0, rj, do_mirror, nf, g.err)) return;
     for (int idx = threadIdx.x; idx < CT * nf; idx += blockDim.x) {
       const int r = idx % CT, c = idx / CT;
       Fi[r * lds + c] = r < ri ? f2_of(raw[c * CT + r]) : f2{0.0f, 0.0f};
@@ -1315,7 +1448,7 @@ void cov_matrix_df(cudaStream_t s, const DevKernel &dk, const GradPlan *pl, cons
   a.ldb = ldb;
   a.s2 = s2;
   // every bulk copy starts on a 16-byte boundary and moves a multiple of 16 bytes
-  a.bulk = (err && dk.nfeat <= 64 && ldf % 2 == 0 && n % 2 == 0 && ((uintptr_t)F & 15) == 0) ? 1 : 0;
+  a.bulk = (err && dk.nfeat <= 64 && bulk_ok(F, ldf, n)) ? 1 : 0;
   a.err = err;
   if (pl) {
     launch_cov_df<true>(s, dk, pl->m, a);

@@ -65,17 +65,13 @@ constexpr int LOOK_PANEL_SMS = 32;
 //    FP64 update of the rest of the panel's lower triangle by them;
 //  - bulk (stream y, after the chain's block): the rows below the panel,
 //    L_b = A_b W^T, and their update of the panel's remaining columns
-//    A_b,rest -= L_b L_p^T = A_b (L_p W)^T, as ONE sliced GEMM of A_b with
-//    B' = [W; -L_p W] into the block's and the remaining columns (the block's
-//    columns zeroed first, beta = 1): one split of A_b and one launch per block
-//    where a GEMM for L_b, a split of L_b and a second GEMM would be three. This
-//    bulk work is launch-bound, not compute-bound (it holds ~3% of the flops).
+//    A_b,rest -= L_b L_p^T, both sliced GEMMs.
 // x and y may be the same stream (the single-stream schedule; same products in
 // the same order, so the same factor). With two streams the bulk GEMMs take no
 // status word: the chain's diagonal kernels may set it while they run.
 void factor_panel(cudaStream_t x, cudaStream_t y, const SideStream *sd, double *A, int64_t n, int64_t lda,
                   double *Winv, double *logdet_part, int *status, int *err, int64_t k0, int64_t kbo, SplitBuf &a,
-                  SplitBuf &w, double *Bp) {
+                  SplitBuf &w, SplitBuf &lp) {
   const bool two = x != y;
   const int64_t pend = k0 + kbo;  // first row / column after the panel
   const int64_t mb = n - pend;    // rows below the panel
@@ -105,18 +101,13 @@ void factor_panel(cudaStream_t x, cudaStream_t y, const SideStream *sd, double *
     double *Ab = A + pend + j0 * lda;
     const int *sst = two ? nullptr : status;
     oz_split(y, Ab, lda, 0, mb, jb, &a.sp);
-    if (mp == 0) {
-      oz_split(y, Wb, NB, 0, jb, jb, &w.sp);
-      oz_gemm(y, a.sp, 0, w.sp, 0, mb, jb, 0, 1, 0, 1.0, 0.0, Ab, lda, false, err, sst);
-      continue;
+    oz_split(y, Wb, NB, 0, jb, jb, &w.sp);
+    oz_gemm(y, a.sp, 0, w.sp, 0, mb, jb, 0, 1, 0, 1.0, 0.0, Ab, lda, false, err, sst);
+    if (mp > 0) {
+      oz_split(y, Ab, lda, 0, mb, jb, &a.sp);
+      oz_split(y, Ap, lda, 0, mp, jb, &lp.sp);
+      oz_gemm(y, a.sp, 0, lp.sp, 0, mb, mp, 0, 1, 0, -1.0, 1.0, A + pend + (j0 + jb) * lda, lda, false, err, sst);
     }
-    // B' (jb + mp rows, ld NBO) = [W; -L_p W]
-    GPGP_CUDA(cudaMemcpy2DAsync(Bp, NBO * sizeof(double), Wb, NB * sizeof(double), jb * sizeof(double), jb,
-                                cudaMemcpyDeviceToDevice, y));
-    gemm64(y, false, false, mp, jb, jb, -1.0, Ap, lda, Wb, NB, 0.0, Bp + jb, NBO);
-    oz_split(y, Bp, NBO, 0, jb + mp, jb, &w.sp);
-    GPGP_CUDA(cudaMemset2DAsync(Ab, lda * sizeof(double), 0, mb * sizeof(double), jb, y));
-    oz_gemm(y, a.sp, 0, w.sp, 0, mb, jb + mp, 0, 1, 0, 1.0, 1.0, Ab, lda, false, err, sst);
   }
   if (two) {  // the panel is complete on x once the bulk is
     GPGP_CUDA(cudaEventRecord(sd->b, y));
@@ -129,9 +120,8 @@ void factor_panel(cudaStream_t x, cudaStream_t y, const SideStream *sd, double *
 void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv,
                  double *logdet_part, int *status, int *err, const SideStream *side) {
   SplitBuf a(s, n, NBO);   // panel operand (rows below the current block)
-  SplitBuf w(s, NBO, NB);  // B' = [W; -L_p W] of the current block
-  DBuf bp;                 // B' in FP64
-  bp.alloc(s, (size_t)NBO * NB);
+  SplitBuf w(s, NB, NB);   // inverse of the diagonal block
+  SplitBuf lp(s, NBO, NB);  // the block's rows inside the panel
   cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
   GPGP_CUDA(cudaStreamIsCapturing(s, &cap_st));
   // Per-kernel timers (tl_kt) time each launch alone, so a profiled call runs the
@@ -139,7 +129,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
   if (!side || !side->s || n <= 2 * NBO || cap_st != cudaStreamCaptureStatusNone || tl_kt) {
     for (int64_t k0 = 0; k0 < n; k0 += NBO) {
       const int64_t kbo = std::min<int64_t>(NBO, n - k0);
-      factor_panel(s, s, nullptr, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, bp.p);
+      factor_panel(s, s, nullptr, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, lp);
       const int64_t m2 = n - k0 - kbo;
       if (m2 > 0) {
         double *P = A + (k0 + kbo) + k0 * lda;
@@ -179,7 +169,7 @@ void potrf_mixed(cudaStream_t s, double *A, int64_t n, int64_t lda, double *Winv
     const int64_t kbo = std::min<int64_t>(NBO, n - k0);
     {
       OzGridCap cap(panel_cap);
-      factor_panel(x, side->s2 ? side->s2 : x, side, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, bp.p);
+      factor_panel(x, side->s2 ? side->s2 : x, side, A, n, lda, Winv, logdet_part, status, err, k0, kbo, a, w, lp);
     }
     GPGP_CUDA(cudaEventRecord(side->l, x));
     GPGP_CUDA(cudaStreamWaitEvent(s, side->l, 0));
