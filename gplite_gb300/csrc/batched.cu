@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fp64math.cuh"
 #include "model.cuh"
 
@@ -65,13 +66,40 @@ __device__ __forceinline__ double bat_kernel(int kind, double lscale, double m2,
   return m2 * (1.0 + a + a * a * (1.0 / 3.0)) * exp_fast(-a);
 }
 
+// The same in double-float arithmetic (mixed-precision plans): c1 is 1/lscale^2
+// (sexp) or sqrt(3 | 5)/lscale (Matern) as a pair; x as pairs.
+__device__ __forceinline__ f2 bat_kernel_df(int kind, f2 c1, f2 m2, const f2 *xi, const f2 *xj, int d) {
+  f2 r2 = f2{0.0f, 0.0f};
+  for (int k = 0; k < d; ++k) {
+    const f2 dh = f2_two_sum(xi[k].h, -xj[k].h);
+    const f2 df = f2_fast_two_sum(dh.h, __fadd_rn(dh.l, __fsub_rn(xi[k].l, xj[k].l)));
+    r2 = f2_fma(df, df, r2);
+  }
+  if (kind == GPGP_CF_SEXP) {
+    const f2 q = f2_mul(r2, c1);
+    return f2_mul(m2, f2_exp_neg(f2{-0.5f * q.h, -0.5f * q.l}));
+  }
+  const f2 a = f2_mul(c1, f2_sqrt(r2));
+  const f2 me = f2_mul(m2, f2_exp_neg(f2_neg(a)));
+  if (kind == GPGP_CF_MATERN32) return f2_fma(me, a, me);
+  const f2 a2_3 = f2_mul(f2_mul(a, a), f2{0x1.555556p-2f, -0x1.555556p-27f});
+  return f2_mul(me, f2_add(f2{1.0f, 0.0f}, f2_add(a, a2_3)));
+}
+
+__device__ __forceinline__ double bat_c1(int kind, double ls) {
+  return kind == GPGP_CF_SEXP ? 1.0 / (ls * ls) : (kind == GPGP_CF_MATERN32 ? sqrt(3.0) : sqrt(5.0)) / ls;
+}
+
 // B = I + s (K + jitter I) s on the lower triangle; identity on the padding.
 // With Bc given, the full symmetric B is also written there (the refinement's
 // residuals read it), the transposed tile through shared memory.
+// DF: K evaluated in double-float arithmetic (mixed-precision plans).
+template <bool DF>
 __global__ void __launch_bounds__(256) bat_cov_B_kernel(int64_t nb, int64_t dm, const double *__restrict__ X,
                                                         const double *__restrict__ prm, double jitter,
                                                         double *__restrict__ B, double *__restrict__ Bc) {
   __shared__ double xi[BT][9], xj[BT][9];
+  __shared__ f2 fxi[DF ? BT : 1][9], fxj[DF ? BT : 1][9];
   __shared__ double tile[BT][BT + 1];
   const int64_t z = blockIdx.y;
   const double *p = prm + z * PRM;
@@ -87,19 +115,36 @@ __global__ void __launch_bounds__(256) bat_cov_B_kernel(int64_t nb, int64_t dm, 
     const int r = idx % BT, k = idx / BT;
     xi[r][k] = (k < d && i0 + r < n) ? Xz[i0 + r + k * nb] : 0.0;
     xj[r][k] = (k < d && j0 + r < n) ? Xz[j0 + r + k * nb] : 0.0;
+    if (DF) {
+      fxi[r][k] = f2_of(xi[r][k]);
+      fxj[r][k] = f2_of(xj[r][k]);
+    }
   }
   __syncthreads();
   double *Bz = B + z * nb * nb;
   const int r = threadIdx.x % BT, cb = threadIdx.x / BT;
   const int64_t i = i0 + r;
+  f2 dc1 = f2{0.0f, 0.0f}, dm2 = f2{0.0f, 0.0f}, ds2 = f2{0.0f, 0.0f};
+  if (DF) {
+    dc1 = f2_of(bat_c1(kind, ls));
+    dm2 = f2_of(m2);
+    ds2 = f2_of(s * s);
+  }
   for (int q = 0; q < BT / 4; ++q) {
     const int c = cb + 4 * q;
     const int64_t j = j0 + c;
     double v;
     if (i < n && j < n) {
-      double k = bat_kernel(kind, ls, m2, &xi[r][0], 1, &xj[c][0], 1, d);
-      if (i == j) k += jitter;
-      v = s * (k * s);
+      if (DF) {
+        // s^2 (K + jitter I) as a pair; the identity added in FP64
+        f2 k = bat_kernel_df(kind, dc1, dm2, &fxi[r][0], &fxj[c][0], d);
+        if (i == j) k = f2_add(k, f2_of(jitter));
+        v = f2_to_double(f2_mul(k, ds2));
+      } else {
+        double k = bat_kernel(kind, ls, m2, &xi[r][0], 1, &xj[c][0], 1, d);
+        if (i == j) k += jitter;
+        v = s * (k * s);
+      }
       if (i == j) v += 1.0;
     } else {
       v = (i == j) ? 1.0 : 0.0;
@@ -117,13 +162,15 @@ __global__ void __launch_bounds__(256) bat_cov_B_kernel(int64_t nb, int64_t dm, 
   }
 }
 
-// R = s K(x, xt) (nb x mb per problem, zero on the padding)
+// R = s K(x, xt) (nb x mb per problem, zero on the padding); DF as above
+template <bool DF>
 __global__ void __launch_bounds__(256) bat_cross_kernel(int64_t nb, int64_t mb, int64_t dm,
                                                         const double *__restrict__ X,
                                                         const double *__restrict__ Xt,
                                                         const double *__restrict__ prm,
                                                         double *__restrict__ R) {
   __shared__ double xi[BT][9], xj[BT][9];
+  __shared__ f2 fxi[DF ? BT : 1][9], fxj[DF ? BT : 1][9];
   const int64_t z = blockIdx.z;
   const double *p = prm + z * PRM;
   const int n = (int)p[0], m = (int)p[1], d = (int)p[2], kind = (int)p[3];
@@ -134,17 +181,32 @@ __global__ void __launch_bounds__(256) bat_cross_kernel(int64_t nb, int64_t mb, 
     const int r = idx % BT, k = idx / BT;
     xi[r][k] = (k < d && i0 + r < n) ? Xz[i0 + r + k * nb] : 0.0;
     xj[r][k] = (k < d && j0 + r < m) ? Tz[j0 + r + k * mb] : 0.0;
+    if (DF) {
+      fxi[r][k] = f2_of(xi[r][k]);
+      fxj[r][k] = f2_of(xj[r][k]);
+    }
   }
   __syncthreads();
   double *Rz = R + z * nb * mb;
   const int r = threadIdx.x % BT, cb = threadIdx.x / BT;
   const int64_t i = i0 + r;
   if (i >= nb) return;
+  f2 dc1 = f2{0.0f, 0.0f}, dm2 = f2{0.0f, 0.0f}, ds = f2{0.0f, 0.0f};
+  if (DF) {
+    dc1 = f2_of(bat_c1(kind, ls));
+    dm2 = f2_of(m2);
+    ds = f2_of(s);
+  }
   for (int q = 0; q < BT / 4; ++q) {
     const int64_t j = j0 + cb + 4 * q;
     if (j >= mb) continue;
     double v = 0.0;
-    if (i < n && j < m) v = s * bat_kernel(kind, ls, m2, &xi[r][0], 1, &xj[cb + 4 * q][0], 1, d);
+    if (i < n && j < m) {
+      if (DF)
+        v = f2_to_double(f2_mul(ds, bat_kernel_df(kind, dc1, dm2, &fxi[r][0], &fxj[cb + 4 * q][0], d)));
+      else
+        v = s * bat_kernel(kind, ls, m2, &xi[r][0], 1, &xj[cb + 4 * q][0], 1, d);
+    }
     Rz[i + j * nb] = v;
   }
 }
@@ -404,13 +466,20 @@ void run_bucket(gpgp_batch *b, Bucket &k, cudaStream_t st) {
   {
     const int64_t T = nb / BT;
     dim3 g((unsigned)(T * (T + 1) / 2), (unsigned)P);
-    bat_cov_B_kernel<<<g, 256, 0, st>>>(nb, k.dm, k.X.p, k.prm.p, b->jitter, k.Bm.p,
-                                        k.variant >= 1 ? k.Bc.p : nullptr);
+    if (b->precision == GPGP_PREC_MIXED)
+      bat_cov_B_kernel<true><<<g, 256, 0, st>>>(nb, k.dm, k.X.p, k.prm.p, b->jitter, k.Bm.p,
+                                                k.variant >= 1 ? k.Bc.p : nullptr);
+    else
+      bat_cov_B_kernel<false><<<g, 256, 0, st>>>(nb, k.dm, k.X.p, k.prm.p, b->jitter, k.Bm.p,
+                                                 k.variant >= 1 ? k.Bc.p : nullptr);
     GPGP_CHECK_LAUNCH();
   }
   {
     dim3 g((unsigned)(nb / BT), (unsigned)((mb + BT - 1) / BT), (unsigned)P);
-    bat_cross_kernel<<<g, 256, 0, st>>>(nb, mb, k.dm, k.X.p, k.Xt.p, k.prm.p, k.R.p);
+    if (b->precision == GPGP_PREC_MIXED)
+      bat_cross_kernel<true><<<g, 256, 0, st>>>(nb, mb, k.dm, k.X.p, k.Xt.p, k.prm.p, k.R.p);
+    else
+      bat_cross_kernel<false><<<g, 256, 0, st>>>(nb, mb, k.dm, k.X.p, k.Xt.p, k.prm.p, k.R.p);
     GPGP_CHECK_LAUNCH();
   }
   // Cholesky of B
