@@ -1639,7 +1639,9 @@ void cov_matvec_df(cudaStream_t s, const DevKernel &dk, uint32_t gmask, const do
     return 1;
   });
   const int64_t T1 = (n1 + CT - 1) / CT, T2 = std::max<int64_t>(1, (n2 + CT - 1) / CT);
-  const int64_t want = std::max<int64_t>(1, (2 * device_sms() + T1 - 1) / T1);
+  // four blocks per SM: the pair arithmetic needs the warps to hide its latency
+  // (two per SM left the FP32 pipe at 56%)
+  const int64_t want = std::max<int64_t>(1, (4 * device_sms() + T1 - 1) / T1);
   const int64_t tpr = (T2 + std::min(want, T2) - 1) / std::min(want, T2);
   const int64_t nrange = (T2 + tpr - 1) / tpr;
   double *dst = out, *part = nullptr;
