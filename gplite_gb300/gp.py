@@ -358,6 +358,8 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     if gp.lik.kind in ("binomial", "betabinom") and trials is None:
         raise ValueError("trials must be provided for the %s likelihood." %
                          ("binomial" if gp.lik.kind == "binomial" else "beta binomial"))
+    if grad and (gp.lik.kind != "gaussian" or gp.method.kind != "full"):
+        raise ValueError("the energy gradient needs lik_gaussian and method_full")
     learn_scales(gp, x)
     lib = L.load()
     ctx = L.default_context(device)
@@ -388,8 +390,6 @@ def gp_fit(gp, x, y, trials=None, offset=None, jitter=None, precision="fp64", de
     gp._free()
     graw = None
     if grad:
-        if gp.lik.kind != "gaussian" or gp.method.kind != "full":
-            raise ValueError("the energy gradient needs lik_gaussian and method_full")
         gt = np.zeros(len(_flat_terms(gp)) * L.TERM_NPARAM)
         gs = C.c_double(0.0)
         st = lib.gpgp_fit_grad(ctx.h, C.byref(k), C.byref(lk), C.byref(me), C.byref(ap), C.byref(op), L.ptr(xf),

@@ -97,3 +97,15 @@ def test_stale_fit_is_refused_before_any_device_call():
                  lambda: G.gp_energy(gp)):
         with pytest.raises(RuntimeError, match="refit"):
             call()
+
+
+def test_fit_with_gradient_needs_gaussian_full_before_any_device_call():
+    """gp_fit(..., grad=True) (the fit and its energy gradient in one call) exists for
+    lik_gaussian with method_full only, like gp_energy_grad; other models are refused on
+    the host, before a context or the library is touched."""
+    import pytest
+    x, y = np.zeros((4, 1)), np.zeros(4)
+    for gp in (G.gp_init(G.cf_sexp(), G.lik_bernoulli()),
+               G.gp_init(G.cf_sexp(), G.lik_gaussian(), method=G.method_fitc(num_inducing=2))):
+        with pytest.raises(ValueError, match="lik_gaussian and method_full"):
+            G.gp_fit(gp, x, y, grad=True)
